@@ -1,0 +1,361 @@
+"""Benchmark: CG solves/sec to a 1e-8 true relative residual on the 512 x 512 variable-diffusion family.
+
+Workload (one step): the 256 held-out instances of the 2-D variable-coefficient diffusion family
+(5-point CSR, n = 262,144, Matern-3/2 log-coefficient fields, seeds 5000-5255, b ~ N(0,1)), all
+solved in one batched call to |b - A x| / |b| <= 1e-8 measured in FP64.  The headline method is
+FP32 preconditioned CG inside FP64 iterative refinement with the learned FSAI preconditioner
+(Jacobi fallback); plain CG and Jacobi-PCG run through the same kernel for comparison.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--method M]
+
+--impl reference times the reference's CG loop (restated with the same torch CPU ops, float64,
+Jacobi preconditioner, tol giving the same 1e-8 residual) on the host cores over a bounded sample.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+import torch
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "CG solves/sec to 1e-8 rel. residual: learned mixed-prec PCG vs plain CG, 1 GB300"
+UNIT = "solves/s"
+WORKLOAD = "diffusion2d-512x512-family-test256"
+TEST_SEEDS0 = 5000
+SYSTEMS = 256
+M = 512
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return None
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(v: float, world: int) -> float:
+    if world == 1:
+        return v
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def bytes_per_system_iter(n, nnz, method):
+    """Algorithmic HBM bytes of one FP32 PCG step of one system: CSR values (the pattern is shared by
+    the batch and read from L2) + 6 vector streams (p read, x r/w, r r/w, p write) + preconditioner."""
+    b = nnz * 4 + 6 * n * 4
+    if method == "jacobi":
+        b += n * 4
+    elif method == "learned":
+        b += 2 * (nnz // 2 + n // 2 + 1) * 4 + 2 * n * 4  # G and G^T values (lower pattern) + the t vector
+    return b
+
+
+def bytes_per_sweep(n, nnz):
+    """FP64 refinement: residual b - A x (values + x, b read, r write) and x += |r| d (x r/w, d read)."""
+    return nnz * 4 + 3 * n * 8 + 2 * n * 8 + n * 4
+
+
+def make_preconditioner(method, fam, coeff, dev):
+    if method != "learned":
+        return None
+    from cola_gb300.precond import learned_fsai
+    return learned_fsai.preconditioner_for(fam, coeff)
+
+
+def run_ours(args, world, rank, local):
+    import cola_gb300 as cola
+    from cola_gb300 import _capi
+    from cola_gb300.linalg.batched import solve_batched
+    from cola_gb300.workloads import diffusion_family_2d
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    _capi.load()
+    seeds = range(TEST_SEEDS0 + rank * args.systems, TEST_SEEDS0 + (rank + 1) * args.systems)
+    fam, B, coeff, _ = diffusion_family_2d(seeds, m=args.m, device=dev)
+    n, nnz = fam.n, fam.indices.numel()
+    method = args.method
+    fsai = None
+    if method == "learned":
+        try:
+            fsai = make_preconditioner(method, fam, coeff, dev)
+        except Exception as e:  # learned weights missing: report and fall back to Jacobi
+            print(f"# learned preconditioner unavailable ({e}); timing jacobi", file=sys.stderr)
+            method = "jacobi"
+    prec = {"plain": "none", "jacobi": "jacobi", "learned": "fsai"}[method]
+    kw = dict(precond=prec, tol=1e-8, inner_tol=args.inner_tol, fsai=fsai)
+    st = torch.cuda.current_stream(dev)
+
+    def step():
+        return solve_batched(fam, B, **kw)
+
+    for _ in range(args.warmup):
+        X, info = step()
+    torch.cuda.synchronize()
+    barrier(world)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    iters_total = 0
+    sweeps = []
+    with Clocks(local) as clk:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            ev[i][0].record(st)
+            X, info = step()
+            ev[i][1].record(st)
+            iters_total += int(info["iterations"].sum().item())
+            sweeps.append(info["sweeps"])
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    barrier(world)
+    ms = [a.elapsed_time(b) for a, b in ev]
+    t_dev = sum(ms) / 1e3
+    t_max = max_over_ranks(t_dev, world)
+    relres_max = float(info["relres"].max().item())
+    status_ok = bool(torch.all((info["status"] == 1) | (info["status"] == 5)).item())
+    value = world * args.systems * args.steps / t_max
+
+    # end to end through the public API from pinned host buffers: H2D of the family values and the
+    # right-hand sides, the solve, D2H of the solutions
+    vals_h = fam.values.cpu().pin_memory()
+    B_h = B.cpu().pin_memory()
+    X_h = torch.empty_like(B_h).pin_memory()
+    e2e_steps = max(1, min(args.steps, 2))
+    from cola_gb300.linalg.batched import BatchedCSR
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(e2e_steps):
+        vals_d = vals_h.to(dev, non_blocking=True)
+        B_d = B_h.to(dev, non_blocking=True)
+        Xd, _ = solve_batched(BatchedCSR(fam.indptr, fam.indices, vals_d), B_d, **kw)
+        X_h.copy_(Xd, non_blocking=True)
+    e1.record(st)
+    torch.cuda.synchronize()
+    t_e2e = max_over_ranks(e0.elapsed_time(e1) / 1e3, world)
+    e2e = {"value": world * args.systems * e2e_steps / t_e2e, "unit": UNIT,
+           "h2d_bytes_per_step": vals_h.numel() * 4 + B_h.numel() * 8, "d2h_bytes_per_step": X_h.numel() * 8}
+
+    peak, peak_kind = peaks()
+    alg_bytes_step = (iters_total / args.steps) * bytes_per_system_iter(n, nnz, method) + \
+        (statistics.mean(sweeps) * args.systems) * bytes_per_sweep(n, nnz)
+    achieved = alg_bytes_step / (t_dev / args.steps) / 1e9
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32-inner/f64-refinement", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "systems_per_gpu": args.systems, "grid": f"{args.m}x{args.m}", "n": n,
+                   "nnz": nnz, "method": method, "tol": 1e-8, "inner_tol": args.inner_tol,
+                   "l2": "inputs larger than L2 (values + vectors > 1 GB per step)", "parallelism": f"replicas{world}"},
+        "quality": {"max_true_relres_fp64": relres_max, "all_converged": status_ok,
+                    "mean_inner_iters_per_system": iters_total / args.steps / args.systems,
+                    "sweeps": statistics.mean(sweeps)},
+        "e2e": e2e,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                     "kernel": "k_batched_ir", "alg_bytes_per_launch": alg_bytes_step},
+        "gpu_launches": args.steps * ((args.systems + 1023) // 1024),
+        "wall_s_timed": wall,
+    }
+    clk_s = clk.summary()
+    if clk_s:
+        out["clocks"] = clk_s
+    if args.compare and rank == 0:
+        cmp = {}
+        for mth in args.compare.split(","):
+            if mth == method:
+                continue
+            p2 = {"plain": "none", "jacobi": "jacobi", "learned": "fsai"}[mth]
+            if mth == "learned" and fsai is None:
+                continue
+            kw2 = dict(precond=p2, tol=1e-8, inner_tol=args.inner_tol, fsai=fsai)
+            solve_batched(fam, B, **kw2)
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(st)
+            _, inf2 = solve_batched(fam, B, **kw2)
+            b.record(st)
+            torch.cuda.synchronize()
+            t2 = a.elapsed_time(b) / 1e3
+            cmp[mth] = {"value": args.systems / t2, "unit": UNIT,
+                        "mean_inner_iters_per_system": float(inf2["iterations"].double().mean().item()),
+                        "max_true_relres_fp64": float(inf2["relres"].max().item())}
+        out["compare"] = cmp
+        if "plain" in cmp:
+            out["speedup_vs_plain_cg"] = value / world / cmp["plain"]["value"]
+    if rank == 0 and args.cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(args, fam, B, sample_s=args.cpu_seconds)
+    return out
+
+
+def cpu_baseline(args, fam, B, sample_s=15.0):
+    """The reference CG loop (torch CPU ops, float64, Jacobi preconditioner) on a bounded sample of the
+    same instances, all host threads."""
+    from oracle.torch_ref import csr_matmat, run_batched_cg
+    threads = os.cpu_count() or 1
+    torch.set_num_threads(threads)
+    indptr, indices = fam.indptr.cpu(), fam.indices.cpu()
+    n = fam.n
+    done, t_used, iters = 0, 0.0, []
+    s = 0
+    while t_used < sample_s and s < fam.num_systems:
+        vals = fam.values[s].double().cpu()
+        mm = csr_matmat(indptr, indices, vals, n)
+        dg = torch.zeros(n, dtype=torch.float64)
+        rows = torch.repeat_interleave(torch.arange(n), (indptr[1:] - indptr[:-1]).long())
+        dg.index_add_(0, rows, torch.where(rows == indices.long(), vals, torch.zeros_like(vals)))
+        dinv = (1.0 / dg)[:, None]
+        b = B[s].double().cpu()[:, None]
+        t0 = time.perf_counter()
+        # stop rule |r_rec| <= 2 tol on the normalised system; tol = 5e-9 targets a 1e-8 residual
+        x, k, _ = run_batched_cg(mm, b, torch.zeros_like(b), 100000, 5e-9, precond=lambda r: dinv * r)
+        t_used += time.perf_counter() - t0
+        iters.append(k)
+        done += 1
+        s += 1
+    return {"value": done / t_used, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{done} of the {fam.num_systems} instances, reference CG loop on torch CPU ops, float64, "
+                      f"Jacobi P, tol 5e-9 (true relres ~1e-8), {statistics.mean(iters):.0f} iterations each",
+            "seconds": t_used}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return None
+    from cola_gb300.workloads import diffusion_family_2d
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    fam, B, _, _ = diffusion_family_2d(range(TEST_SEEDS0, TEST_SEEDS0 + max(1, args.ref_systems)), m=args.m,
+                                       device=dev)
+    vals = []
+    cb = None
+    for _ in range(args.warmup if args.warmup < 1 else 0):
+        pass
+    for _ in range(args.steps):
+        cb = cpu_baseline(args, fam, B, sample_s=args.ref_seconds)
+        vals.append(cb["value"])
+    v = statistics.mean(vals)
+    return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": WORKLOAD, "grid": f"{args.m}x{args.m}", "method": "jacobi-cg (reference loop)",
+                       "tol": 1e-8},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cb["cores"], "kind": "port", "sample": cb["sample"]},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--method", default="learned", choices=["learned", "jacobi", "plain"])
+    ap.add_argument("--compare", default="plain,jacobi")
+    ap.add_argument("--systems", type=int, default=SYSTEMS)
+    ap.add_argument("--m", type=int, default=M)
+    ap.add_argument("--inner-tol", type=float, default=1e-4)
+    ap.add_argument("--cpu-baseline", type=int, default=1)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--ref-seconds", type=float, default=20.0)
+    ap.add_argument("--ref-systems", type=int, default=4)
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        out = run_reference(args, world, rank)
+    else:
+        out = run_ours(args, world, rank, local)
+    if rank == 0 and out is not None:
+        print(json.dumps(out))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

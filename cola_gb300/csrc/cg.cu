@@ -1,0 +1,813 @@
+// Conjugate gradients (cola/linalg/inverse/cg.py) on sm_103a.
+//
+// Reference loop (run_batched_cg, cg.py:94-119; take_cg_step :141-154):
+//   mult = |b|_col ; b <- b / mult (safe division, :96-97)
+//   r0 = b - A x0 ; z0 = P r0 ; p0 = z0 ; gamma0 = <r0, z0>              (initialize :122-130)
+//   tol_eff = tol * |r0| + tol                                           (:101)
+//   while any(|r| > tol_eff) and k < max_iters:                          (cond_fun :133-138)
+//     conv = |r| < 1e-40 ; Ap = A p ; alpha = gamma / <p, Ap> (0 if conv) (:143-147, :157-162)
+//     x += alpha p ; r -= alpha Ap ; z = P r                             (:148-150)
+//     gamma' = <r, z> ; beta = gamma' / gamma (0 if conv) ; p = z + beta p (:151-152, :165-170)
+//   return x * mult                                                      (:119)
+// Divisions use do_safe_div (:173-178): |denominator| < 1e-40 is replaced by 1e-40.
+//
+// Two executions of that loop:
+//   * fused: one cooperative persistent kernel runs the whole solve for a Dense or CSR operator
+//     (optionally + c*I) with P = identity or Diagonal; three bounded grid barriers per step.
+//   * generic: any operator program / preconditioner; four launches per step, the stop test is
+//     evaluated on the device and the host polls it every `check_every` steps (the reference
+//     syncs twice per step, torch_tqdm.py:42 and cg.py:136).
+// Column sums are reduced in a fixed order so every CTA derives bit-identical alpha / beta.
+#include <cmath>
+#include <type_traits>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "ops.cuh"
+
+namespace colagb {
+
+template <class T> struct SmallValue;
+template <> struct SmallValue<float> { static constexpr float v = 1e-40f; };
+template <> struct SmallValue<double> { static constexpr double v = 1e-40; };
+
+template <class T>
+__device__ __forceinline__ T safe_div(T num, T den) {
+  const T eps = SmallValue<T>::v;
+  return num / (fabs(den) < eps ? eps : den);
+}
+
+template <class T>
+__device__ __forceinline__ T ldcg(const T* p) { return __ldcg(p); }
+
+// ---------------------------------------------------------------------------------------------
+// Column reductions.  Threads of a block are arranged as (rows_per_pass x kc) with kc = min(k, 256);
+// f(i, c) is evaluated for every owned unit and summed per column; the block writes partials[c].
+template <class T, class F>
+__device__ __forceinline__ void block_col_partials(int64_t row_base, int64_t row_end, int64_t bidx, int64_t nblk,
+                                                   int64_t k, F f, T* partials_out, T* smem) {
+  // rows row_base + bidx*rpp + my_r, stepping rpp*nblk; bidx/nblk = (blockIdx, gridDim) for a
+  // grid-stride sweep or (0, 1) for a block-private row range.
+  const int t = threadIdx.x;
+  for (int64_t c0 = 0; c0 < k; c0 += blockDim.x) {
+    const int kc = (int)((k - c0) < (int64_t)blockDim.x ? (k - c0) : (int64_t)blockDim.x);
+    const int rpp = blockDim.x / kc;
+    const int my_c = t % kc, my_r = t / kc;
+    T acc = T(0);
+    if (my_r < rpp) {
+      const int64_t c = c0 + my_c;
+      for (int64_t i = row_base + bidx * rpp + my_r; i < row_end; i += (int64_t)rpp * nblk) acc += f(i, c);
+    }
+    smem[t] = acc;
+    __syncthreads();
+    if (t < kc) {
+      T s = T(0);
+      for (int q = 0; q < rpp; ++q) s += smem[q * kc + t];
+      partials_out[c0 + t] = s;
+    }
+    __syncthreads();
+  }
+}
+
+// Fixed-order sum of partials[b * k + c] over b < nb (reads bypass L1).
+template <class T>
+__device__ __forceinline__ T sum_partials(const T* partials, int nb, int64_t k, int64_t c) {
+  T s = T(0);
+  for (int b = 0; b < nb; ++b) s += ldcg(partials + (int64_t)b * k + c);
+  return s;
+}
+
+__device__ __forceinline__ bool is_last_block(unsigned int* counter) {
+  __shared__ int s_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (s_last) __threadfence();
+  return s_last != 0;
+}
+
+// ---------------------------------------------------------------------------------------------
+// State of one solve in device memory
+template <class T>
+struct CgScalars {
+  T* mult;     // |b| per column
+  T* tol_eff;  // tol * |r0| + tol
+  T* gamma;    // <r, z>
+  T* alpha;
+  T* beta;
+  T* rnorm;    // |r|
+  int* conv;   // |r| < 1e-40 at the start of the current step
+  int* done;   // loop finished
+  int* iters;  // k
+  T* pA;       // partials [nb][k] for <p, Ap> / |b|
+  T* pB;       // partials [nb][k] for <r, z>
+  T* pC;       // partials [nb][k] for |r|^2
+  unsigned int* counters;  // 4 last-block counters
+};
+
+// ---------------------------------------------------------------------------------------------
+// generic-path kernels (grid = nb blocks of 256 threads)
+
+template <class T>
+__global__ void __launch_bounds__(256) k_colnorm_b(const T* B, int64_t ldb, int64_t n, int64_t k, CgScalars<T> s) {
+  __shared__ T smem[256];
+  block_col_partials<T>(0, n, blockIdx.x, gridDim.x, k,
+                        [&](int64_t i, int64_t c) { const T v = B[i * ldb + c]; return v * v; },
+                        s.pA + (int64_t)blockIdx.x * k, smem);
+  if (is_last_block(s.counters + 0)) {
+    for (int64_t c = threadIdx.x; c < k; c += blockDim.x) s.mult[c] = sqrt(sum_partials(s.pA, gridDim.x, k, c));
+    if (threadIdx.x == 0) s.counters[0] = 0;
+  }
+}
+
+// r = b / mult
+template <class T>
+__global__ void k_scale_b(const T* B, int64_t ldb, T* R, int64_t n, int64_t k, CgScalars<T> s) {
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n * k; u += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = u / k, c = u - i * k;
+    R[u] = safe_div(B[i * ldb + c], s.mult[c]);
+  }
+}
+
+// p = z (z = dinv*r, r, or Z); partials <r,z>, |r|^2; last block: gamma, rnorm, tol_eff, done
+template <class T, int PK>
+__global__ void __launch_bounds__(256) k_init(const T* R, const T* Z, const T* dinv, T* P, int64_t n, int64_t k,
+                                              double tol, int max_iters, T* hist, CgScalars<T> s) {
+  __shared__ T smem[256];
+  block_col_partials<T>(0, n, blockIdx.x, gridDim.x, k,
+                        [&](int64_t i, int64_t c) {
+                          const T r = R[i * k + c];
+                          const T z = PK == 0 ? r : (PK == 1 ? dinv[i] * r : Z[i * k + c]);
+                          P[i * k + c] = z;
+                          return r * z;
+                        },
+                        s.pB + (int64_t)blockIdx.x * k, smem);
+  block_col_partials<T>(0, n, blockIdx.x, gridDim.x, k,
+                        [&](int64_t i, int64_t c) { const T r = R[i * k + c]; return r * r; },
+                        s.pC + (int64_t)blockIdx.x * k, smem);
+  if (is_last_block(s.counters + 1)) {
+    __shared__ int s_any;
+    __shared__ T s_mean;
+    if (threadIdx.x == 0) { s_any = 0; s_mean = T(0); }
+    __syncthreads();
+    for (int64_t c = threadIdx.x; c < k; c += blockDim.x) {
+      const T g = sum_partials(s.pB, gridDim.x, k, c);
+      const T rn = sqrt(sum_partials(s.pC, gridDim.x, k, c));
+      s.gamma[c] = g;
+      s.rnorm[c] = rn;
+      s.alpha[c] = T(0);
+      s.beta[c] = T(0);
+      const T te = (T)tol * rn + (T)tol;
+      s.tol_eff[c] = te;
+      if (rn > te) atomicOr(&s_any, 1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      T m = T(0);
+      for (int64_t c = 0; c < k; ++c) m += s.rnorm[c];
+      if (hist) hist[0] = m / (T)k;
+      *s.iters = 0;
+      *s.done = !(s_any && 0 < max_iters);
+      s.counters[1] = 0;
+    }
+  }
+}
+
+// <p, Ap> partials; last block: conv flags and alpha
+template <class T>
+__global__ void __launch_bounds__(256) k_alpha(const T* P, const T* AP, int64_t n, int64_t k, CgScalars<T> s) {
+  if (*s.done) return;
+  __shared__ T smem[256];
+  block_col_partials<T>(0, n, blockIdx.x, gridDim.x, k,
+                        [&](int64_t i, int64_t c) { return P[i * k + c] * AP[i * k + c]; },
+                        s.pA + (int64_t)blockIdx.x * k, smem);
+  if (is_last_block(s.counters + 2)) {
+    for (int64_t c = threadIdx.x; c < k; c += blockDim.x) {
+      const int cv = s.rnorm[c] < SmallValue<T>::v;
+      s.conv[c] = cv;
+      const T a = safe_div(s.gamma[c], sum_partials(s.pA, gridDim.x, k, c));
+      s.alpha[c] = cv ? T(0) : a;
+    }
+    if (threadIdx.x == 0) s.counters[2] = 0;
+  }
+}
+
+// x += alpha p ; r -= alpha Ap ; (PK 0/1: z from r) partials <r,z>, |r|^2 ; last block: beta, stop test.
+// PK == 2 (general P): only x, r and |r|^2 here; <r, z> comes from k_gamma after z = P r.
+template <class T, int PK>
+__global__ void __launch_bounds__(256) k_update(T* X, int64_t ldx, T* R, const T* P, const T* AP, const T* dinv,
+                                                int64_t n, int64_t k, int max_iters, T* hist, CgScalars<T> s) {
+  if (*s.done) return;
+  __shared__ T smem[256];
+  block_col_partials<T>(0, n, blockIdx.x, gridDim.x, k,
+                        [&](int64_t i, int64_t c) {
+                          const T a = s.alpha[c];
+                          X[i * ldx + c] += a * P[i * k + c];
+                          const T r = R[i * k + c] - a * AP[i * k + c];
+                          R[i * k + c] = r;
+                          return r * r;
+                        },
+                        s.pC + (int64_t)blockIdx.x * k, smem);
+  if (PK != 2)
+    block_col_partials<T>(0, n, blockIdx.x, gridDim.x, k,
+                          [&](int64_t i, int64_t c) {
+                            const T r = R[i * k + c];
+                            return r * (PK == 0 ? r : dinv[i] * r);
+                          },
+                          s.pB + (int64_t)blockIdx.x * k, smem);
+  if (PK == 2) {
+    if (is_last_block(s.counters + 3)) {
+      for (int64_t c = threadIdx.x; c < k; c += blockDim.x) s.rnorm[c] = sqrt(sum_partials(s.pC, gridDim.x, k, c));
+      if (threadIdx.x == 0) s.counters[3] = 0;
+    }
+    return;
+  }
+  if (is_last_block(s.counters + 3)) {
+    __shared__ int s_any;
+    if (threadIdx.x == 0) s_any = 0;
+    __syncthreads();
+    for (int64_t c = threadIdx.x; c < k; c += blockDim.x) {
+      const T g1 = sum_partials(s.pB, gridDim.x, k, c);
+      const T b = safe_div(g1, s.gamma[c]);
+      s.beta[c] = s.conv[c] ? T(0) : b;
+      s.gamma[c] = g1;
+      const T rn = sqrt(sum_partials(s.pC, gridDim.x, k, c));
+      s.rnorm[c] = rn;
+      if (rn > s.tol_eff[c]) atomicOr(&s_any, 1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const int it = *s.iters + 1;
+      *s.iters = it;
+      if (hist) {
+        T m = T(0);
+        for (int64_t c = 0; c < k; ++c) m += s.rnorm[c];
+        hist[it] = m / (T)k;
+      }
+      *s.done = !(s_any && it < max_iters);
+      s.counters[3] = 0;
+    }
+  }
+}
+
+// general P: <r, z> partials with z = P r already formed; last block: beta, stop test
+template <class T>
+__global__ void __launch_bounds__(256) k_gamma(const T* R, const T* Z, int64_t n, int64_t k, int max_iters, T* hist,
+                                               CgScalars<T> s) {
+  if (*s.done) return;
+  __shared__ T smem[256];
+  block_col_partials<T>(0, n, blockIdx.x, gridDim.x, k,
+                        [&](int64_t i, int64_t c) { return R[i * k + c] * Z[i * k + c]; },
+                        s.pB + (int64_t)blockIdx.x * k, smem);
+  if (is_last_block(s.counters + 2)) {
+    __shared__ int s_any;
+    if (threadIdx.x == 0) s_any = 0;
+    __syncthreads();
+    for (int64_t c = threadIdx.x; c < k; c += blockDim.x) {
+      const T g1 = sum_partials(s.pB, gridDim.x, k, c);
+      const T b = safe_div(g1, s.gamma[c]);
+      s.beta[c] = s.conv[c] ? T(0) : b;
+      s.gamma[c] = g1;
+      if (s.rnorm[c] > s.tol_eff[c]) atomicOr(&s_any, 1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const int it = *s.iters + 1;
+      *s.iters = it;
+      if (hist) {
+        T m = T(0);
+        for (int64_t c = 0; c < k; ++c) m += s.rnorm[c];
+        hist[it] = m / (T)k;
+      }
+      *s.done = !(s_any && it < max_iters);
+      s.counters[2] = 0;
+    }
+  }
+}
+
+// p = z + beta p   (z = r, dinv*r or Z)
+// Skipped once `done` is set: p is not read after the last step.
+template <class T, int PK>
+__global__ void k_pupdate(T* P, const T* R, const T* Z, const T* dinv, int64_t n, int64_t k, CgScalars<T> s,
+                          const int* done) {
+  if (*done) return;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n * k; u += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = u / k, c = u - i * k;
+    const T r = R[u];
+    const T z = PK == 0 ? r : (PK == 1 ? dinv[i] * r : Z[u]);
+    P[u] = z + s.beta[c] * P[u];
+  }
+}
+
+template <class T>
+__global__ void k_scale_x(T* X, int64_t ldx, int64_t n, int64_t k, CgScalars<T> s) {
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n * k; u += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = u / k, c = u - i * k;
+    X[i * ldx + c] *= s.mult[c];
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// fused persistent kernel
+
+template <class T, class S>
+struct FusedArgs {
+  int kind;            // COLAGB_OP_DENSE or COLAGB_OP_CSR
+  const S* vals;       // dense matrix or CSR values
+  int64_t lda;
+  const int32_t* indptr;
+  const int32_t* indices;
+  T shift;             // A + shift * I
+  const T* dinv;       // Jacobi diagonal (PK == 1)
+  const T* B;
+  int64_t ldb;
+  T* X;
+  int64_t ldx;
+  T* R;
+  T* P;
+  T* AP;
+  int64_t n, k;
+  double tol;
+  int max_iters;
+  int vec4;            // dense rows and the vector are 16-byte aligned and n % 4 == 0
+  T* hist;
+  CgScalars<T> s;
+  GridBarrier gb;
+};
+
+// OUT[i, c] = shift * V[i, c] + (A V)[i, c] for the CTA's rows [r0, r1) and all k columns.
+// CSR: one thread per (row, column) unit.  Dense: one warp per row, lanes stride the row
+// (128-bit loads when the row is 16-byte aligned).  Ends with __syncthreads so the CTA can read
+// OUT back.
+template <class T, class S>
+__device__ __forceinline__ void own_matvec(const FusedArgs<T, S>& a, const T* V, T* OUT, int64_t r0, int64_t r1) {
+  const int64_t k = a.k, n = a.n;
+  if (a.kind == COLAGB_OP_CSR) {
+    for (int64_t u = threadIdx.x; u < (r1 - r0) * k; u += blockDim.x) {
+      const int64_t i = r0 + u / k, c = u % k;
+      T acc = a.shift * V[i * k + c];
+      const int32_t b = a.indptr[i], e = a.indptr[i + 1];
+      for (int32_t j = b; j < e; ++j) acc += cvt<T>(a.vals[j]) * V[(int64_t)a.indices[j] * k + c];
+      OUT[i * k + c] = acc;
+    }
+  } else {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int64_t i = r0 + warp; i < r1; i += nw) {
+      const S* row = a.vals + i * a.lda;
+      for (int64_t c = 0; c < k; ++c) {
+        T acc = T(0);
+        if constexpr (std::is_same<S, float>::value && std::is_same<T, float>::value) {
+          if (a.vec4 && k == 1) {
+            const float4* r4 = reinterpret_cast<const float4*>(row);
+            const float4* v4 = reinterpret_cast<const float4*>(V);
+            for (int64_t j = lane; j < n / 4; j += 32) {
+              const float4 av = r4[j], vv = v4[j];
+              acc += av.x * vv.x + av.y * vv.y + av.z * vv.z + av.w * vv.w;
+            }
+          } else {
+            for (int64_t j = lane; j < n; j += 32) acc += row[j] * V[j * k + c];
+          }
+        } else {
+          for (int64_t j = lane; j < n; j += 32) acc += cvt<T>(row[j]) * V[j * k + c];
+        }
+        acc = warp_sum(acc);
+        if (lane == 0) OUT[i * k + c] = acc + a.shift * V[i * k + c];
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// Every CTA computes the column totals itself from the per-CTA partials (same order everywhere).
+template <class T>
+__device__ __forceinline__ void all_totals(const T* partials, int nb, int64_t k, T* out_smem) {
+  for (int64_t c = threadIdx.x; c < k; c += blockDim.x) out_smem[c] = sum_partials(partials, nb, k, c);
+  __syncthreads();
+}
+
+template <class T, class S, int PK>
+__global__ void __launch_bounds__(256) k_cg_fused(FusedArgs<T, S> a) {
+  extern __shared__ unsigned char smem_raw[];
+  T* red = reinterpret_cast<T*>(smem_raw);           // 256 reduction slots
+  T* tot1 = red + 256;                                // k column totals
+  T* tot2 = tot1 + a.k;                               // k column totals
+  T* alpha = tot2 + a.k;                              // k
+  T* beta = alpha + a.k;                              // k
+  T* gamma = beta + a.k;                              // k
+  T* tol_eff = gamma + a.k;                           // k
+  T* mult = tol_eff + a.k;                            // k
+  int* conv = reinterpret_cast<int*>(mult + a.k);     // k
+  __shared__ int s_any;
+
+  const int64_t n = a.n, k = a.k;
+  const int nb = gridDim.x;
+  const int64_t rows_per_block = ceil_div(n, nb);
+  const int64_t r0 = (int64_t)blockIdx.x * rows_per_block;
+  const int64_t r1 = (r0 + rows_per_block < n) ? r0 + rows_per_block : n;
+  const int64_t kc = k < 256 ? k : 256;
+  T* pA = a.s.pA + (int64_t)blockIdx.x * k;
+  T* pB = a.s.pB + (int64_t)blockIdx.x * k;
+  T* pC = a.s.pC + (int64_t)blockIdx.x * k;
+  (void)kc;
+
+  // row-range iteration helper: f(i, c) over owned units, summed per column into `part`
+  auto own_partials = [&](auto f, T* part) { block_col_partials<T>(r0, r1, 0, 1, k, f, part, red); };
+
+  // ---- init: mult = |b| ----
+  own_partials([&](int64_t i, int64_t c) { const T v = a.B[i * a.ldb + c]; return v * v; }, pA);
+  if (!grid_sync(a.gb)) return;
+  all_totals(a.s.pA, nb, k, tot1);
+  for (int64_t c = threadIdx.x; c < k; c += blockDim.x) mult[c] = sqrt(tot1[c]);
+  __syncthreads();
+  // r = b / mult - A x0 (x0 gathered through P as scratch: P <- x0 first)
+  for (int64_t i = r0; i < r1; ++i)
+    for (int64_t c = threadIdx.x; c < k; c += blockDim.x) a.P[i * k + c] = a.X[i * a.ldx + c];
+  if (!grid_sync(a.gb)) return;
+  own_matvec(a, a.P, a.AP, r0, r1);
+  for (int64_t u = threadIdx.x; u < (r1 - r0) * k; u += blockDim.x) {
+    const int64_t i = r0 + u / k, c = u % k;
+    a.R[i * k + c] = safe_div(a.B[i * a.ldb + c], mult[c]) - a.AP[i * k + c];
+  }
+  if (!grid_sync(a.gb)) return;  // everyone done reading x0 out of P
+  own_partials([&](int64_t i, int64_t c) {
+    const T r = a.R[i * k + c];
+    const T z = PK == 0 ? r : a.dinv[i] * r;
+    a.P[i * k + c] = z;
+    return r * z;
+  }, pB);
+  own_partials([&](int64_t i, int64_t c) { const T r = a.R[i * k + c]; return r * r; }, pC);
+  if (!grid_sync(a.gb)) return;
+  all_totals(a.s.pB, nb, k, tot1);
+  all_totals(a.s.pC, nb, k, tot2);
+  if (threadIdx.x == 0) s_any = 0;
+  __syncthreads();
+  for (int64_t c = threadIdx.x; c < k; c += blockDim.x) {
+    gamma[c] = tot1[c];
+    const T rn = sqrt(tot2[c]);
+    tot2[c] = rn;
+    tol_eff[c] = (T)a.tol * rn + (T)a.tol;
+    conv[c] = rn < SmallValue<T>::v;
+    if (rn > tol_eff[c]) atomicOr(&s_any, 1);
+  }
+  __syncthreads();
+  if (blockIdx.x == 0 && threadIdx.x == 0 && a.hist) {
+    T m = T(0);
+    for (int64_t c = 0; c < k; ++c) m += tot2[c];
+    a.hist[0] = m / (T)k;
+  }
+  int it = 0;
+  bool running = s_any && it < a.max_iters;
+  __syncthreads();
+
+  while (running) {
+    // ---- phase A: Ap = A p, <p, Ap> ----
+    own_matvec(a, a.P, a.AP, r0, r1);
+    own_partials([&](int64_t i, int64_t c) { return a.P[i * k + c] * a.AP[i * k + c]; }, pA);
+    if (!grid_sync(a.gb)) return;
+    all_totals(a.s.pA, nb, k, tot1);
+    for (int64_t c = threadIdx.x; c < k; c += blockDim.x) alpha[c] = conv[c] ? T(0) : safe_div(gamma[c], tot1[c]);
+    __syncthreads();
+    // ---- phase B: x, r updates, <r, z>, |r|^2 ----
+    own_partials([&](int64_t i, int64_t c) {
+      const T al = alpha[c];
+      a.X[i * a.ldx + c] += al * a.P[i * k + c];
+      const T r = a.R[i * k + c] - al * a.AP[i * k + c];
+      a.R[i * k + c] = r;
+      return r * r;
+    }, pC);
+    own_partials([&](int64_t i, int64_t c) {
+      const T r = a.R[i * k + c];
+      return r * (PK == 0 ? r : a.dinv[i] * r);
+    }, pB);
+    if (!grid_sync(a.gb)) return;
+    all_totals(a.s.pB, nb, k, tot1);
+    all_totals(a.s.pC, nb, k, tot2);
+    if (threadIdx.x == 0) s_any = 0;
+    __syncthreads();
+    for (int64_t c = threadIdx.x; c < k; c += blockDim.x) {
+      const T g1 = tot1[c];
+      beta[c] = conv[c] ? T(0) : safe_div(g1, gamma[c]);
+      gamma[c] = g1;
+      const T rn = sqrt(tot2[c]);
+      tot2[c] = rn;
+      conv[c] = rn < SmallValue<T>::v;
+      if (rn > tol_eff[c]) atomicOr(&s_any, 1);
+    }
+    __syncthreads();
+    ++it;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && a.hist) {
+      T m = T(0);
+      for (int64_t c = 0; c < k; ++c) m += tot2[c];
+      a.hist[it] = m / (T)k;
+    }
+    running = s_any && it < a.max_iters;
+    __syncthreads();
+    if (!running) break;
+    // ---- phase C: p = z + beta p ----
+    for (int64_t u = threadIdx.x; u < (r1 - r0) * k; u += blockDim.x) {
+      const int64_t i = r0 + u / k, c = u % k;
+      const T r = a.R[i * k + c];
+      const T z = PK == 0 ? r : a.dinv[i] * r;
+      a.P[i * k + c] = z + beta[c] * a.P[i * k + c];
+    }
+    if (!grid_sync(a.gb)) return;
+  }
+  // ---- x *= mult ----
+  for (int64_t u = threadIdx.x; u < (r1 - r0) * k; u += blockDim.x) {
+    const int64_t i = r0 + u / k, c = u % k;
+    a.X[i * a.ldx + c] *= mult[c];
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *a.s.iters = it;
+}
+
+// ---------------------------------------------------------------------------------------------
+// host side
+
+struct CgPlan {
+  int64_t n = 0, k = 0;
+  int nb = 1;          // blocks of the generic kernels
+  int pk = 0;          // 0 identity, 1 diagonal (fused into the kernels), 2 general operator
+  const colagb_op_node* pdiag = nullptr;
+  bool fused_ok = false;
+  FusedForm ff;
+  int fused_blocks = 0;
+};
+
+template <class T>
+static CgScalars<T> carve(Bump& ws, int64_t k, int nb) {
+  CgScalars<T> s;
+  s.mult = ws.take<T>(k);
+  s.tol_eff = ws.take<T>(k);
+  s.gamma = ws.take<T>(k);
+  s.alpha = ws.take<T>(k);
+  s.beta = ws.take<T>(k);
+  s.rnorm = ws.take<T>(k);
+  s.conv = ws.take<int>(k);
+  s.done = ws.take<int>(4);
+  s.iters = ws.take<int>(4);
+  s.pA = ws.take<T>((size_t)nb * k);
+  s.pB = ws.take<T>((size_t)nb * k);
+  s.pC = ws.take<T>((size_t)nb * k);
+  s.counters = ws.take<unsigned int>(8);
+  return s;
+}
+
+static int generic_blocks(int64_t n, int64_t k) {
+  const int64_t want = ceil_div(n * k, 1024);
+  const int64_t cap = (int64_t)num_sms() * 4;
+  return (int)(want < 1 ? 1 : (want > cap ? cap : want));
+}
+
+template <class T, class S, int PK>
+static int fused_blocks_for() {
+  int occ = 0;
+  const size_t smem = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cg_fused<T, S, PK>, 256, smem);
+  if (occ < 1) occ = 1;
+  return num_sms() * (occ < 2 ? occ : 2);
+}
+
+static int plan_cg(const colagb_op* A, const colagb_op* P, int64_t k, CgPlan& pl) {
+  const colagb_op_node& r = A->nodes[A->root];
+  if (r.rows != r.cols) return fail(COLAGB_ERR_INVALID, "CG needs a square operator");
+  pl.n = r.rows;
+  pl.k = k;
+  pl.nb = generic_blocks(pl.n, k);
+  pl.pk = 0;
+  if (P) {
+    const colagb_op_node& pr = P->nodes[P->root];
+    if (pr.rows != pl.n || pr.cols != pl.n) return fail(COLAGB_ERR_INVALID, "preconditioner shape mismatch");
+    if (P->compute_dtype != A->compute_dtype)
+      return fail(COLAGB_ERR_INVALID, "preconditioner and operator compute types differ");
+    if (pr.kind == COLAGB_OP_IDENTITY) pl.pk = 0;
+    else if (pr.kind == COLAGB_OP_DIAG &&
+             (pr.dtype == A->compute_dtype)) { pl.pk = 1; pl.pdiag = &pr; }
+    else pl.pk = 2;
+  }
+  pl.ff = fused_form(A);
+  pl.fused_ok = pl.ff.ok && pl.pk != 2 && k <= 64 && pl.n > 0 &&
+                (pl.ff.leaf->kind == COLAGB_OP_CSR || k <= 8) &&
+                (pl.ff.leaf->dtype == A->compute_dtype || pl.ff.leaf->dtype == COLAGB_BF16);
+  return COLAGB_OK;
+}
+
+template <class T>
+static size_t cg_ws(const colagb_op* A, const colagb_op* P, const CgPlan& pl, Bump& ws, CgScalars<T>* out,
+                    T** R, T** Pv, T** AP, T** Z, T** hist_dummy, void** opws, size_t* opws_bytes) {
+  const int64_t n = pl.n, k = pl.k;
+  CgScalars<T> s = carve<T>(ws, k, pl.nb > pl.fused_blocks ? pl.nb : pl.fused_blocks);
+  *R = ws.take<T>(n * k);
+  *Pv = ws.take<T>(n * k);
+  *AP = ws.take<T>(n * k);
+  *Z = pl.pk == 2 ? ws.take<T>(n * k) : nullptr;
+  (void)hist_dummy;
+  size_t a_b = 0, p_b = 0;
+  colagb_matmat_workspace_bytes(A, k, &a_b);
+  if (P && pl.pk == 2) colagb_matmat_workspace_bytes(P, k, &p_b);
+  *opws_bytes = a_b > p_b ? a_b : p_b;
+  *opws = ws.take<char>(*opws_bytes > 0 ? *opws_bytes : 1);
+  if (out) *out = s;
+  return ws.peak;
+}
+
+template <class T>
+static int run_generic(const colagb_op* A, const colagb_op* P, const CgPlan& pl, const T* B, int64_t ldb, T* X,
+                       int64_t ldx, const colagb_cg_params& prm, T* hist, CgScalars<T> s, T* R, T* Pv, T* AP, T* Z,
+                       void* opws, size_t opws_bytes, colagb_cg_result* res, cudaStream_t st) {
+  const int64_t n = pl.n, k = pl.k;
+  const int nb = pl.nb;
+  const T* dinv = pl.pk == 1 ? static_cast<const T*>(pl.pdiag->data) : nullptr;
+  const int eg = (int)std::min<int64_t>(std::max<int64_t>(ceil_div(n * k, 256), 1), (int64_t)num_sms() * 8);
+  COLAGB_CUDA(cudaMemsetAsync(s.counters, 0, 8 * sizeof(unsigned int), st));
+  k_colnorm_b<T><<<nb, 256, 0, st>>>(B, ldb, n, k, s);
+  k_scale_b<T><<<eg, 256, 0, st>>>(B, ldb, R, n, k, s);
+  COLAGB_CUDA(cudaGetLastError());
+  {
+    Bump w(opws, opws_bytes);
+    COLAGB_TRY(op_apply<T>(A, A->root, X, ldx, 0, R, k, 0, k, 1, T(-1), T(1), w, nullptr, st));
+  }
+  if (pl.pk == 2) {
+    Bump w(opws, opws_bytes);
+    COLAGB_TRY(op_apply<T>(P, P->root, R, k, 0, Z, k, 0, k, 1, T(1), T(0), w, nullptr, st));
+  }
+  switch (pl.pk) {
+    case 0: k_init<T, 0><<<nb, 256, 0, st>>>(R, Z, dinv, Pv, n, k, prm.tol, prm.max_iters, hist, s); break;
+    case 1: k_init<T, 1><<<nb, 256, 0, st>>>(R, Z, dinv, Pv, n, k, prm.tol, prm.max_iters, hist, s); break;
+    default: k_init<T, 2><<<nb, 256, 0, st>>>(R, Z, dinv, Pv, n, k, prm.tol, prm.max_iters, hist, s); break;
+  }
+  COLAGB_CUDA(cudaGetLastError());
+  int h_done[2] = {0, 0};
+  const int every = prm.check_every > 0 ? prm.check_every : 16;
+  int launched = 0;
+  int status = COLAGB_OK;
+  while (true) {
+    for (int j = 0; j < every && launched < prm.max_iters; ++j, ++launched) {
+      Bump w(opws, opws_bytes);
+      status = op_apply<T>(A, A->root, Pv, k, 0, AP, k, 0, k, 1, T(1), T(0), w, s.done, st);
+      if (status != COLAGB_OK) break;
+      k_alpha<T><<<nb, 256, 0, st>>>(Pv, AP, n, k, s);
+      switch (pl.pk) {
+        case 0: k_update<T, 0><<<nb, 256, 0, st>>>(X, ldx, R, Pv, AP, dinv, n, k, prm.max_iters, hist, s); break;
+        case 1: k_update<T, 1><<<nb, 256, 0, st>>>(X, ldx, R, Pv, AP, dinv, n, k, prm.max_iters, hist, s); break;
+        default: {
+          k_update<T, 2><<<nb, 256, 0, st>>>(X, ldx, R, Pv, AP, dinv, n, k, prm.max_iters, hist, s);
+          Bump w2(opws, opws_bytes);
+          status = op_apply<T>(P, P->root, R, k, 0, Z, k, 0, k, 1, T(1), T(0), w2, s.done, st);
+          if (status != COLAGB_OK) break;
+          k_gamma<T><<<nb, 256, 0, st>>>(R, Z, n, k, prm.max_iters, hist, s);
+        }
+      }
+      if (status != COLAGB_OK) break;
+      // p update runs only when the step did not finish the loop (done flag now set => skip)
+      switch (pl.pk) {
+        case 0: k_pupdate<T, 0><<<eg, 256, 0, st>>>(Pv, R, Z, dinv, n, k, s, s.done); break;
+        case 1: k_pupdate<T, 1><<<eg, 256, 0, st>>>(Pv, R, Z, dinv, n, k, s, s.done); break;
+        default: k_pupdate<T, 2><<<eg, 256, 0, st>>>(Pv, R, Z, dinv, n, k, s, s.done); break;
+      }
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) { status = check_cuda(e, "cg step launch"); break; }
+    }
+    if (status != COLAGB_OK) break;
+    cudaError_t e = cudaMemcpyAsync(h_done, s.done, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) { status = check_cuda(e, "cg poll"); break; }
+    if (h_done[0] || launched >= prm.max_iters) break;
+  }
+  if (status != COLAGB_OK) return status;
+  k_scale_x<T><<<eg, 256, 0, st>>>(X, ldx, n, k, s);
+  COLAGB_CUDA(cudaGetLastError());
+  int it = 0;
+  COLAGB_CUDA(cudaMemcpyAsync(&it, s.iters, sizeof(int), cudaMemcpyDeviceToHost, st));
+  COLAGB_CUDA(cudaStreamSynchronize(st));
+  res->iterations = it;
+  res->fused = 0;
+  res->status = COLAGB_OK;
+  return COLAGB_OK;
+}
+
+template <class T, class S, int PK>
+static int run_fused(const CgPlan& pl, const T* B, int64_t ldb, T* X, int64_t ldx, const colagb_cg_params& prm, T* hist,
+                     CgScalars<T> s, T* R, T* Pv, T* AP, colagb_cg_result* res, cudaStream_t st) {
+  FusedArgs<T, S> a;
+  const colagb_op_node* leaf = pl.ff.leaf;
+  a.kind = leaf->kind;
+  a.vals = static_cast<const S*>(leaf->data);
+  a.lda = leaf->ld;
+  a.indptr = leaf->indptr;
+  a.indices = leaf->indices;
+  a.shift = (T)pl.ff.shift;
+  a.dinv = PK == 1 ? static_cast<const T*>(pl.pdiag->data) : nullptr;
+  a.B = B;
+  a.ldb = ldb;
+  a.X = X;
+  a.ldx = ldx;
+  a.R = R;
+  a.P = Pv;
+  a.AP = AP;
+  a.n = pl.n;
+  a.k = pl.k;
+  a.tol = prm.tol;
+  a.max_iters = prm.max_iters;
+  a.hist = hist;
+  a.vec4 = leaf->kind == COLAGB_OP_DENSE && (pl.n % 4 == 0) && (leaf->ld % 4 == 0) &&
+           ((uintptr_t)leaf->data % 16 == 0) && ((uintptr_t)Pv % 16 == 0);
+  a.s = s;
+  a.gb.count = s.counters + 4;
+  a.gb.generation = s.counters + 5;
+  a.gb.err = reinterpret_cast<int*>(s.counters + 6);
+  a.gb.spin_limit = prm.spin_limit > 0 ? prm.spin_limit : kDefaultSpinLimit;
+  const size_t smem = 256 * sizeof(T) + 7 * (size_t)pl.k * sizeof(T) + (size_t)pl.k * sizeof(int);
+  int occ = 0;
+  COLAGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cg_fused<T, S, PK>, 256, smem));
+  if (occ < 1) return fail(COLAGB_ERR_UNSUPPORTED, "fused CG kernel cannot be resident");
+  const int nb = num_sms() * (occ < 2 ? occ : 2);
+  if (nb > pl.fused_blocks) return fail(COLAGB_ERR_WORKSPACE, "fused CG block count exceeds planned partials");
+  a.gb.nblocks = (unsigned)nb;
+  COLAGB_CUDA(cudaMemsetAsync(s.counters, 0, 8 * sizeof(unsigned int), st));
+  void* args[] = {&a};
+  COLAGB_CUDA(cudaLaunchCooperativeKernel((const void*)k_cg_fused<T, S, PK>, dim3(nb), dim3(256), args, smem, st));
+  int h[3] = {0, 0, 0};
+  COLAGB_CUDA(cudaMemcpyAsync(&h[0], s.iters, sizeof(int), cudaMemcpyDeviceToHost, st));
+  COLAGB_CUDA(cudaMemcpyAsync(&h[1], s.counters + 6, sizeof(int), cudaMemcpyDeviceToHost, st));
+  COLAGB_CUDA(cudaStreamSynchronize(st));
+  res->iterations = h[0];
+  res->fused = 1;
+  res->status = h[1];
+  if (h[1] != 0) return fail(COLAGB_ERR_TIMEOUT, "fused CG: a grid barrier timed out");
+  return COLAGB_OK;
+}
+
+template <class T>
+static int cg_solve_t(const colagb_op* A, const colagb_op* P, const void* Bv, int64_t ldb, void* Xv, int64_t ldx,
+                      int64_t k, const colagb_cg_params& prm, void* histv, void* workspace, size_t ws_bytes,
+                      colagb_cg_result* res, cudaStream_t st) {
+  CgPlan pl;
+  COLAGB_TRY(plan_cg(A, P, k, pl));
+  pl.fused_blocks = num_sms() * 2;
+  Bump ws(workspace, ws_bytes);
+  CgScalars<T> s;
+  T *R, *Pv, *AP, *Z, *hd;
+  void* opws;
+  size_t opws_b;
+  cg_ws<T>(A, P, pl, ws, &s, &R, &Pv, &AP, &Z, &hd, &opws, &opws_b);
+  if (ws.overflow() || workspace == nullptr)
+    return fail(COLAGB_ERR_WORKSPACE, "colagb_cg_solve: workspace too small (need " + std::to_string(ws.peak) + ")");
+  const T* B = static_cast<const T*>(Bv);
+  T* X = static_cast<T*>(Xv);
+  T* hist = static_cast<T*>(histv);
+  if (pl.n == 0 || k == 0) {
+    res->iterations = 0;
+    res->fused = 0;
+    res->status = COLAGB_OK;
+    return COLAGB_OK;
+  }
+  if (prm.allow_fused && pl.fused_ok) {
+    const int sd = pl.ff.leaf->dtype;
+    if (sd == COLAGB_BF16) {
+      return pl.pk == 0 ? run_fused<T, __nv_bfloat16, 0>(pl, B, ldb, X, ldx, prm, hist, s, R, Pv, AP, res, st)
+                        : run_fused<T, __nv_bfloat16, 1>(pl, B, ldb, X, ldx, prm, hist, s, R, Pv, AP, res, st);
+    }
+    return pl.pk == 0 ? run_fused<T, T, 0>(pl, B, ldb, X, ldx, prm, hist, s, R, Pv, AP, res, st)
+                      : run_fused<T, T, 1>(pl, B, ldb, X, ldx, prm, hist, s, R, Pv, AP, res, st);
+  }
+  return run_generic<T>(A, P, pl, B, ldb, X, ldx, prm, hist, s, R, Pv, AP, Z, opws, opws_b, res, st);
+}
+
+}  // namespace colagb
+
+using namespace colagb;
+
+extern "C" int colagb_cg_workspace_bytes(const colagb_op* A, const colagb_op* P, int64_t k, size_t* bytes) {
+  if (!A || !bytes || k < 0) return fail(COLAGB_ERR_INVALID, "colagb_cg_workspace_bytes: bad arguments");
+  CgPlan pl;
+  COLAGB_TRY(plan_cg(A, P, k, pl));
+  pl.fused_blocks = num_sms() * 2;
+  Bump ws(nullptr, 0);
+  void* opws;
+  size_t ob;
+  if (A->compute_dtype == COLAGB_F64) {
+    double *R, *Pv, *AP, *Z, *h;
+    cg_ws<double>(A, P, pl, ws, nullptr, &R, &Pv, &AP, &Z, &h, &opws, &ob);
+  } else {
+    float *R, *Pv, *AP, *Z, *h;
+    cg_ws<float>(A, P, pl, ws, nullptr, &R, &Pv, &AP, &Z, &h, &opws, &ob);
+  }
+  *bytes = ws.peak;
+  return COLAGB_OK;
+}
+
+extern "C" int colagb_cg_solve(const colagb_op* A, const colagb_op* P, const void* B, int64_t ldb, void* X,
+                               int64_t ldx, int64_t k, const colagb_cg_params* params, void* residual_history,
+                               void* workspace, size_t workspace_bytes, colagb_cg_result* result, void* stream) {
+  if (!A || !params || !result) return fail(COLAGB_ERR_INVALID, "colagb_cg_solve: null argument");
+  if (k < 0 || ldb < k || ldx < k) return fail(COLAGB_ERR_INVALID, "colagb_cg_solve: bad k / leading dimensions");
+  if (params->max_iters < 0) return fail(COLAGB_ERR_INVALID, "colagb_cg_solve: max_iters < 0");
+  const int64_t n = A->nodes[A->root].rows;
+  if (n * k > 0 && (!B || !X)) return fail(COLAGB_ERR_INVALID, "colagb_cg_solve: null B/X");
+  cudaStream_t st = as_stream(stream);
+  if (A->compute_dtype == COLAGB_F64)
+    return cg_solve_t<double>(A, P, B, ldb, X, ldx, k, *params, residual_history, workspace, workspace_bytes, result, st);
+  return cg_solve_t<float>(A, P, B, ldb, X, ldx, k, *params, residual_history, workspace, workspace_bytes, result, st);
+}

@@ -1,0 +1,528 @@
+// Lanczos with full reorthogonalisation and the FP64 tridiagonal eigensolver.
+//
+// Reference (cola/linalg/decompositions/lanczos.py):
+//   init_lanczos :275-284   V[..., 1] = rhs / |rhs|, i = 1
+//   lanczos_fact :235-272   while i <= max_iters and any(subdiag[i-1] > tol*subdiag[1] or i <= 1):
+//       V[i] /= |V[i]| ; w = A V[i] ; diag[i-1] = <w, V[i]>
+//       w -= diag[i-1] V[i] + subdiag[i-1] V[i-1] ; w = CGS2(V, w) ; V[i+1] = w ; subdiag[i] = |w| ; i++
+//   do_double_gram :287-296 two passes of w -= V (V^T w) over the basis.
+// The reference's CGS passes run over all max_iters+2 slots; the unfilled ones are zero, so only
+// slots 1..i are visited here (same values, fewer bytes).
+//
+// Basis layout: slot j is an n x bs row-major block at basis + j*n*bs (probe index fastest), so
+// every pass reads contiguous, coalesced rows.  Per step: 1 operator application, 2 column-norm
+// reductions, 1 dot, and 2 x (V^T w then w -= V h) passes over the filled slots.
+#include <cmath>
+#include <string>
+
+#include "common.cuh"
+#include "ops.cuh"
+
+namespace colagb {
+
+template <class T>
+struct LzState {
+  T* nrm;         // bs
+  T* hbuf;        // (max_iters + 2) x bs projection coefficients
+  T* hpart;       // nblk x (max_iters + 2) x bs partial projections
+  T* npart;       // nblk x bs partial norms / dots
+  int* done;
+  int* step;      // current i
+  unsigned int* counters;
+};
+
+__device__ __forceinline__ bool lz_last_block(unsigned int* counter) {
+  __shared__ int s_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (s_last) __threadfence();
+  return s_last != 0;
+}
+
+// Per-probe column reduction over rows of an n x bs block: f(r, b) summed per b.
+// Block layout: threads = (rows_per_pass x bsc), bsc = min(bs, 256).
+template <class T, class F>
+__device__ __forceinline__ void lz_partials(int64_t n, int64_t bs, F f, T* out, T* smem) {
+  const int t = threadIdx.x;
+  for (int64_t b0 = 0; b0 < bs; b0 += blockDim.x) {
+    const int bc = (int)((bs - b0) < (int64_t)blockDim.x ? (bs - b0) : (int64_t)blockDim.x);
+    const int rpp = blockDim.x / bc;
+    const int my_b = t % bc, my_r = t / bc;
+    T acc = T(0);
+    if (my_r < rpp)
+      for (int64_t r = (int64_t)blockIdx.x * rpp + my_r; r < n; r += (int64_t)rpp * gridDim.x) acc += f(r, b0 + my_b);
+    smem[t] = acc;
+    __syncthreads();
+    if (t < bc) {
+      T s = T(0);
+      for (int q = 0; q < rpp; ++q) s += smem[q * bc + t];
+      out[b0 + t] = s;
+    }
+    __syncthreads();
+  }
+}
+
+template <class T>
+__device__ __forceinline__ T lz_sum(const T* part, int nb, int64_t bs, int64_t b) {
+  T s = T(0);
+  for (int q = 0; q < nb; ++q) s += __ldcg(part + (int64_t)q * bs + b);
+  return s;
+}
+
+// V[i] /= |V[i]|   (norm pass; the division is k_lz_scale)
+template <class T>
+__global__ void __launch_bounds__(256) k_lz_norm(const T* v, int64_t n, int64_t bs, LzState<T> s) {
+  if (*s.done) return;
+  __shared__ T smem[256];
+  lz_partials<T>(n, bs, [&](int64_t r, int64_t b) { const T x = v[r * bs + b]; return x * x; },
+                 s.npart + (int64_t)blockIdx.x * bs, smem);
+  if (lz_last_block(s.counters + 0)) {
+    for (int64_t b = threadIdx.x; b < bs; b += blockDim.x) s.nrm[b] = sqrt(lz_sum(s.npart, gridDim.x, bs, b));
+    if (threadIdx.x == 0) s.counters[0] = 0;
+  }
+}
+
+template <class T>
+__global__ void k_lz_scale(T* v, int64_t n, int64_t bs, LzState<T> s) {
+  if (*s.done) return;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n * bs; u += (int64_t)gridDim.x * blockDim.x)
+    v[u] = v[u] / s.nrm[u % bs];
+}
+
+// diag[b][i-1] = <w, V[i]>
+template <class T>
+__global__ void __launch_bounds__(256) k_lz_alpha(const T* w, const T* vi, int64_t n, int64_t bs, T* diag,
+                                                  int max_iters, LzState<T> s) {
+  if (*s.done) return;
+  __shared__ T smem[256];
+  lz_partials<T>(n, bs, [&](int64_t r, int64_t b) { return w[r * bs + b] * vi[r * bs + b]; },
+                 s.npart + (int64_t)blockIdx.x * bs, smem);
+  if (lz_last_block(s.counters + 1)) {
+    const int i = *s.step;
+    for (int64_t b = threadIdx.x; b < bs; b += blockDim.x)
+      diag[b * max_iters + (i - 1)] = lz_sum(s.npart, gridDim.x, bs, b);
+    if (threadIdx.x == 0) s.counters[1] = 0;
+  }
+}
+
+// w -= diag[i-1] V[i] + subdiag[i-1] V[i-1]
+template <class T>
+__global__ void k_lz_three_term(T* w, const T* vi, const T* vim1, int64_t n, int64_t bs, const T* diag,
+                                const T* subdiag, int max_iters, LzState<T> s) {
+  if (*s.done) return;
+  const int i = *s.step;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n * bs; u += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = u % bs;
+    w[u] -= diag[b * max_iters + (i - 1)] * vi[u] + subdiag[b * (max_iters + 1) + (i - 1)] * vim1[u];
+  }
+}
+
+// Projection partials: hpart[blk][j][b] = sum over the block's rows of V[j][r][b] * w[r][b], j = 1..i.
+// Each block owns a contiguous row range (staged w rows reused across all j).
+template <class T>
+__global__ void __launch_bounds__(256) k_lz_project(const T* basis, const T* w, int64_t n, int64_t bs,
+                                                    int64_t slots, LzState<T> s) {
+  if (*s.done) return;
+  __shared__ T smem[256];
+  const int i = *s.step;
+  const int64_t rows_per_block = ceil_div(n, gridDim.x);
+  const int64_t r0 = (int64_t)blockIdx.x * rows_per_block;
+  const int64_t r1 = r0 + rows_per_block < n ? r0 + rows_per_block : n;
+  T* out = s.hpart + (int64_t)blockIdx.x * slots * bs;
+  const int t = threadIdx.x;
+  for (int64_t b0 = 0; b0 < bs; b0 += blockDim.x) {
+    const int bc = (int)((bs - b0) < (int64_t)blockDim.x ? (bs - b0) : (int64_t)blockDim.x);
+    const int rpp = blockDim.x / bc;
+    const int my_b = t % bc, my_r = t / bc;
+    for (int j = 1; j <= i; ++j) {
+      const T* vj = basis + (int64_t)j * n * bs;
+      T acc = T(0);
+      if (my_r < rpp)
+        for (int64_t r = r0 + my_r; r < r1; r += rpp) acc += vj[r * bs + b0 + my_b] * w[r * bs + b0 + my_b];
+      smem[t] = acc;
+      __syncthreads();
+      if (t < bc) {
+        T sum = T(0);
+        for (int q = 0; q < rpp; ++q) sum += smem[q * bc + t];
+        out[(int64_t)j * bs + b0 + t] = sum;
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// h[j][b] = sum over blocks of hpart  (thread per (j, b))
+template <class T>
+__global__ void k_lz_reduce_h(int nblk, int64_t bs, int64_t slots, LzState<T> s) {
+  if (*s.done) return;
+  const int i = *s.step;
+  const int64_t total = (int64_t)(i + 1) * bs;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < total; u += (int64_t)gridDim.x * blockDim.x) {
+    T acc = T(0);
+    if (u >= bs)  // slot 0 is the zero vector
+      for (int q = 0; q < nblk; ++q) acc += s.hpart[(int64_t)q * slots * bs + u];
+    s.hbuf[u] = acc;
+  }
+}
+
+// w -= sum_j V[j] h[j]
+template <class T>
+__global__ void k_lz_subtract(const T* basis, T* w, int64_t n, int64_t bs, LzState<T> s) {
+  if (*s.done) return;
+  const int i = *s.step;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n * bs; u += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = u % bs;
+    T acc = T(0);
+    for (int j = 1; j <= i; ++j) acc += basis[(int64_t)j * n * bs + u] * s.hbuf[(int64_t)j * bs + b];
+    w[u] -= acc;
+  }
+}
+
+// subdiag[b][i] = |w| ; i += 1 ; stop test of lanczos_fact.cond_fun
+template <class T>
+__global__ void __launch_bounds__(256) k_lz_finish(const T* w, int64_t n, int64_t bs, T* subdiag, int max_iters,
+                                                   double tol, LzState<T> s) {
+  if (*s.done) return;
+  __shared__ T smem[256];
+  lz_partials<T>(n, bs, [&](int64_t r, int64_t b) { const T x = w[r * bs + b]; return x * x; },
+                 s.npart + (int64_t)blockIdx.x * bs, smem);
+  if (lz_last_block(s.counters + 2)) {
+    __shared__ int s_any;
+    const int i = *s.step;
+    if (threadIdx.x == 0) s_any = 0;
+    __syncthreads();
+    for (int64_t b = threadIdx.x; b < bs; b += blockDim.x) {
+      const T nv = sqrt(lz_sum(s.npart, gridDim.x, bs, b));
+      subdiag[b * (max_iters + 1) + i] = nv;
+      const T first = subdiag[b * (max_iters + 1) + 1];
+      if (nv > (T)tol * first) atomicOr(&s_any, 1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const int ni = i + 1;
+      *s.step = ni;
+      *s.done = !(ni <= max_iters && (s_any || ni <= 1));
+      s.counters[2] = 0;
+    }
+  }
+}
+
+// V[1] = V0 / |V0| (init_lanczos) -- norm partials then scale
+template <class T>
+__global__ void k_lz_init_copy(const T* v0, int64_t ldv0, T* v1, int64_t n, int64_t bs) {
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n * bs; u += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = u / bs, b = u % bs;
+    v1[u] = v0[r * ldv0 + b];
+  }
+}
+
+template <class T>
+__global__ void k_lz_set_state(LzState<T> s, int max_iters) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    *s.step = 1;
+    *s.done = !(1 <= max_iters);
+  }
+}
+
+// out[r][b] = sum_{j<m} basis[j+1][r][b] * coef[b * ldc + j]
+template <class T>
+__global__ void k_basis_combine(const T* basis, int64_t n, int64_t bs, int m, const T* coef, int64_t ldc, T* out) {
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n * bs; u += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = u % bs;
+    T acc = T(0);
+    for (int j = 0; j < m; ++j) acc += basis[(int64_t)(j + 1) * n * bs + u] * coef[b * ldc + j];
+    out[u] = acc;
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// FP64 symmetric tridiagonal eigensolver: implicit QL with Wilkinson shifts, one CTA per matrix.
+// Thread 0 runs the scalar recurrence; each QL sweep's Givens rotations are recorded in shared
+// memory and then applied by all threads to their own rows of the eigenvector matrix (rows are
+// independent under column rotations).  Row 0 alone (Gauss weights) is tracked by thread 0.
+__global__ void k_tridiag_ql(const double* A, const double* Bv, int64_t m, double* evals, double* first_row,
+                             double* evecs, int32_t* status) {
+  extern __shared__ double sm[];
+  double* d = sm;              // m
+  double* e = d + m;           // m
+  double* z0 = e + m;          // m (row 0 of Z)
+  double* rc = z0 + m;         // m rotation cosines
+  double* rs = rc + m;         // m rotation sines
+  int* perm = reinterpret_cast<int*>(rs + m);  // m
+  __shared__ int s_cmd, s_lo, s_hi, s_fail;
+  const int64_t sys = blockIdx.x;
+  const double* a = A + sys * m;
+  const double* b = Bv + sys * m;
+  double* Z = evecs ? evecs + sys * m * m : nullptr;
+  for (int64_t i = threadIdx.x; i < m; i += blockDim.x) {
+    d[i] = a[i];
+    e[i] = (i + 1 < m) ? b[i] : 0.0;
+    z0[i] = (i == 0) ? 1.0 : 0.0;
+  }
+  if (Z)
+    for (int64_t u = threadIdx.x; u < m * m; u += blockDim.x) Z[u] = (u / m == u % m) ? 1.0 : 0.0;
+  if (threadIdx.x == 0) s_fail = 0;
+  __syncthreads();
+  int l = 0, iter = 0;
+  while (true) {
+    // thread 0: one QL sweep (or decide to move on)
+    if (threadIdx.x == 0) {
+      s_cmd = 0;  // 0 = nothing to apply, 1 = apply rotations [s_lo, s_hi), 2 = finished
+      while (l < m) {
+        int mm = l;
+        for (; mm < m - 1; ++mm) {
+          const double dd = fabs(d[mm]) + fabs(d[mm + 1]);
+          if (fabs(e[mm]) <= 2.220446049250313e-16 * dd) break;
+        }
+        if (mm == l) { ++l; iter = 0; continue; }
+        if (iter++ >= 60) { s_fail = 1; ++l; iter = 0; continue; }
+        double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
+        double r = hypot(g, 1.0);
+        g = d[mm] - d[l] + e[l] / (g + (g >= 0.0 ? fabs(r) : -fabs(r)));
+        double s = 1.0, c = 1.0, p = 0.0;
+        int i = mm - 1;
+        bool underflow = false;
+        for (; i >= l; --i) {
+          double f = s * e[i], bb = c * e[i];
+          r = hypot(f, g);
+          e[i + 1] = r;
+          if (r == 0.0) {
+            d[i + 1] -= p;
+            e[mm] = 0.0;
+            underflow = true;
+            break;
+          }
+          s = f / r;
+          c = g / r;
+          g = d[i + 1] - p;
+          r = (d[i] - g) * s + 2.0 * c * bb;
+          p = s * r;
+          d[i + 1] = g + p;
+          g = c * r - bb;
+          rc[i] = c;
+          rs[i] = s;
+          const double zf = z0[i + 1];
+          z0[i + 1] = s * z0[i] + c * zf;
+          z0[i] = c * z0[i] - s * zf;
+        }
+        if (underflow) {
+          s_lo = i + 1;
+          s_hi = mm;
+        } else {
+          d[l] -= p;
+          e[l] = g;
+          e[mm] = 0.0;
+          s_lo = l;
+          s_hi = mm;
+        }
+        s_cmd = 1;
+        break;
+      }
+      if (l >= m) s_cmd = (s_cmd == 1) ? 1 : 2;
+    }
+    __syncthreads();
+    const int cmd = s_cmd;
+    if (cmd == 1 && Z) {
+      // rotations were generated for i = hi-1 down to lo, apply in that order
+      const int lo = s_lo, hi = s_hi;
+      for (int64_t row = threadIdx.x; row < m; row += blockDim.x) {
+        double* zr = Z + row * m;
+        for (int i = hi - 1; i >= lo; --i) {
+          const double c = rc[i], s = rs[i];
+          const double f = zr[i + 1];
+          zr[i + 1] = s * zr[i] + c * f;
+          zr[i] = c * zr[i] - s * f;
+        }
+      }
+    }
+    __syncthreads();
+    if (cmd == 2) break;
+    if (cmd == 0) break;
+  }
+  // sort ascending (selection by thread 0), then permute outputs
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < m; ++i) perm[i] = i;
+    for (int i = 0; i < m; ++i) {
+      int k = i;
+      for (int j = i + 1; j < m; ++j)
+        if (d[perm[j]] < d[perm[k]]) k = j;
+      const int t = perm[i];
+      perm[i] = perm[k];
+      perm[k] = t;
+    }
+  }
+  __syncthreads();
+  for (int64_t j = threadIdx.x; j < m; j += blockDim.x) {
+    evals[sys * m + j] = d[perm[j]];
+    if (first_row) first_row[sys * m + j] = Z ? Z[perm[j]] : z0[perm[j]];
+  }
+  __syncthreads();
+  if (Z) {
+    double* tmp = rc;  // reuse as a row buffer
+    for (int64_t row = 0; row < m; ++row) {
+      for (int64_t j = threadIdx.x; j < m; j += blockDim.x) tmp[j] = Z[row * m + perm[j]];
+      __syncthreads();
+      for (int64_t j = threadIdx.x; j < m; j += blockDim.x) Z[row * m + j] = tmp[j];
+      __syncthreads();
+    }
+  }
+  if (threadIdx.x == 0 && status) status[sys] = s_fail;
+}
+
+// ---------------------------------------------------------------------------------------------
+// host
+
+static int lz_blocks(int64_t n, int64_t bs) {
+  const int64_t want = ceil_div(n * bs, 1024);
+  const int64_t cap = (int64_t)num_sms() * 4;
+  return (int)(want < 1 ? 1 : (want > cap ? cap : want));
+}
+
+template <class T>
+static LzState<T> lz_carve(Bump& ws, int64_t bs, int32_t max_iters, int nb) {
+  LzState<T> s;
+  const int64_t slots = (int64_t)max_iters + 2;
+  s.nrm = ws.take<T>(bs);
+  s.hbuf = ws.take<T>(slots * bs);
+  s.hpart = ws.take<T>((size_t)nb * slots * bs);
+  s.npart = ws.take<T>((size_t)nb * bs);
+  s.done = ws.take<int>(4);
+  s.step = ws.take<int>(4);
+  s.counters = ws.take<unsigned int>(8);
+  return s;
+}
+
+template <class T>
+static int lanczos_t(const colagb_op* A, const T* V0, int64_t ldv0, int64_t bs, const colagb_lanczos_params& prm,
+                     T* basis, T* diag, T* subdiag, int32_t* steps, void* workspace, size_t ws_bytes,
+                     cudaStream_t st) {
+  const int64_t n = A->nodes[A->root].rows;
+  const int m = prm.max_iters;
+  const int64_t slots = (int64_t)m + 2;
+  const int nb = lz_blocks(n, bs);
+  Bump ws(workspace, ws_bytes);
+  LzState<T> s = lz_carve<T>(ws, bs, m, nb);
+  size_t opb = 0;
+  COLAGB_TRY(colagb_matmat_workspace_bytes(A, bs, &opb));
+  void* opws = ws.take<char>(opb > 0 ? opb : 1);
+  if (workspace == nullptr || ws.overflow())
+    return fail(COLAGB_ERR_WORKSPACE, "colagb_lanczos: workspace too small (need " + std::to_string(ws.peak) + ")");
+  const int eg = (int)std::min<int64_t>(std::max<int64_t>(ceil_div(n * bs, 256), 1), (int64_t)num_sms() * 8);
+  const size_t blk = (size_t)n * bs;
+  COLAGB_CUDA(cudaMemsetAsync(basis, 0, sizeof(T) * blk * slots, st));
+  COLAGB_CUDA(cudaMemsetAsync(diag, 0, sizeof(T) * bs * m, st));
+  COLAGB_CUDA(cudaMemsetAsync(subdiag, 0, sizeof(T) * bs * (m + 1), st));
+  COLAGB_CUDA(cudaMemsetAsync(s.counters, 0, 8 * sizeof(unsigned int), st));
+  k_lz_set_state<T><<<1, 32, 0, st>>>(s, m);
+  // V[1] = V0 / |V0|
+  T* v1 = basis + blk;
+  k_lz_init_copy<T><<<eg, 256, 0, st>>>(V0, ldv0, v1, n, bs);
+  k_lz_norm<T><<<nb, 256, 0, st>>>(v1, n, bs, s);
+  k_lz_scale<T><<<eg, 256, 0, st>>>(v1, n, bs, s);
+  COLAGB_CUDA(cudaGetLastError());
+  const int every = prm.check_every > 0 ? prm.check_every : 8;
+  int host_step = 1;  // the step index the next launch group starts at (upper bound)
+  int hdone = 0;
+  while (true) {
+    for (int q = 0; q < every && host_step <= m; ++q, ++host_step) {
+      const int i = host_step;  // kernels read the device step; host_step picks the basis slots
+      T* vi = basis + (size_t)i * blk;
+      T* vim1 = basis + (size_t)(i - 1) * blk;
+      T* w = basis + (size_t)(i + 1) * blk;
+      k_lz_norm<T><<<nb, 256, 0, st>>>(vi, n, bs, s);
+      k_lz_scale<T><<<eg, 256, 0, st>>>(vi, n, bs, s);
+      Bump ow(opws, opb > 0 ? opb : 1);
+      COLAGB_TRY(op_apply<T>(A, A->root, vi, bs, 0, w, bs, 0, bs, 1, T(1), T(0), ow, s.done, st));
+      k_lz_alpha<T><<<nb, 256, 0, st>>>(w, vi, n, bs, diag, m, s);
+      k_lz_three_term<T><<<eg, 256, 0, st>>>(w, vi, vim1, n, bs, diag, subdiag, m, s);
+      for (int pass = 0; pass < 2; ++pass) {
+        k_lz_project<T><<<nb, 256, 0, st>>>(basis, w, n, bs, slots, s);
+        k_lz_reduce_h<T><<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div((int64_t)(i + 1) * bs, 256), 4096)),
+                           256, 0, st>>>(nb, bs, slots, s);
+        k_lz_subtract<T><<<eg, 256, 0, st>>>(basis, w, n, bs, s);
+      }
+      k_lz_finish<T><<<nb, 256, 0, st>>>(w, n, bs, subdiag, m, prm.tol, s);
+      COLAGB_CUDA(cudaGetLastError());
+    }
+    COLAGB_CUDA(cudaMemcpyAsync(&hdone, s.done, sizeof(int), cudaMemcpyDeviceToHost, st));
+    COLAGB_CUDA(cudaStreamSynchronize(st));
+    if (hdone || host_step > m) break;
+  }
+  int dstep = 0;
+  COLAGB_CUDA(cudaMemcpyAsync(&dstep, s.step, sizeof(int), cudaMemcpyDeviceToHost, st));
+  COLAGB_CUDA(cudaStreamSynchronize(st));
+  *steps = dstep;
+  return COLAGB_OK;
+}
+
+}  // namespace colagb
+
+using namespace colagb;
+
+extern "C" int colagb_lanczos_workspace_bytes(const colagb_op* A, int64_t bs, int32_t max_iters, size_t* bytes) {
+  if (!A || !bytes || bs < 1 || max_iters < 0) return fail(COLAGB_ERR_INVALID, "colagb_lanczos_workspace_bytes: bad arguments");
+  const int64_t n = A->nodes[A->root].rows;
+  Bump ws(nullptr, 0);
+  if (A->compute_dtype == COLAGB_F64) lz_carve<double>(ws, bs, max_iters, lz_blocks(n, bs));
+  else lz_carve<float>(ws, bs, max_iters, lz_blocks(n, bs));
+  size_t opb = 0;
+  COLAGB_TRY(colagb_matmat_workspace_bytes(A, bs, &opb));
+  ws.take<char>(opb > 0 ? opb : 1);
+  *bytes = ws.peak;
+  return COLAGB_OK;
+}
+
+extern "C" int colagb_lanczos(const colagb_op* A, const void* V0, int64_t ldv0, int64_t bs,
+                              const colagb_lanczos_params* params, void* basis, void* diag, void* subdiag,
+                              int32_t* steps, void* workspace, size_t workspace_bytes, void* stream) {
+  if (!A || !params || !V0 || !basis || !diag || !subdiag || !steps)
+    return fail(COLAGB_ERR_INVALID, "colagb_lanczos: null argument");
+  const colagb_op_node& r = A->nodes[A->root];
+  if (r.rows != r.cols) return fail(COLAGB_ERR_INVALID, "colagb_lanczos: operator must be square");
+  if (bs < 1 || ldv0 < bs || params->max_iters < 0)
+    return fail(COLAGB_ERR_INVALID, "colagb_lanczos: bad bs / ldv0 / max_iters");
+  cudaStream_t st = as_stream(stream);
+  if (A->compute_dtype == COLAGB_F64)
+    return lanczos_t<double>(A, static_cast<const double*>(V0), ldv0, bs, *params, static_cast<double*>(basis),
+                             static_cast<double*>(diag), static_cast<double*>(subdiag), steps, workspace,
+                             workspace_bytes, st);
+  return lanczos_t<float>(A, static_cast<const float*>(V0), ldv0, bs, *params, static_cast<float*>(basis),
+                          static_cast<float*>(diag), static_cast<float*>(subdiag), steps, workspace, workspace_bytes,
+                          st);
+}
+
+extern "C" int colagb_basis_combine(const void* basis, int64_t n, int64_t bs, int32_t m, const void* coef,
+                                    int64_t ldc, void* out, int32_t dtype, void* stream) {
+  if (!basis || !coef || !out || n < 0 || bs < 1 || m < 0 || ldc < m)
+    return fail(COLAGB_ERR_INVALID, "colagb_basis_combine: bad arguments");
+  cudaStream_t st = as_stream(stream);
+  const int eg = (int)std::min<int64_t>(std::max<int64_t>(ceil_div(n * bs, 256), 1), (int64_t)num_sms() * 8);
+  if (n * bs == 0) return COLAGB_OK;
+  if (dtype == COLAGB_F64)
+    k_basis_combine<double><<<eg, 256, 0, st>>>(static_cast<const double*>(basis), n, bs, m,
+                                                 static_cast<const double*>(coef), ldc, static_cast<double*>(out));
+  else if (dtype == COLAGB_F32)
+    k_basis_combine<float><<<eg, 256, 0, st>>>(static_cast<const float*>(basis), n, bs, m,
+                                                static_cast<const float*>(coef), ldc, static_cast<float*>(out));
+  else
+    return fail(COLAGB_ERR_UNSUPPORTED, "colagb_basis_combine: dtype must be F32 or F64");
+  COLAGB_CUDA(cudaGetLastError());
+  return COLAGB_OK;
+}
+
+extern "C" int colagb_tridiag_eig_f64(const double* a, const double* b, int64_t m, int64_t batch, double* evals,
+                                      double* first_row, double* evecs, int32_t* status, void* stream) {
+  if (m < 0 || batch < 0 || (m * batch > 0 && (!a || !b || !evals)))
+    return fail(COLAGB_ERR_INVALID, "colagb_tridiag_eig_f64: bad arguments");
+  if (m * batch == 0) return COLAGB_OK;
+  const size_t smem = (size_t)m * (5 * sizeof(double) + sizeof(int));
+  if (smem > 200 * 1024) return fail(COLAGB_ERR_INVALID, "colagb_tridiag_eig_f64: m too large (max 4000)");
+  if (smem > 48 * 1024)
+    COLAGB_CUDA(cudaFuncSetAttribute(k_tridiag_ql, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  cudaStream_t st = as_stream(stream);
+  k_tridiag_ql<<<(unsigned)batch, 128, smem, st>>>(a, b, m, evals, first_row, evecs, status);
+  COLAGB_CUDA(cudaGetLastError());
+  return COLAGB_OK;
+}

@@ -1,0 +1,684 @@
+// Operator-program runtime and the structured matvec kernels (Dense, Sparse CSR, Diagonal,
+// ScalarMul/Identity, and the Sum / Product / Kronecker / BlockDiag compositions).
+//
+// Reference behaviour (cola/ops/operators.py):
+//   Dense._matmat      :26-28   A @ X
+//   Sparse._matmat     :77-78   CSR @ X
+//   ScalarMul._matmat  :97-98   c * X
+//   Identity._matmat   :122-123 X
+//   Product._matmat    :153-156 right-to-left chain
+//   Sum._matmat        :182-183 sum of child products
+//   Kronecker._matmat  :216-223 one contraction per factor along its own axis
+//   BlockDiag._matmat  :299-310 each block (times its multiplicity) on its row slice
+//   Diagonal._matmat   :338-339 d[:, None] * X
+// Kronecker factors are applied as strided-batched contractions on the (pre, c_i, post*k) view,
+// so no moveaxis copy is materialised.
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "ops.cuh"
+
+namespace colagb {
+
+// --------------------------------------------------------------------------------------------
+// error state
+static thread_local std::string g_last_error;
+void set_error(const std::string& msg) { g_last_error = msg; }
+int fail(int code, const std::string& msg) {
+  set_error(msg);
+  return code;
+}
+int check_cuda(cudaError_t e, const char* what) {
+  return fail(COLAGB_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+int num_sms() {
+  static std::mutex mu;
+  static std::vector<int> cache;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+  std::lock_guard<std::mutex> lk(mu);
+  if ((int)cache.size() <= dev) cache.resize(dev + 1, 0);
+  if (cache[dev] == 0) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    cache[dev] = v > 0 ? v : 1;
+  }
+  return cache[dev];
+}
+
+// --------------------------------------------------------------------------------------------
+// leaf kernels
+
+template <class T>
+__device__ __forceinline__ T combine(T acc, T alpha, T beta, const T* y) {
+  return beta == T(0) ? alpha * acc : alpha * acc + beta * (*y);
+}
+
+// Dense, few columns (k <= 4): one warp per output row, lanes stride over the row.
+template <class T, class S, int K>
+__global__ void __launch_bounds__(256) dense_gemv_kernel(const S* __restrict__ A, int64_t lda, int64_t rows,
+                                                         int64_t cols, const T* __restrict__ X, int64_t ldx,
+                                                         int64_t bsx, T* __restrict__ Y, int64_t ldy,
+                                                         int64_t bsy, T alpha, T beta, const int* skip) {
+  if (skip && *skip) return;
+  const int64_t b = blockIdx.y;
+  X += b * bsx;
+  Y += b * bsy;
+  const int lane = threadIdx.x & 31;
+  const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (row >= rows) return;
+  const S* a = A + row * lda;
+  T acc[K];
+#pragma unroll
+  for (int c = 0; c < K; ++c) acc[c] = T(0);
+  for (int64_t j = lane; j < cols; j += 32) {
+    const T av = cvt<T>(a[j]);
+#pragma unroll
+    for (int c = 0; c < K; ++c) acc[c] += av * X[j * ldx + c];
+  }
+#pragma unroll
+  for (int c = 0; c < K; ++c) {
+    const T s = warp_sum(acc[c]);
+    if (lane == 0) Y[row * ldy + c] = combine(s, alpha, beta, Y + row * ldy + c);
+  }
+}
+
+// Dense, many columns: 64x64 output tile, 16-deep k-slices through shared memory,
+// 256 threads each owning a 4x4 micro-tile.  blockIdx.z = batch.
+template <class T, class S>
+__global__ void __launch_bounds__(256) dense_gemm_kernel(const S* __restrict__ A, int64_t lda, int64_t M,
+                                                         int64_t K, const T* __restrict__ X, int64_t ldx,
+                                                         int64_t bsx, T* __restrict__ Y, int64_t ldy,
+                                                         int64_t bsy, int64_t N, T alpha, T beta,
+                                                         const int* skip) {
+  if (skip && *skip) return;
+  constexpr int BM = 64, BN = 64, BK = 16;
+  __shared__ T As[BK][BM + 1];
+  __shared__ T Xs[BK][BN];
+  const int64_t b = blockIdx.z;
+  X += b * bsx;
+  Y += b * bsy;
+  const int64_t m0 = (int64_t)blockIdx.y * BM, n0 = (int64_t)blockIdx.x * BN;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  T acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
+  for (int64_t k0 = 0; k0 < K; k0 += BK) {
+    // A tile: BM x BK, 1024 elements, 4 per thread
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int idx = threadIdx.x + r * 256;
+      const int mm = idx / BK, kk = idx % BK;
+      const int64_t gm = m0 + mm, gk = k0 + kk;
+      As[kk][mm] = (gm < M && gk < K) ? cvt<T>(A[gm * lda + gk]) : T(0);
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int idx = threadIdx.x + r * 256;
+      const int kk = idx / BN, nn = idx % BN;
+      const int64_t gk = k0 + kk, gn = n0 + nn;
+      Xs[kk][nn] = (gk < K && gn < N) ? X[gk * ldx + gn] : T(0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      T av[4], xv[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) av[i] = As[kk][ty * 4 + i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) xv[j] = Xs[kk][tx * 4 + j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] += av[i] * xv[j];
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int64_t gm = m0 + ty * 4 + i;
+    if (gm >= M) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int64_t gn = n0 + tx * 4 + j;
+      if (gn < N) Y[gm * ldy + gn] = combine(acc[i][j], alpha, beta, Y + gm * ldy + gn);
+    }
+  }
+}
+
+// CSR, one column: TPR lanes per row, lanes stride over the row's entries.
+template <class T, class S, int TPR>
+__global__ void __launch_bounds__(256) csr_spmv_kernel(const int32_t* __restrict__ indptr,
+                                                       const int32_t* __restrict__ indices,
+                                                       const S* __restrict__ vals, int64_t rows,
+                                                       const T* __restrict__ X, int64_t ldx, int64_t bsx,
+                                                       T* __restrict__ Y, int64_t ldy, int64_t bsy, T alpha,
+                                                       T beta, const int* skip) {
+  if (skip && *skip) return;
+  const int64_t b = blockIdx.y;
+  X += b * bsx;
+  Y += b * bsy;
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t row = gt / TPR;
+  const int sub = (int)(gt % TPR);
+  T acc = T(0);
+  if (row < rows) {
+    const int32_t beg = indptr[row], end = indptr[row + 1];
+    for (int32_t j = beg + sub; j < end; j += TPR) acc += cvt<T>(vals[j]) * X[(int64_t)indices[j] * ldx];
+  }
+#pragma unroll
+  for (int o = TPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (row < rows && sub == 0) Y[row * ldy] = combine(acc, alpha, beta, Y + row * ldy);
+}
+
+// CSR, k columns: one warp per row, lanes over 32-column chunks; each entry reads a contiguous
+// row segment of X (coalesced).
+template <class T, class S>
+__global__ void __launch_bounds__(256) csr_spmm_kernel(const int32_t* __restrict__ indptr,
+                                                       const int32_t* __restrict__ indices,
+                                                       const S* __restrict__ vals, int64_t rows,
+                                                       const T* __restrict__ X, int64_t ldx, int64_t bsx,
+                                                       T* __restrict__ Y, int64_t ldy, int64_t bsy, int64_t k,
+                                                       T alpha, T beta, const int* skip) {
+  if (skip && *skip) return;
+  const int64_t b = blockIdx.z;
+  X += b * bsx;
+  Y += b * bsy;
+  const int lane = threadIdx.x & 31;
+  const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int64_t c = (int64_t)blockIdx.y * 32 + lane;
+  if (row >= rows) return;
+  const int32_t beg = indptr[row], end = indptr[row + 1];
+  T acc = T(0);
+  if (c < k)
+    for (int32_t j = beg; j < end; ++j) acc += cvt<T>(vals[j]) * X[(int64_t)indices[j] * ldx + c];
+  if (c < k) Y[row * ldy + c] = combine(acc, alpha, beta, Y + row * ldy + c);
+}
+
+// Diagonal: Y = alpha * d * X + beta * Y
+template <class T, class S>
+__global__ void diag_kernel(const S* __restrict__ d, int64_t rows, const T* __restrict__ X, int64_t ldx,
+                            int64_t bsx, T* __restrict__ Y, int64_t ldy, int64_t bsy, int64_t k, T alpha,
+                            T beta, const int* skip) {
+  if (skip && *skip) return;
+  const int64_t b = blockIdx.y;
+  X += b * bsx;
+  Y += b * bsy;
+  const int64_t total = rows * k;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < total; u += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = u / k, c = u - i * k;
+    const T v = cvt<T>(d[i]) * X[i * ldx + c];
+    Y[i * ldy + c] = combine(v, alpha, beta, Y + i * ldy + c);
+  }
+}
+
+// Y = alpha * X + beta * Y  (ScalarMul, Identity, Sum accumulation)
+template <class T>
+__global__ void axpby_kernel(const T* __restrict__ X, int64_t ldx, int64_t bsx, T* __restrict__ Y, int64_t ldy,
+                             int64_t bsy, int64_t rows, int64_t k, T alpha, T beta, const int* skip) {
+  if (skip && *skip) return;
+  const int64_t b = blockIdx.y;
+  X += b * bsx;
+  Y += b * bsy;
+  const int64_t total = rows * k;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < total; u += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = u / k, c = u - i * k;
+    Y[i * ldy + c] = combine(X[i * ldx + c], alpha, beta, Y + i * ldy + c);
+  }
+}
+
+// --------------------------------------------------------------------------------------------
+// launch helpers
+
+static int elementwise_grid(int64_t total) {
+  const int64_t want = ceil_div(total, 256);
+  const int64_t cap = (int64_t)num_sms() * 8;
+  return (int)(want < 1 ? 1 : (want > cap ? cap : want));
+}
+
+template <class T>
+int launch_axpby_b(const T* X, int64_t ldx, int64_t bsx, T* Y, int64_t ldy, int64_t bsy, int64_t rows, int64_t k,
+                   int64_t batch, T alpha, T beta, const int* skip, cudaStream_t st) {
+  if (rows * k == 0) return COLAGB_OK;
+  dim3 grid(elementwise_grid(rows * k), (unsigned)batch);
+  axpby_kernel<T><<<grid, 256, 0, st>>>(X, ldx, bsx, Y, ldy, bsy, rows, k, alpha, beta, skip);
+  COLAGB_CUDA(cudaGetLastError());
+  return COLAGB_OK;
+}
+
+template <class T>
+int launch_axpby(const T* X, int64_t ldx, T* Y, int64_t ldy, int64_t rows, int64_t k, T alpha, T beta,
+                 const int* skip, cudaStream_t st) {
+  return launch_axpby_b<T>(X, ldx, 0, Y, ldy, 0, rows, k, 1, alpha, beta, skip, st);
+}
+template int launch_axpby<float>(const float*, int64_t, float*, int64_t, int64_t, int64_t, float, float,
+                                 const int*, cudaStream_t);
+template int launch_axpby<double>(const double*, int64_t, double*, int64_t, int64_t, int64_t, double, double,
+                                  const int*, cudaStream_t);
+
+template <class T, class S>
+static int launch_dense(const colagb_op_node& nd, const T* X, int64_t ldx, int64_t bsx, T* Y, int64_t ldy,
+                        int64_t bsy, int64_t k, int64_t batch, T alpha, T beta, const int* skip, cudaStream_t st) {
+  const S* A = static_cast<const S*>(nd.data);
+  if (nd.rows == 0 || k == 0) return COLAGB_OK;
+  if (k <= 4) {
+    dim3 grid((unsigned)ceil_div(nd.rows, 8), (unsigned)batch);
+    switch (k) {
+      case 1: dense_gemv_kernel<T, S, 1><<<grid, 256, 0, st>>>(A, nd.ld, nd.rows, nd.cols, X, ldx, bsx, Y, ldy, bsy, alpha, beta, skip); break;
+      case 2: dense_gemv_kernel<T, S, 2><<<grid, 256, 0, st>>>(A, nd.ld, nd.rows, nd.cols, X, ldx, bsx, Y, ldy, bsy, alpha, beta, skip); break;
+      case 3: dense_gemv_kernel<T, S, 3><<<grid, 256, 0, st>>>(A, nd.ld, nd.rows, nd.cols, X, ldx, bsx, Y, ldy, bsy, alpha, beta, skip); break;
+      default: dense_gemv_kernel<T, S, 4><<<grid, 256, 0, st>>>(A, nd.ld, nd.rows, nd.cols, X, ldx, bsx, Y, ldy, bsy, alpha, beta, skip); break;
+    }
+  } else {
+    dim3 grid((unsigned)ceil_div(k, 64), (unsigned)ceil_div(nd.rows, 64), (unsigned)batch);
+    dense_gemm_kernel<T, S><<<grid, 256, 0, st>>>(A, nd.ld, nd.rows, nd.cols, X, ldx, bsx, Y, ldy, bsy, k, alpha,
+                                                  beta, skip);
+  }
+  COLAGB_CUDA(cudaGetLastError());
+  return COLAGB_OK;
+}
+
+template <class T, class S>
+static int launch_csr(const colagb_op_node& nd, const T* X, int64_t ldx, int64_t bsx, T* Y, int64_t ldy,
+                      int64_t bsy, int64_t k, int64_t batch, T alpha, T beta, const int* skip, cudaStream_t st) {
+  const S* v = static_cast<const S*>(nd.data);
+  if (nd.rows == 0 || k == 0) return COLAGB_OK;
+  if (k == 1) {
+    const double avg = nd.rows > 0 ? (double)nd.nnz / (double)nd.rows : 0.0;
+    int tpr = 1;
+    while (tpr < 32 && tpr * 2 <= avg) tpr *= 2;
+    dim3 grid((unsigned)ceil_div(nd.rows * tpr, 256), (unsigned)batch);
+#define COLAGB_CSR_CASE(N)                                                                                  \
+  case N:                                                                                                   \
+    csr_spmv_kernel<T, S, N><<<grid, 256, 0, st>>>(nd.indptr, nd.indices, v, nd.rows, X, ldx, bsx, Y, ldy, \
+                                                   bsy, alpha, beta, skip);                                 \
+    break;
+    switch (tpr) {
+      COLAGB_CSR_CASE(1)
+      COLAGB_CSR_CASE(2)
+      COLAGB_CSR_CASE(4)
+      COLAGB_CSR_CASE(8)
+      COLAGB_CSR_CASE(16)
+      COLAGB_CSR_CASE(32)
+    }
+#undef COLAGB_CSR_CASE
+  } else {
+    dim3 grid((unsigned)ceil_div(nd.rows, 8), (unsigned)ceil_div(k, 32), (unsigned)batch);
+    csr_spmm_kernel<T, S><<<grid, 256, 0, st>>>(nd.indptr, nd.indices, v, nd.rows, X, ldx, bsx, Y, ldy, bsy, k,
+                                                alpha, beta, skip);
+  }
+  COLAGB_CUDA(cudaGetLastError());
+  return COLAGB_OK;
+}
+
+template <class T, class S>
+static int launch_diag(const colagb_op_node& nd, const T* X, int64_t ldx, int64_t bsx, T* Y, int64_t ldy,
+                       int64_t bsy, int64_t k, int64_t batch, T alpha, T beta, const int* skip, cudaStream_t st) {
+  if (nd.rows * k == 0) return COLAGB_OK;
+  dim3 grid(elementwise_grid(nd.rows * k), (unsigned)batch);
+  diag_kernel<T, S><<<grid, 256, 0, st>>>(static_cast<const S*>(nd.data), nd.rows, X, ldx, bsx, Y, ldy, bsy, k,
+                                          alpha, beta, skip);
+  COLAGB_CUDA(cudaGetLastError());
+  return COLAGB_OK;
+}
+
+template <class T>
+struct LeafLaunch {
+  static int run(int kind, int32_t dtype, const colagb_op_node& nd, const T* X, int64_t ldx, int64_t bsx, T* Y,
+                 int64_t ldy, int64_t bsy, int64_t k, int64_t batch, T alpha, T beta, const int* skip,
+                 cudaStream_t st) {
+#define COLAGB_LEAF(S)                                                                                      \
+  do {                                                                                                      \
+    if (kind == COLAGB_OP_DENSE) return launch_dense<T, S>(nd, X, ldx, bsx, Y, ldy, bsy, k, batch, alpha, beta, skip, st); \
+    if (kind == COLAGB_OP_CSR) return launch_csr<T, S>(nd, X, ldx, bsx, Y, ldy, bsy, k, batch, alpha, beta, skip, st);     \
+    return launch_diag<T, S>(nd, X, ldx, bsx, Y, ldy, bsy, k, batch, alpha, beta, skip, st);                \
+  } while (0)
+    if (dtype == COLAGB_F32) COLAGB_LEAF(float);
+    if (dtype == COLAGB_BF16) COLAGB_LEAF(__nv_bfloat16);
+    if (dtype == COLAGB_F64) {
+      if constexpr (std::is_same<T, double>::value) COLAGB_LEAF(double);
+    }
+#undef COLAGB_LEAF
+    return fail(COLAGB_ERR_UNSUPPORTED, "leaf storage dtype not supported for this compute dtype");
+  }
+};
+
+// --------------------------------------------------------------------------------------------
+// executor
+
+template <class T>
+int op_apply(const colagb_op* op, int node, const T* X, int64_t ldx, int64_t bsx, T* Y, int64_t ldy, int64_t bsy,
+             int64_t k, int64_t batch, T alpha, T beta, Bump& ws, const int* skip, cudaStream_t st) {
+  const colagb_op_node& nd = op->nodes[node];
+  const std::vector<int32_t>& ch = op->children[node];
+  const bool measuring = ws.base == nullptr;
+  switch (nd.kind) {
+    case COLAGB_OP_DENSE:
+    case COLAGB_OP_CSR:
+    case COLAGB_OP_DIAG:
+      if (measuring) return COLAGB_OK;
+      return LeafLaunch<T>::run(nd.kind, nd.dtype, nd, X, ldx, bsx, Y, ldy, bsy, k, batch, alpha, beta, skip, st);
+    case COLAGB_OP_SCALAR:
+      if (measuring) return COLAGB_OK;
+      return launch_axpby_b<T>(X, ldx, bsx, Y, ldy, bsy, nd.rows, k, batch, alpha * (T)nd.scalar, beta, skip, st);
+    case COLAGB_OP_IDENTITY:
+      if (measuring) return COLAGB_OK;
+      return launch_axpby_b<T>(X, ldx, bsx, Y, ldy, bsy, nd.rows, k, batch, alpha, beta, skip, st);
+    case COLAGB_OP_SUM: {
+      for (size_t c = 0; c < ch.size(); ++c)
+        COLAGB_TRY(op_apply<T>(op, ch[c], X, ldx, bsx, Y, ldy, bsy, k, batch, alpha, c == 0 ? beta : T(1), ws, skip, st));
+      return COLAGB_OK;
+    }
+    case COLAGB_OP_PRODUCT: {
+      // c * I factors commute: fold them into alpha; then v <- M_last v, ..., Y = alpha * M_0 v + beta * Y
+      std::vector<int32_t> chain;
+      T a_eff = alpha;
+      for (int32_t c : ch) {
+        const colagb_op_node& m = op->nodes[c];
+        if (m.kind == COLAGB_OP_SCALAR) a_eff *= (T)m.scalar;
+        else if (m.kind != COLAGB_OP_IDENTITY) chain.push_back(c);
+      }
+      if (chain.empty()) {
+        if (measuring) return COLAGB_OK;
+        return launch_axpby_b<T>(X, ldx, bsx, Y, ldy, bsy, nd.rows, k, batch, a_eff, beta, skip, st);
+      }
+      const size_t mark = ws.used;
+      for (int64_t b = 0; b < batch; ++b) {
+        ws.used = mark;
+        const T* cur = X + b * bsx;
+        int64_t cur_ld = ldx;
+        for (int c = (int)chain.size() - 1; c >= 1; --c) {
+          const colagb_op_node& m = op->nodes[chain[c]];
+          T* tmp = ws.take<T>((size_t)m.rows * k);
+          COLAGB_TRY(op_apply<T>(op, chain[c], cur, cur_ld, 0, tmp, k, 0, k, 1, T(1), T(0), ws, skip, st));
+          cur = tmp;
+          cur_ld = k;
+        }
+        COLAGB_TRY(op_apply<T>(op, chain[0], cur, cur_ld, 0, Y + b * bsy, ldy, 0, k, 1, a_eff, beta, ws, skip, st));
+        if (measuring) break;
+      }
+      ws.release(mark);
+      return COLAGB_OK;
+    }
+    case COLAGB_OP_KRON: {
+      // X viewed as (c_0, ..., c_{m-1}, k).  Factor i contracts axis i:
+      //   out[pre, r_i, post*k] = M_i (r_i x c_i) @ in[pre, c_i, post*k]
+      // i.e. a batch of `pre` (c_i x post*k) blocks with row stride post*k.
+      const int m = (int)ch.size();
+      std::vector<int64_t> r(m), c(m);
+      for (int i = 0; i < m; ++i) {
+        r[i] = op->nodes[ch[i]].rows;
+        c[i] = op->nodes[ch[i]].cols;
+      }
+      int64_t maxsz = 1;
+      for (int i = -1; i < m; ++i) {  // i = -1: the input itself
+        int64_t s = 1;
+        for (int j = 0; j <= i; ++j) s *= r[j];
+        for (int j = i + 1; j < m; ++j) s *= c[j];
+        if (s > maxsz) maxsz = s;
+      }
+      const size_t mark = ws.used;
+      T* buf[2] = {ws.take<T>((size_t)maxsz * k), ws.take<T>((size_t)maxsz * k)};
+      for (int64_t b = 0; b < batch && !measuring; ++b) {
+        const T* in = X + b * bsx;
+        int which = 0;  // next scratch buffer to write
+        if (ldx != k) {  // make the input contiguous first
+          COLAGB_TRY(launch_axpby_b<T>(in, ldx, 0, buf[1], k, 0, nd.cols, k, 1, T(1), T(0), skip, st));
+          in = buf[1];
+          which = 0;
+        }
+        for (int i = 0; i < m; ++i) {
+          int64_t pre = 1, post = 1;
+          for (int j = 0; j < i; ++j) pre *= r[j];
+          for (int j = i + 1; j < m; ++j) post *= c[j];
+          const bool last = (i == m - 1);
+          const bool direct = last && ldy == k;
+          T* out = direct ? (Y + b * bsy) : buf[which];
+          COLAGB_TRY(op_apply<T>(op, ch[i], in, post * k, c[i] * post * k, out, post * k, r[i] * post * k, post * k,
+                                 pre, direct ? alpha : T(1), direct ? beta : T(0), ws, skip, st));
+          if (last && !direct)
+            COLAGB_TRY(launch_axpby_b<T>(out, k, 0, Y + b * bsy, ldy, 0, nd.rows, k, 1, alpha, beta, skip, st));
+          in = out;
+          which ^= 1;
+        }
+      }
+      if (measuring) {  // children of a Kronecker may need workspace of their own
+        for (int i = 0; i < m; ++i)
+          COLAGB_TRY(op_apply<T>(op, ch[i], nullptr, k, 0, nullptr, k, 0, k, 1, T(1), T(0), ws, skip, st));
+      }
+      ws.release(mark);
+      return COLAGB_OK;
+    }
+    case COLAGB_OP_BLOCKDIAG: {
+      int64_t ri = 0, ci = 0;
+      for (size_t cidx = 0; cidx < ch.size(); ++cidx) {
+        const colagb_op_node& m = op->nodes[ch[cidx]];
+        const int64_t mult = op->mult[node].empty() ? 1 : op->mult[node][cidx];
+        for (int64_t b = 0; b < batch; ++b) {
+          // the `mult` copies act on consecutive row slices: a batched apply
+          COLAGB_TRY(op_apply<T>(op, ch[cidx], X + b * bsx + ci * ldx, ldx, m.cols * ldx, Y + b * bsy + ri * ldy,
+                                 ldy, m.rows * ldy, k, mult, alpha, beta, ws, skip, st));
+          if (measuring) break;
+        }
+        ri += mult * m.rows;
+        ci += mult * m.cols;
+      }
+      return COLAGB_OK;
+    }
+    default:
+      return fail(COLAGB_ERR_UNSUPPORTED, "unknown operator node kind");
+  }
+}
+
+template int op_apply<float>(const colagb_op*, int, const float*, int64_t, int64_t, float*, int64_t, int64_t,
+                             int64_t, int64_t, float, float, Bump&, const int*, cudaStream_t);
+template int op_apply<double>(const colagb_op*, int, const double*, int64_t, int64_t, double*, int64_t, int64_t,
+                              int64_t, int64_t, double, double, Bump&, const int*, cudaStream_t);
+
+FusedForm fused_form(const colagb_op* op) {
+  FusedForm f;
+  const colagb_op_node& r = op->nodes[op->root];
+  auto is_leaf = [](const colagb_op_node& n) {
+    return (n.kind == COLAGB_OP_CSR || n.kind == COLAGB_OP_DENSE) && n.rows == n.cols;
+  };
+  if (is_leaf(r)) {
+    f.ok = true;
+    f.leaf = &r;
+    return f;
+  }
+  if (r.kind == COLAGB_OP_SUM && op->children[op->root].size() == 2) {
+    const auto& ch = op->children[op->root];
+    for (int a = 0; a < 2; ++a) {
+      const colagb_op_node& L = op->nodes[ch[a]];
+      const colagb_op_node& Sn = op->nodes[ch[1 - a]];
+      if (is_leaf(L) && (Sn.kind == COLAGB_OP_SCALAR || Sn.kind == COLAGB_OP_IDENTITY)) {
+        f.ok = true;
+        f.leaf = &L;
+        f.shift = Sn.kind == COLAGB_OP_SCALAR ? Sn.scalar : 1.0;
+        return f;
+      }
+    }
+  }
+  return f;
+}
+
+}  // namespace colagb
+
+// --------------------------------------------------------------------------------------------
+// C ABI
+using namespace colagb;
+
+extern "C" const char* colagb_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" int colagb_version(int32_t* version, int32_t* arch) {
+  if (version) *version = 100;
+  if (arch) *arch = 1003;
+  return COLAGB_OK;
+}
+
+static int validate_node(const colagb_op_node& n, int idx, int num_nodes) {
+  auto bad = [&](const char* what) {
+    return fail(COLAGB_ERR_INVALID, "operator node " + std::to_string(idx) + ": " + what);
+  };
+  if (n.rows < 0 || n.cols < 0) return bad("negative shape");
+  switch (n.kind) {
+    case COLAGB_OP_DENSE:
+      if (!n.data && n.rows * n.cols > 0) return bad("Dense without data");
+      if (n.ld < n.cols) return bad("Dense leading dimension smaller than cols");
+      break;
+    case COLAGB_OP_CSR:
+      if ((!n.indptr || !n.indices || !n.data) && n.nnz > 0) return bad("Sparse without indptr/indices/values");
+      if (!n.indptr && n.rows > 0) return bad("Sparse without indptr");
+      break;
+    case COLAGB_OP_DIAG:
+      if (n.rows != n.cols) return bad("Diagonal must be square");
+      if (!n.data && n.rows > 0) return bad("Diagonal without data");
+      break;
+    case COLAGB_OP_SCALAR:
+    case COLAGB_OP_IDENTITY:
+      if (n.rows != n.cols) return bad("ScalarMul/Identity must be square");
+      break;
+    case COLAGB_OP_SUM:
+    case COLAGB_OP_PRODUCT:
+    case COLAGB_OP_KRON:
+    case COLAGB_OP_BLOCKDIAG:
+      if (n.num_children <= 0 || !n.children) return bad("composite without children");
+      for (int c = 0; c < n.num_children; ++c)
+        if (n.children[c] < 0 || n.children[c] >= num_nodes) return bad("child index out of range");
+      break;
+    default:
+      return bad("unknown kind");
+  }
+  if (n.kind == COLAGB_OP_DENSE || n.kind == COLAGB_OP_CSR || n.kind == COLAGB_OP_DIAG) {
+    if (n.dtype != COLAGB_F32 && n.dtype != COLAGB_F64 && n.dtype != COLAGB_BF16) return bad("unknown dtype");
+  }
+  return COLAGB_OK;
+}
+
+static int check_shapes(const colagb_op* op, int node, std::vector<int>& state) {
+  // state: 0 = unvisited, 1 = on stack, 2 = done (cycle detection)
+  if (state[node] == 1) return fail(COLAGB_ERR_INVALID, "operator graph has a cycle");
+  if (state[node] == 2) return COLAGB_OK;
+  state[node] = 1;
+  const colagb_op_node& n = op->nodes[node];
+  const auto& ch = op->children[node];
+  for (int c : ch) COLAGB_TRY(check_shapes(op, c, state));
+  auto dims = [&](int c) { return std::make_pair(op->nodes[c].rows, op->nodes[c].cols); };
+  switch (n.kind) {
+    case COLAGB_OP_SUM:
+      for (int c : ch)
+        if (dims(c) != std::make_pair(n.rows, n.cols)) return fail(COLAGB_ERR_INVALID, "Sum child shape mismatch");
+      break;
+    case COLAGB_OP_PRODUCT:
+      if (op->nodes[ch.front()].rows != n.rows || op->nodes[ch.back()].cols != n.cols)
+        return fail(COLAGB_ERR_INVALID, "Product outer shape mismatch");
+      for (size_t i = 0; i + 1 < ch.size(); ++i)
+        if (op->nodes[ch[i]].cols != op->nodes[ch[i + 1]].rows)
+          return fail(COLAGB_ERR_INVALID, "Product inner dimension mismatch");
+      break;
+    case COLAGB_OP_KRON: {
+      int64_t r = 1, c = 1;
+      for (int x : ch) {
+        r *= op->nodes[x].rows;
+        c *= op->nodes[x].cols;
+      }
+      if (r != n.rows || c != n.cols) return fail(COLAGB_ERR_INVALID, "Kronecker shape mismatch");
+      break;
+    }
+    case COLAGB_OP_BLOCKDIAG: {
+      int64_t r = 0, c = 0;
+      for (size_t i = 0; i < ch.size(); ++i) {
+        const int64_t m = op->mult[node].empty() ? 1 : op->mult[node][i];
+        if (m < 1) return fail(COLAGB_ERR_INVALID, "BlockDiag multiplicity must be >= 1");
+        r += m * op->nodes[ch[i]].rows;
+        c += m * op->nodes[ch[i]].cols;
+      }
+      if (r != n.rows || c != n.cols) return fail(COLAGB_ERR_INVALID, "BlockDiag shape mismatch");
+      break;
+    }
+    default:
+      break;
+  }
+  state[node] = 2;
+  return COLAGB_OK;
+}
+
+extern "C" int colagb_op_create(const colagb_op_node* nodes, int32_t num_nodes, int32_t root, colagb_op** out) {
+  if (!nodes || !out || num_nodes <= 0 || root < 0 || root >= num_nodes)
+    return fail(COLAGB_ERR_INVALID, "colagb_op_create: bad arguments");
+  *out = nullptr;
+  for (int i = 0; i < num_nodes; ++i) COLAGB_TRY(validate_node(nodes[i], i, num_nodes));
+  colagb_op* op = new colagb_op();
+  op->nodes.assign(nodes, nodes + num_nodes);
+  op->children.resize(num_nodes);
+  op->mult.resize(num_nodes);
+  op->root = root;
+  bool any64 = false;
+  for (int i = 0; i < num_nodes; ++i) {
+    const colagb_op_node& n = nodes[i];
+    if (n.num_children > 0) op->children[i].assign(n.children, n.children + n.num_children);
+    if (n.kind == COLAGB_OP_BLOCKDIAG && n.multiplicities)
+      op->mult[i].assign(n.multiplicities, n.multiplicities + n.num_children);
+    op->nodes[i].children = nullptr;        // the copies above own these now
+    op->nodes[i].multiplicities = nullptr;
+    if ((n.kind == COLAGB_OP_DENSE || n.kind == COLAGB_OP_CSR || n.kind == COLAGB_OP_DIAG) && n.dtype == COLAGB_F64)
+      any64 = true;
+  }
+  op->compute_dtype = any64 ? COLAGB_F64 : COLAGB_F32;
+  std::vector<int> state(num_nodes, 0);
+  int s = check_shapes(op, root, state);
+  if (s != COLAGB_OK) {
+    delete op;
+    return s;
+  }
+  *out = op;
+  return COLAGB_OK;
+}
+
+extern "C" int colagb_op_free(colagb_op* op) {
+  delete op;
+  return COLAGB_OK;
+}
+
+extern "C" int colagb_op_info(const colagb_op* op, int64_t* rows, int64_t* cols, int32_t* compute_dtype) {
+  if (!op) return fail(COLAGB_ERR_INVALID, "null operator");
+  if (rows) *rows = op->nodes[op->root].rows;
+  if (cols) *cols = op->nodes[op->root].cols;
+  if (compute_dtype) *compute_dtype = op->compute_dtype;
+  return COLAGB_OK;
+}
+
+extern "C" int colagb_matmat_workspace_bytes(const colagb_op* op, int64_t k, size_t* bytes) {
+  if (!op || !bytes || k < 0) return fail(COLAGB_ERR_INVALID, "colagb_matmat_workspace_bytes: bad arguments");
+  Bump ws(nullptr, 0);
+  int s = op->compute_dtype == COLAGB_F64
+              ? op_apply<double>(op, op->root, nullptr, k, 0, nullptr, k, 0, k, 1, 1.0, 0.0, ws, nullptr, 0)
+              : op_apply<float>(op, op->root, nullptr, k, 0, nullptr, k, 0, k, 1, 1.f, 0.f, ws, nullptr, 0);
+  if (s != COLAGB_OK) return s;
+  *bytes = ws.peak;
+  return COLAGB_OK;
+}
+
+extern "C" int colagb_matmat(const colagb_op* op, const void* X, int64_t ldx, void* Y, int64_t ldy, int64_t k,
+                             double alpha, double beta, void* workspace, size_t workspace_bytes, void* stream) {
+  if (!op) return fail(COLAGB_ERR_INVALID, "null operator");
+  const colagb_op_node& r = op->nodes[op->root];
+  if (k < 0 || ldx < k || ldy < k) return fail(COLAGB_ERR_INVALID, "colagb_matmat: bad k / leading dimensions");
+  if ((r.cols * k > 0 && !X) || (r.rows * k > 0 && !Y)) return fail(COLAGB_ERR_INVALID, "colagb_matmat: null X/Y");
+  size_t need = 0;
+  COLAGB_TRY(colagb_matmat_workspace_bytes(op, k, &need));
+  if (need > 0 && (workspace == nullptr || workspace_bytes < need))
+    return fail(COLAGB_ERR_WORKSPACE, "colagb_matmat: workspace too small (need " + std::to_string(need) + " bytes)");
+  Bump ws(workspace, workspace_bytes);
+  cudaStream_t st = as_stream(stream);
+  if (op->compute_dtype == COLAGB_F64)
+    return op_apply<double>(op, op->root, static_cast<const double*>(X), ldx, 0, static_cast<double*>(Y), ldy, 0, k,
+                            1, alpha, beta, ws, nullptr, st);
+  return op_apply<float>(op, op->root, static_cast<const float*>(X), ldx, 0, static_cast<float*>(Y), ldy, 0, k, 1,
+                         (float)alpha, (float)beta, ws, nullptr, st);
+}

@@ -1,0 +1,143 @@
+"""Seeded synthetic inputs with the shapes and value distributions of the benchmark configurations
+(no public dataset is involved).  Generation uses tensor ops on the target device; it is set-up
+work, not part of any timed Krylov loop.
+"""
+from __future__ import annotations
+
+import math
+
+import torch
+
+from .linalg.batched import BatchedCSR
+
+
+# ---------------------------------------------------------------------------------------------
+# dense SPD with a log-uniform spectrum (Q from the QR of an N(0,1) matrix)
+
+def dense_spd(n: int = 2048, seed: int = 0, lo: float = 1e-2, hi: float = 1e2, dtype=torch.float32, device="cpu"):
+    """A = Q diag(lam) Q^T, lam log-uniform in [lo, hi]; b ~ N(0, 1).  Returns (A, b, lam)."""
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    M = torch.randn(n, n, dtype=torch.float64, generator=g)
+    Q, _ = torch.linalg.qr(M)
+    lam = torch.exp(torch.empty(n, dtype=torch.float64).uniform_(math.log(lo), math.log(hi), generator=g))
+    A = ((Q * lam) @ Q.T)
+    A = 0.5 * (A + A.T)
+    b = torch.randn(n, dtype=torch.float64, generator=g)
+    return A.to(dtype).to(device), b.to(dtype).to(device), lam
+
+
+# ---------------------------------------------------------------------------------------------
+# 2-D / 3-D variable-coefficient diffusion (finite volumes, harmonic-mean faces, Dirichlet walls)
+
+def grid_pattern_2d(m: int, device="cpu"):
+    """CSR pattern of the 5-point stencil on an m x m grid, rows i*m + j, columns sorted."""
+    n = m * m
+    p = torch.arange(n, device=device)
+    i, j = p // m, p % m
+    cand = torch.stack([p - m, p - 1, p, p + 1, p + m], 1)
+    ok = torch.stack([i > 0, j > 0, torch.ones_like(i, dtype=torch.bool), j < m - 1, i < m - 1], 1)
+    counts = ok.sum(1)
+    indptr = torch.zeros(n + 1, dtype=torch.int64, device=device)
+    indptr[1:] = torch.cumsum(counts, 0)
+    indices = cand[ok]
+    return indptr.to(torch.int32), indices.to(torch.int32), ok
+
+
+def diffusion_values_2d(a: torch.Tensor, ok: torch.Tensor) -> torch.Tensor:
+    """CSR values (float32, pattern order of grid_pattern_2d) for cell coefficients a (S, m, m)."""
+    S, m, _ = a.shape
+    a = a.double()
+
+    def harm(x, y):
+        return 2 * x * y / (x + y)
+    tN = torch.full_like(a, 0.0)
+    tS = torch.full_like(a, 0.0)
+    tW = torch.full_like(a, 0.0)
+    tE = torch.full_like(a, 0.0)
+    tN[:, 1:, :] = harm(a[:, 1:, :], a[:, :-1, :])   # face to row i-1
+    tN[:, 0, :] = 2 * a[:, 0, :]
+    tS[:, :-1, :] = harm(a[:, :-1, :], a[:, 1:, :])  # face to row i+1
+    tS[:, -1, :] = 2 * a[:, -1, :]
+    tW[:, :, 1:] = harm(a[:, :, 1:], a[:, :, :-1])
+    tW[:, :, 0] = 2 * a[:, :, 0]
+    tE[:, :, :-1] = harm(a[:, :, :-1], a[:, :, 1:])
+    tE[:, :, -1] = 2 * a[:, :, -1]
+    diag = tN + tS + tW + tE
+    full = torch.stack([-tN, -tW, diag, -tE, -tS], -1).reshape(S, m * m, 5)
+    return full[:, ok].to(torch.float32)
+
+
+def matern32_field(m: int, ell: float, var: float, gen: torch.Generator, device) -> torch.Tensor:
+    """Gaussian random field with Matern-3/2 covariance on the unit square (m x m cells), by
+    circulant embedding on a periodic 2m x 2m grid (spectral density (3/ell^2 + 4 pi^2 |k|^2)^-5/2)."""
+    N = 2 * m
+    h = 1.0 / m
+    k = torch.fft.fftfreq(N, d=h, device=device, dtype=torch.float64)
+    k2 = k[:, None] ** 2 + k[None, :] ** 2
+    S = (3.0 / ell**2 + 4 * math.pi**2 * k2) ** (-2.5)
+    w = torch.randn(N, N, generator=gen, device=device, dtype=torch.float64)
+    f = torch.fft.ifft2(torch.fft.fft2(w) * torch.sqrt(S)).real
+    f = f * math.sqrt(var / S.mean().item())
+    return f[:m, :m]
+
+
+def diffusion_family_2d(seeds, m: int = 512, device="cuda", ell_range=(0.05, 0.2), var_range=(0.5, 2.0)):
+    """The learned-preconditioner family: one operator per seed on a shared m x m 5-point pattern.
+
+    Coefficient field exp(f), f a Matern-3/2 GRF with lengthscale ~ U[0.05, 0.2] and variance
+    ~ U[0.5, 2]; b ~ N(0, 1).  Returns (BatchedCSR, B (S, n) float64, coeff (S, m, m) float32,
+    params list)."""
+    indptr, indices, ok = grid_pattern_2d(m, device)
+    vals, Bs, coeffs, params = [], [], [], []
+    for s in seeds:
+        gen = torch.Generator(device=device).manual_seed(int(s))
+        u = torch.rand(2, generator=gen, device=device, dtype=torch.float64).cpu()
+        ell = ell_range[0] + (ell_range[1] - ell_range[0]) * float(u[0])
+        var = var_range[0] + (var_range[1] - var_range[0]) * float(u[1])
+        f = matern32_field(m, ell, var, gen, device)
+        a = torch.exp(f)
+        coeffs.append(a.float())
+        vals.append(diffusion_values_2d(a[None], ok)[0])
+        Bs.append(torch.randn(m * m, generator=gen, device=device, dtype=torch.float64))
+        params.append((ell, var))
+    return BatchedCSR(indptr, indices, torch.stack(vals)), torch.stack(Bs), torch.stack(coeffs), params
+
+
+def diffusion_3d(m: int = 128, seed: int = 1, shift: float = 1e-3, device="cuda"):
+    """7-point variable-coefficient diffusion on an m^3 grid, cell coefficients exp(g), g ~ N(0,1)
+    i.i.d. per cell, harmonic-mean faces, Dirichlet walls, plus shift * I.  Returns CSR arrays."""
+    n = m**3
+    gen = torch.Generator(device=device).manual_seed(seed)
+    a = torch.exp(torch.randn(m, m, m, generator=gen, device=device, dtype=torch.float64))
+    p = torch.arange(n, device=device)
+    z, y, x = p // (m * m), (p // m) % m, p % m
+    offs = [(-m * m, z > 0, (-1, 0, 0)), (-m, y > 0, (0, -1, 0)), (-1, x > 0, (0, 0, -1)), (0, None, None),
+            (1, x < m - 1, (0, 0, 1)), (m, y < m - 1, (0, 1, 0)), (m * m, z < m - 1, (1, 0, 0))]
+    af = a.reshape(-1)
+    diag = torch.full((n,), shift, dtype=torch.float64, device=device)
+    cols, vals, oks = [], [], []
+    for off, valid, _ in offs:
+        if off == 0:
+            continue
+        nb = (p + off).clamp(0, n - 1)
+        t_int = 2 * af * af[nb] / (af + af[nb])
+        t = torch.where(valid, t_int, 2 * af)
+        diag += t
+    for off, valid, _ in offs:
+        if off == 0:
+            cols.append(p)
+            vals.append(diag)
+            oks.append(torch.ones(n, dtype=torch.bool, device=device))
+        else:
+            nb = (p + off).clamp(0, n - 1)
+            t_int = 2 * af * af[nb] / (af + af[nb])
+            cols.append(p + off)
+            vals.append(-t_int)
+            oks.append(valid)
+    C = torch.stack(cols, 1)
+    V = torch.stack(vals, 1)
+    OK = torch.stack(oks, 1)
+    counts = OK.sum(1)
+    indptr = torch.zeros(n + 1, dtype=torch.int64, device=device)
+    indptr[1:] = torch.cumsum(counts, 0)
+    return indptr.to(torch.int32), C[OK].to(torch.int32), V[OK].to(torch.float32)

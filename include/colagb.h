@@ -1,0 +1,235 @@
+/*
+ * colagb.h -- C ABI of libcolagb, the sm_103a implementation of CoLA's
+ * iterative Krylov hot path (CG for solve/inv, Lanczos for eig, stochastic
+ * Lanczos quadrature for logdet/trace) and of the structured matvecs those
+ * loops call.
+ *
+ * Conventions
+ *   - Every pointer to array data is a DEVICE pointer unless the comment says
+ *     "host".  Nothing here takes or returns a framework tensor type.
+ *   - A block of k vectors of length n ("n x k") is row-major with a leading
+ *     dimension ld >= k: element (i, c) lives at X[i * ld + c].  This is the
+ *     layout of CoLA's (n,) / (n, k) right-hand sides (cola/linalg/inverse/cg.py:59-64).
+ *   - Every entry point returns an int status: COLAGB_OK (0) or an error code;
+ *     colagb_last_error() gives a human readable message for the calling thread.
+ *   - Work is enqueued on the caller's stream.  Entry points that must make a
+ *     host decision (the CG / Lanczos stop rules) synchronise that stream.
+ *   - Temporary device memory is supplied by the caller through a workspace
+ *     pointer whose size comes from the matching *_workspace_bytes query; the
+ *     library itself never allocates device memory on these paths.
+ */
+#ifndef COLAGB_H
+#define COLAGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define COLAGB_OK 0
+#define COLAGB_ERR_INVALID 1      /* bad argument: shape, dtype, null pointer  (Python: ValueError) */
+#define COLAGB_ERR_CUDA 2         /* CUDA runtime error                        (Python: RuntimeError) */
+#define COLAGB_ERR_TIMEOUT 3      /* a bounded device wait gave up             (Python: RuntimeError) */
+#define COLAGB_ERR_UNSUPPORTED 4  /* operator / dtype combination not handled   (Python: NotImplementedError) */
+#define COLAGB_ERR_WORKSPACE 5    /* workspace smaller than the query returned  (Python: ValueError) */
+
+/* ---- element types ------------------------------------------------------ */
+#define COLAGB_F32 0
+#define COLAGB_F64 1
+#define COLAGB_BF16 2
+
+/* ---- per-system solver status (colagb_cg_batched_*) --------------------- */
+#define COLAGB_SYS_RUNNING 0
+#define COLAGB_SYS_CONVERGED 1
+#define COLAGB_SYS_MAX_ITERS 2
+#define COLAGB_SYS_BREAKDOWN 3    /* <p, A p> <= 0: operator not SPD in working precision */
+#define COLAGB_SYS_NAN 4
+#define COLAGB_SYS_FALLBACK 5     /* learned preconditioner stalled; finished with Jacobi */
+
+const char* colagb_last_error(void);
+/* Library version and the sm architecture it was built for (e.g. 1003 = sm_103a). */
+int colagb_version(int32_t* version, int32_t* arch);
+
+/* ======================================================================== *
+ *  Operator programs                                                       *
+ *  A LinearOperator tree (cola/ops/operators.py) lowered to a flat array   *
+ *  of nodes.  The handle keeps a copy of the node array; the device arrays *
+ *  it points to stay owned by the caller and must outlive the handle.      *
+ * ======================================================================== */
+#define COLAGB_OP_DENSE 1      /* Dense(A)                 operators.py:12-28   */
+#define COLAGB_OP_CSR 2        /* Sparse(data, row, col)   operators.py:48-81   */
+#define COLAGB_OP_DIAG 3       /* Diagonal(d)              operators.py:323-339 */
+#define COLAGB_OP_SCALAR 4     /* ScalarMul(c) = c * I     operators.py:84-101  */
+#define COLAGB_OP_IDENTITY 5   /* Identity / I_like        operators.py:104-136 */
+#define COLAGB_OP_SUM 6        /* Sum(*Ms)                 operators.py:168-196 */
+#define COLAGB_OP_PRODUCT 7    /* Product(*Ms)             operators.py:139-165 */
+#define COLAGB_OP_KRON 8       /* Kronecker(*Ms)           operators.py:199-228 */
+#define COLAGB_OP_BLOCKDIAG 9  /* BlockDiag(*Ms, mult)     operators.py:278-320 */
+
+typedef struct colagb_op_node {
+  int32_t kind;            /* COLAGB_OP_* */
+  int32_t dtype;           /* storage type of data (DENSE values, CSR values, DIAG entries) */
+  int64_t rows, cols;
+  const void* data;        /* DENSE: row-major matrix; CSR: values[nnz]; DIAG: diagonal[rows] */
+  int64_t ld;              /* DENSE: row stride in elements (>= cols) */
+  const int32_t* indptr;   /* CSR: rows + 1 row offsets */
+  const int32_t* indices;  /* CSR: nnz column indices */
+  int64_t nnz;             /* CSR */
+  double scalar;           /* SCALAR: c */
+  const int32_t* children; /* host: indices of child nodes in the node array */
+  int32_t num_children;
+  const int64_t* multiplicities; /* host, BLOCKDIAG: one per child, NULL = all 1 */
+} colagb_op_node;
+
+typedef struct colagb_op colagb_op; /* opaque */
+
+/* Build a handle for the operator rooted at nodes[root]. */
+int colagb_op_create(const colagb_op_node* nodes, int32_t num_nodes, int32_t root, colagb_op** out);
+int colagb_op_free(colagb_op* op);
+/* Shape and compute type (COLAGB_F32 or COLAGB_F64) of the vectors the operator acts on. */
+int colagb_op_info(const colagb_op* op, int64_t* rows, int64_t* cols, int32_t* compute_dtype);
+
+/* Y = alpha * (op @ X) + beta * Y, X: cols x k, Y: rows x k, vector type = compute_dtype.
+ * Replaces LinearOperator.__matmul__ -> _matmat (cola/ops/operator_base.py:97-106). */
+int colagb_matmat_workspace_bytes(const colagb_op* op, int64_t k, size_t* bytes);
+int colagb_matmat(const colagb_op* op, const void* X, int64_t ldx, void* Y, int64_t ldy, int64_t k,
+                  double alpha, double beta, void* workspace, size_t workspace_bytes, void* stream);
+
+/* ======================================================================== *
+ *  Conjugate gradients                                                     *
+ *  Replaces cg() / run_batched_cg() / take_cg_step()                       *
+ *  (cola/linalg/inverse/cg.py:39-178) and the while_loop_winfo driver      *
+ *  (cola/utils/torch_tqdm.py:7-71).  Semantics follow the reference: each  *
+ *  column of B is normalised by its norm, r0 = B/|B| - A X0, the loop runs *
+ *  while any column has |r| > tol*|r0| + tol and k < max_iters, alpha and  *
+ *  beta use the 1e-40 safe division and are zeroed once |r| < 1e-40, and   *
+ *  the solution is scaled back by |B|.                                     *
+ * ======================================================================== */
+typedef struct colagb_cg_params {
+  double tol;            /* CG(tol=...) */
+  int32_t max_iters;     /* CG(max_iters=...) */
+  int32_t check_every;   /* host polls the device stop flag every this many iterations (0 = 16) */
+  int32_t allow_fused;   /* 1: use the single-launch persistent kernel when the operator allows it */
+  int32_t reserved;
+  int64_t spin_limit;    /* grid-barrier spin bound of the persistent kernel (0 = default) */
+} colagb_cg_params;
+
+typedef struct colagb_cg_result {
+  int32_t iterations;    /* k, the number of CG steps taken (state[1] of run_batched_cg) */
+  int32_t fused;         /* 1 if the persistent single-launch kernel ran */
+  int32_t status;        /* COLAGB_OK or COLAGB_ERR_TIMEOUT */
+  int32_t reserved;
+} colagb_cg_result;
+
+/* P may be NULL (identity).  X holds x0 on entry and the solution on exit.
+ * residual_history (device, compute dtype, max_iters + 1 entries, may be NULL) receives
+ * mean_c |r_c| (normalised scale) after each step, index 0 = initial residual; this is the
+ * quantity the reference's info['errors'] records. */
+int colagb_cg_workspace_bytes(const colagb_op* A, const colagb_op* P, int64_t k, size_t* bytes);
+int colagb_cg_solve(const colagb_op* A, const colagb_op* P, const void* B, int64_t ldb, void* X, int64_t ldx,
+                    int64_t k, const colagb_cg_params* params, void* residual_history,
+                    void* workspace, size_t workspace_bytes, colagb_cg_result* result, void* stream);
+
+/* ------------------------------------------------------------------------ *
+ *  Batched independent SPD systems sharing one CSR sparsity pattern        *
+ *  (a family of discretised operators: same mesh, different coefficients). *
+ *  S systems, each n x n with nnz entries; values[s * nnz + j].            *
+ *  Solved to a TRUE relative residual |b - A x| / |b| <= tol measured in   *
+ *  FP64, by FP32 preconditioned CG inside FP64 iterative refinement.       *
+ *  The reference solves such systems one call at a time                    *
+ *  (cola/linalg/inverse/inv.py:66-69 per system); here one persistent      *
+ *  launch per refinement sweep advances all of them with per-system        *
+ *  convergence masks.                                                      *
+ * ------------------------------------------------------------------------ */
+#define COLAGB_PREC_NONE 0
+#define COLAGB_PREC_JACOBI 1   /* CG(P=Diagonal(1/diag(A))) */
+#define COLAGB_PREC_FSAI 2     /* P = G^T G, G lower triangular on A's lower pattern */
+
+typedef struct colagb_batched_csr {
+  int64_t n, nnz, num_systems;
+  const int32_t* indptr;   /* n + 1 */
+  const int32_t* indices;  /* nnz, sorted within each row */
+  const float* values;     /* num_systems * nnz */
+  /* FSAI factor G (only for COLAGB_PREC_FSAI): lower pattern and its transpose */
+  int64_t g_nnz;
+  const int32_t* g_indptr;    /* n + 1 */
+  const int32_t* g_indices;   /* g_nnz */
+  const int32_t* gt_indptr;   /* n + 1, pattern of G^T */
+  const int32_t* gt_indices;  /* g_nnz */
+  const int32_t* gt_perm;     /* g_nnz: G^T entry e holds G value gt_perm[e] */
+  const float* g_values;      /* num_systems * g_nnz */
+} colagb_batched_csr;
+
+typedef struct colagb_ir_params {
+  double tol;            /* target true relative residual (FP64), e.g. 1e-8 */
+  double inner_tol;      /* relative reduction asked of each inner FP32 PCG solve */
+  int32_t max_sweeps;    /* refinement sweeps */
+  int32_t max_inner_iters;
+  int32_t preconditioner;/* COLAGB_PREC_* */
+  int32_t fallback;      /* 1: a system whose FSAI-PCG stalls restarts with Jacobi */
+  int64_t spin_limit;    /* grid-barrier spin bound (0 = default) */
+} colagb_ir_params;
+
+typedef struct colagb_ir_result {
+  int32_t sweeps;
+  int32_t total_inner_iters;   /* sum over sweeps of the max inner iterations */
+  int32_t status;              /* COLAGB_OK or COLAGB_ERR_TIMEOUT */
+  int32_t reserved;
+} colagb_ir_result;
+
+/* B: num_systems x n FP64 right-hand sides; X: num_systems x n FP64 solutions (out).
+ * per_system_iters / per_system_status / relres (device, may be NULL): inner iterations summed
+ * over sweeps, COLAGB_SYS_* and the final FP64 true relative residual of each system. */
+int colagb_cg_batched_csr_workspace_bytes(const colagb_batched_csr* A, const colagb_ir_params* params,
+                                          size_t* bytes);
+int colagb_cg_batched_csr_solve(const colagb_batched_csr* A, const double* B, double* X,
+                                const colagb_ir_params* params, int32_t* per_system_iters,
+                                int32_t* per_system_status, double* relres, void* workspace,
+                                size_t workspace_bytes, colagb_ir_result* result, void* stream);
+
+/* ======================================================================== *
+ *  Lanczos with full reorthogonalisation                                   *
+ *  Replaces lanczos() / lanczos_fact() / do_double_gram()                  *
+ *  (cola/linalg/decompositions/lanczos.py:185-296).  bs start vectors are  *
+ *  run together (the probe block of LanczosUnary, unary.py:46-60).         *
+ *  V0: n x bs start vectors.  basis: (max_iters + 2) x n x bs, slot j holds *
+ *  the reference's V[..., j] (slot 0 stays zero).  diag: bs x max_iters and *
+ *  subdiag: bs x (max_iters + 1), compute dtype, exactly the reference's    *
+ *  `diag` / `subdiag` arrays.  *steps = the reference's final loop index i. *
+ * ======================================================================== */
+typedef struct colagb_lanczos_params {
+  double tol;
+  int32_t max_iters;
+  int32_t check_every;   /* host polls the device stop flag every this many steps (0 = 8) */
+} colagb_lanczos_params;
+
+int colagb_lanczos_workspace_bytes(const colagb_op* A, int64_t bs, int32_t max_iters, size_t* bytes);
+int colagb_lanczos(const colagb_op* A, const void* V0, int64_t ldv0, int64_t bs,
+                   const colagb_lanczos_params* params, void* basis, void* diag, void* subdiag,
+                   int32_t* steps, void* workspace, size_t workspace_bytes, void* stream);
+
+/* Ritz combination: out (n x bs) = for each probe b: sum_j basis[j+1][:, b] * coef[b][j], j < m.
+ * Forms Q @ w for the LanczosUnary quadrature (unary.py:58-59) and Ritz vectors. */
+int colagb_basis_combine(const void* basis, int64_t n, int64_t bs, int32_t m, const void* coef, int64_t ldc,
+                         void* out, int32_t dtype, void* stream);
+
+/* ======================================================================== *
+ *  FP64 symmetric tridiagonal eigensolver (batched), implicit QL with      *
+ *  Wilkinson shifts.  Replaces xnp.eigh(T) in lanczos_eigs (lanczos.py:57), *
+ *  LanczosUnary (unary.py:52) and slq_fwd (tbd/slq.py:44).                 *
+ *  a: batch x m diagonal, b: batch x m off-diagonal (b[i] couples i, i+1;  *
+ *  b[m-1] ignored).  evals: batch x m ascending.  first_row: batch x m,    *
+ *  row 0 of the eigenvector matrix (Gauss quadrature weights), may be NULL. *
+ *  evecs: batch x m x m (row-major, column j = eigenvector j), may be NULL. *
+ *  status: batch ints, 0 = converged, 1 = iteration limit hit.            *
+ * ======================================================================== */
+int colagb_tridiag_eig_f64(const double* a, const double* b, int64_t m, int64_t batch, double* evals,
+                           double* first_row, double* evecs, int32_t* status, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* COLAGB_H */

@@ -1,0 +1,348 @@
+"""CUDA path (through the C ABI) against the oracle, the golden vectors recorded from the reference,
+and FP64 references.  Tolerances are stated per test."""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+import cola_gb300 as cola
+from cola_gb300.linalg import CG, Hutch, Lanczos
+from cola_gb300.linalg.prng import PRNGKey, next_key, randn
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda"
+
+
+def rel(a, b):
+    a = a.detach().double().cpu().numpy() if isinstance(a, torch.Tensor) else np.asarray(a, dtype=np.float64)
+    b = b.detach().double().cpu().numpy() if isinstance(b, torch.Tensor) else np.asarray(b, dtype=np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def T(x, dtype=None):
+    t = torch.as_tensor(np.asarray(x))
+    return t.to(DEV, dtype=dtype) if dtype else t.to(DEV)
+
+
+def csr(rows, cols, vals, n, dtype):
+    return cola.ops.Sparse(T(vals, dtype), T(rows), T(cols), (n, n))
+
+
+# ---------------------------------------------------------------------------------------------
+# structured matvecs
+
+@pytest.mark.parametrize("dtype,tol", [(torch.float32, 1e-5), (torch.float64, 1e-12), (torch.bfloat16, 1e-2)])
+@pytest.mark.parametrize("k", [1, 3, 17, 70])
+def test_dense_matmat(dtype, tol, k):
+    g = torch.Generator().manual_seed(k)
+    A = torch.randn(131, 97, generator=g)
+    X = torch.randn(97, k, generator=g)
+    op = cola.ops.Dense(A.to(DEV, dtype))
+    cdt = torch.float64 if dtype == torch.float64 else torch.float32
+    Y = op @ X.to(DEV, cdt)
+    ref = A.to(dtype).double() @ X.to(cdt).double()
+    assert rel(Y, ref) < tol
+
+
+@pytest.mark.parametrize("k", [1, 2, 5, 33, 64])
+@pytest.mark.parametrize("dtype,tol", [(torch.float32, 1e-5), (torch.float64, 1e-12)])
+def test_csr_matmat(k, dtype, tol):
+    from cola_gb300.workloads import diffusion_3d
+    ip, ix, v = diffusion_3d(m=9, device=DEV)
+    n = 9**3
+    counts = (ip[1:] - ip[:-1]).long()
+    rows = torch.repeat_interleave(torch.arange(n, device=DEV), counts)
+    op = cola.ops.Sparse(v.to(dtype), rows, ix.long(), (n, n))
+    X = torch.randn(n, k, device=DEV, dtype=dtype)
+    dense = torch.zeros(n, n, dtype=torch.float64, device=DEV)
+    dense[rows, ix.long()] = v.double()
+    assert rel(op @ X, dense @ X.double()) < tol
+
+
+def test_sparse_known_answer(golden):
+    g = golden("ops_sparse_known")
+    S = cola.ops.Sparse(T(g["data"]), T(g["rows"]), T(g["cols"]), (3, 4))
+    y = S @ T(g["x"])
+    np.testing.assert_allclose(y.cpu().numpy(), g["y"], rtol=1e-6)
+
+
+def test_sparse_duplicates_and_unsorted():
+    """Duplicate COO entries are summed and columns sorted, with values kept aligned."""
+    data = T([1.0, 2.0, 3.0, 4.0, 5.0], torch.float32)
+    rows = T([1, 0, 1, 0, 1])
+    cols = T([2, 1, 0, 1, 2])
+    S = cola.ops.Sparse(data, rows, cols, (2, 3))
+    D = torch.zeros(2, 3)
+    for d, r, c in zip([1.0, 2, 3, 4, 5], [1, 0, 1, 0, 1], [2, 1, 0, 1, 2]):
+        D[r, c] += d
+    X = torch.randn(3, 2)
+    assert rel(S @ X.to(DEV), D @ X) < 1e-6
+
+
+def test_composites_golden(golden):
+    g = golden("ops_kron")
+    K = cola.ops.Kronecker(cola.ops.Dense(T(g["A1"])), cola.ops.Dense(T(g["A2"])))
+    assert rel(K @ T(g["X"]), g["Y"]) < 1e-12
+    g = golden("ops_blockdiag")
+    BD = cola.ops.BlockDiag(cola.ops.Dense(T(g["B1"])), cola.ops.Dense(T(g["B2"])), multiplicities=[2, 3])
+    assert rel(BD @ T(g["X"]), g["Y"]) < 1e-12
+    g = golden("ops_sum_product")
+    D = cola.ops.Dense(T(g["D"]))
+    S = D + cola.ops.Diagonal(T(g["d"])) + 0.5 * cola.ops.I_like(D)
+    assert rel(S @ T(g["X"]), g["Ysum"]) < 1e-12
+    P = D @ cola.ops.Dense(T(g["D"].T.copy()))
+    assert rel(P @ T(g["X"]), g["Yprod"]) < 1e-12
+
+
+def test_kron_three_factors_and_strided():
+    rng = np.random.default_rng(3)
+    Ms = [rng.standard_normal((s, s)) for s in (4, 3, 5)]
+    K = cola.ops.Kronecker(*[cola.ops.Dense(T(M)) for M in Ms])
+    X = rng.standard_normal((60, 7))
+    ref = np.kron(np.kron(Ms[0], Ms[1]), Ms[2]) @ X
+    assert rel(K @ T(X), ref) < 1e-12
+    # non-contiguous X (leading dimension > k) goes through the executor's copy path
+    Xw = T(rng.standard_normal((60, 9)))[:, :7]
+    assert rel(K @ Xw, np.kron(np.kron(Ms[0], Ms[1]), Ms[2]) @ Xw.cpu().numpy()) < 1e-12
+    # nested: Kronecker of a Sum and a Diagonal
+    A = cola.ops.Dense(T(Ms[0])) + 2.0 * cola.ops.I_like(cola.ops.Dense(T(Ms[0])))
+    d = rng.standard_normal(3)
+    K2 = cola.ops.Kronecker(A, cola.ops.Diagonal(T(d)))
+    X2 = rng.standard_normal((12, 4))
+    assert rel(K2 @ T(X2), np.kron(Ms[0] + 2 * np.eye(4), np.diag(d)) @ X2) < 1e-12
+
+
+# ---------------------------------------------------------------------------------------------
+# CG
+
+@pytest.mark.parametrize("fused", [True, False])
+def test_cg_dense_f64_golden(golden, fused):
+    g = golden("cg_dense_f64")
+    op = cola.PSD(cola.ops.Dense(T(g["A"])))
+    x, info = cola.linalg.inverse.cg(op, T(g["b"]), tol=float(g["tol"]), max_iters=int(g["max_iters"]),
+                                     allow_fused=fused)
+    assert info["fused"] == fused
+    assert rel(x, g["x"]) < 1e-9
+    assert abs(info["iterations"] - int(g["iterations"])) <= 0.03 * int(g["iterations"]) + 2
+    np.testing.assert_allclose(info["errors"][:10], g["errors"][:10], rtol=1e-10)
+
+
+@pytest.mark.parametrize("fused", [True, False])
+def test_cg_dense_f32_golden(golden, fused):
+    g = golden("cg_dense_f32")
+    A = cola.PSD(cola.ops.Dense(T(g["A"])))
+    Ainv = cola.inv(A, CG(tol=float(g["tol"]), max_iters=int(g["max_iters"])))
+    x = Ainv @ T(g["b"]) if fused else cola.linalg.inverse.cg(A, T(g["b"]), tol=float(g["tol"]),
+                                                              max_iters=int(g["max_iters"]), allow_fused=False)[0]
+    # float32: iteration count within 5 % of the reference's, solution within 2e-3 of the reference's
+    if fused:
+        assert abs(Ainv.info["iterations"] - int(g["iterations"])) <= 0.05 * int(g["iterations"]) + 1
+    assert rel(x, g["x"]) < 2e-3
+    xs = np.linalg.solve(g["A"].astype(np.float64), g["b"].astype(np.float64))
+    assert rel(x, xs) < 1.5 * rel(g["x"], xs) + 1e-4
+
+
+@pytest.mark.parametrize("fused", [True, False])
+def test_cg_multi_rhs_jacobi_x0(golden, fused):
+    g = golden("cg_multi_jacobi_x0")
+    P = cola.ops.Diagonal(T(g["dinv"]))
+    x, info = cola.linalg.inverse.cg(cola.PSD(cola.ops.Dense(T(g["A"]))), T(g["B"]), x0=T(g["X0"]), P=P,
+                                     tol=float(g["tol"]), max_iters=int(g["max_iters"]), allow_fused=fused)
+    assert info["fused"] == fused
+    assert abs(info["iterations"] - int(g["iterations"])) <= 1
+    assert rel(x, g["x"]) < 1e-9
+
+
+@pytest.mark.parametrize("tag", ["f32", "f64"])
+@pytest.mark.parametrize("fused", [True, False])
+def test_cg_sparse_golden(golden, tag, fused):
+    g = golden(f"cg_sparse_{tag}")
+    n = g["B"].shape[0]
+    dt = torch.float32 if tag == "f32" else torch.float64
+    op = cola.PSD(csr(g["rows"], g["cols"], g["vals"], n, dt))
+    x, info = cola.linalg.inverse.cg(op, T(g["B"], dt), tol=float(g["tol"]), max_iters=int(g["max_iters"]),
+                                     allow_fused=fused)
+    assert info["fused"] == fused
+    if tag == "f64":
+        assert abs(info["iterations"] - int(g["iterations"])) <= 1
+        assert rel(x, g["x"]) < 1e-9
+    else:
+        assert abs(info["iterations"] - int(g["iterations"])) <= 2
+        assert rel(x, g["x"]) < 1e-4
+
+
+def test_cg_repeated_eig(golden):
+    g = golden("cg_repeated_eig")
+    x, info = cola.linalg.inverse.cg(cola.PSD(cola.ops.Dense(T(g["A"]))), T(g["rhs"]), tol=1e-11, max_iters=100)
+    assert info["iterations"] - 1 < 7
+    assert rel(x, g["x"]) < 1e-4
+
+
+def test_cg_general_preconditioner_and_shift():
+    """Generic path: Sum(Sparse, c I) operator with a Product preconditioner, against the oracle."""
+    from cola_gb300.workloads import grid_pattern_2d, diffusion_values_2d
+    m = 12
+    ip, ix, ok = grid_pattern_2d(m, DEV)
+    a = torch.exp(torch.randn(1, m, m, device=DEV, dtype=torch.float64))
+    v = diffusion_values_2d(a, ok)[0].double()
+    n = m * m
+    S = cola.ops.Sparse.from_csr(ip, ix, v, (n, n))
+    Aop = cola.PSD(S + 0.3 * cola.ops.I_like(S))
+    dg = torch.zeros(n, dtype=torch.float64, device=DEV)
+    rows = torch.repeat_interleave(torch.arange(n, device=DEV), (ip[1:] - ip[:-1]).long())
+    dg.index_add_(0, rows, torch.where(rows == ix.long(), v, torch.zeros_like(v)))
+    dinv = 1.0 / (dg + 0.3)
+    P = cola.ops.Diagonal(dinv.sqrt()) @ cola.ops.Diagonal(dinv.sqrt())
+    B = torch.randn(n, 2, device=DEV, dtype=torch.float64)
+    x, info = cola.linalg.inverse.cg(Aop, B, P=P, tol=1e-10, max_iters=400)
+    assert not info["fused"]
+    Ad = torch.zeros(n, n, dtype=torch.float64, device=DEV)
+    Ad[rows, ix.long()] = v
+    Ad += 0.3 * torch.eye(n, device=DEV, dtype=torch.float64)
+    xo, ko, info_o = oracle.cg_solve(oracle.dense_op(Ad.cpu().numpy()), B.cpu().numpy(),
+                                     precond=lambda r: dinv.cpu().numpy()[:, None] * r, tol=1e-10, max_iters=400)
+    assert rel(x, xo) < 1e-8
+    assert abs(info["iterations"] - info_o["iterations"]) <= 1
+    # the fused kernel on the same shifted operator with Jacobi agrees
+    x2, info2 = cola.linalg.inverse.cg(Aop, B, P=cola.ops.Diagonal(dinv), tol=1e-10, max_iters=400)
+    assert info2["fused"] and rel(x2, xo) < 1e-8
+
+
+def test_cg_edge_cases():
+    A = cola.PSD(cola.ops.Dense(torch.tensor([[2.0]], device=DEV)))
+    x, info = cola.linalg.inverse.cg(A, torch.tensor([4.0], device=DEV), tol=1e-8)
+    assert abs(x.item() - 2.0) < 1e-6
+    # max_iters = 0 returns x0 scaled back, zero steps
+    B = torch.ones(3, device=DEV)
+    A3 = cola.PSD(cola.ops.Diagonal(torch.tensor([1.0, 2.0, 4.0], device=DEV)))
+    x, info = cola.linalg.inverse.cg(A3, B, tol=1e-8, max_iters=0)
+    assert info["iterations"] == 1 and torch.all(x == 0)
+    # a zero right-hand side stays zero (safe division)
+    x, info = cola.linalg.inverse.cg(A3, torch.zeros(3, device=DEV), tol=1e-8, max_iters=10)
+    assert torch.all(x == 0)
+    with pytest.raises(AssertionError):
+        cola.inv(cola.ops.Dense(torch.eye(3, device=DEV)), CG())
+
+
+# ---------------------------------------------------------------------------------------------
+# Lanczos, eig, SLQ
+
+def test_lanczos_batched_golden(golden):
+    g = golden("lanczos_batched")
+    Q, Tm, info = cola.linalg.lanczos(cola.ops.Dense(T(g["A"])), T(g["V0"]), max_iters=int(g["max_iters"]),
+                                      tol=float(g["tol"]))
+    assert info["iterations"] == int(g["iterations"])
+    assert rel(Tm.beta[:, :, 0], g["beta"]) < 1e-10
+    assert rel(Tm.alpha[:, :, 0], g["alpha"]) < 1e-10
+    assert rel(Q.A, g["Q"]) < 1e-9
+
+
+@pytest.mark.parametrize("case", ["early", "three", "two"])
+def test_lanczos_known_answers(golden, case):
+    g = golden(f"lanczos_case_{case}")
+    Q, Tm, info = cola.linalg.lanczos(cola.ops.Dense(T(g["A"], torch.float32)), T(g["rhs"], torch.float32),
+                                      max_iters=3, tol=1e-7)
+    assert info["iterations"] - 1 == int(g["iterations"]) - 1
+    np.testing.assert_allclose(Tm.beta[:, :, 0].cpu().numpy(), g["beta"], rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(Tm.alpha[:, :, 0].cpu().numpy(), g["alpha"], rtol=1e-5, atol=1e-6)
+
+
+def test_eig_lanczos_golden(golden):
+    g = golden("eig_lanczos")
+    op = cola.SelfAdjoint(cola.ops.Dense(T(g["A"])))
+    vals, vecs = cola.eig(op, 5, "LM", Lanczos(max_iters=40, tol=1e-10))
+    # eigenvalues within 1e-5 relative of the reference's (here far tighter: FP64 throughout)
+    assert rel(vals, g["evals"]) < 1e-9
+    V = vecs.cpu().numpy()
+    s = np.sign(np.sum(V * g["evecs"], axis=0))
+    assert rel(V * s, g["evecs"]) < 1e-7
+
+
+def test_lanczos_unary_golden(golden):
+    g = golden("lanczos_unary_log")
+    F = cola.linalg.LanczosUnary(cola.PSD(cola.ops.Dense(T(g["A"]))), torch.log, max_iters=int(g["max_iters"]),
+                                 tol=float(g["tol"]))
+    Y = F @ T(g["Z"])
+    assert rel(Y, g["Y"]) < 1e-8
+
+
+def test_logdet_slq_dense_golden(golden):
+    g = golden("logdet_slq_dense")
+    op = cola.PSD(cola.ops.Dense(T(g["A"])))
+    ld = cola.logdet(op, Lanczos(max_iters=int(g["max_iters"]), tol=float(g["tol"])),
+                     Hutch(max_iters=int(g["hutch_iters"]), key=PRNGKey(42)))
+    # identical probes: agreement far inside the SLQ standard error
+    assert abs(float(ld) - float(g["logdet"])) < 1e-7
+
+
+def test_logdet_kron_slq_golden(golden):
+    g = golden("logdet_kron_slq")
+    K = cola.ops.Kronecker(*[cola.ops.Dense(T(g[k])) for k in ("K1", "K2", "K3")])
+    op = cola.PSD(K + 0.01 * cola.ops.I_like(K))
+    ld = cola.logdet(op, Lanczos(max_iters=40, tol=1e-10), Hutch(max_iters=3, rand="rademacher", key=PRNGKey(7)))
+    assert abs(float(ld) - float(g["logdet"])) < 1e-6
+
+
+def test_slq_tbd_golden(golden):
+    g = golden("slq_tbd")
+    est = cola.linalg.stochastic_lanczos_quad(cola.ops.Dense(T(g["A"])), torch.log, max_iters=30, tol=1e-7,
+                                              probes=T(g["probes"]))
+    assert abs(float(est) - float(g["estimate"])) < 1e-8
+
+
+@pytest.mark.parametrize("m", [1, 2, 3, 31, 32, 33, 100, 257])
+def test_tridiag_eigh(m):
+    rng = np.random.default_rng(m)
+    bsz = 4
+    a = rng.standard_normal((bsz, m))
+    b = rng.standard_normal((bsz, max(m - 1, 0)))
+    ev, P, status = cola.linalg.tridiag_eigh(T(a), T(b), want_vectors=True)
+    ev2, first, _ = cola.linalg.tridiag_eigh(T(a), T(b), want_vectors=False)
+    assert int(status.sum()) == 0
+    for i in range(bsz):
+        Tm = np.diag(a[i]) + (np.diag(b[i], -1) + np.diag(b[i], 1) if m > 1 else 0)
+        w, V = np.linalg.eigh(Tm)
+        np.testing.assert_allclose(ev[i].cpu().numpy(), w, rtol=1e-10, atol=1e-12)
+        np.testing.assert_allclose(ev2[i].cpu().numpy(), w, rtol=1e-10, atol=1e-12)
+        Pm = P[i].cpu().numpy()
+        np.testing.assert_allclose(Tm @ Pm, Pm * w[None, :], atol=1e-9)
+        np.testing.assert_allclose(np.abs(first[i].cpu().numpy()), np.abs(V[0]), atol=1e-9)
+
+
+# ---------------------------------------------------------------------------------------------
+# batched systems on a shared pattern, FP64 iterative refinement
+
+@pytest.mark.parametrize("precond", ["none", "jacobi"])
+def test_batched_ir_small_family(precond):
+    from cola_gb300.workloads import diffusion_family_2d
+    fam, B, _, _ = diffusion_family_2d(range(7), m=24, device=DEV)
+    B[3].zero_()  # a zero right-hand side converges at once with x = 0
+    X, info = cola.linalg.solve_batched(fam, B, precond=precond, tol=1e-8, inner_tol=1e-4)
+    assert torch.all(info["status"] == 1), info["status"]
+    assert float(info["relres"].max()) <= 1e-8
+    R = B - fam.matvec(X)
+    rr = R.norm(dim=1) / B.norm(dim=1).clamp_min(1e-300)
+    rr[3] = 0
+    assert float(rr.max()) <= 1.01e-8
+    assert torch.all(X[3] == 0)
+    n = fam.n
+    for s in (0, 6):
+        A = torch.sparse_csr_tensor(fam.indptr.long(), fam.indices.long(), fam.values[s].double(), (n, n)).to_dense()
+        xs = torch.linalg.solve(A, B[s])
+        assert rel(X[s], xs) < 1e-6
+
+
+def test_batched_ir_matches_oracle_iteration_structure():
+    """The device IR loop and the oracle's IR restatement need comparable inner iterations."""
+    from cola_gb300.workloads import diffusion_family_2d
+    fam, B, _, _ = diffusion_family_2d([11], m=20, device=DEV)
+    X, info = cola.linalg.solve_batched(fam, B, precond="none", tol=1e-8, inner_tol=1e-4)
+    n = fam.n
+    A = torch.sparse_csr_tensor(fam.indptr.long(), fam.indices.long(), fam.values[0].double(), (n, n)).to_dense()
+    A64 = A.cpu().numpy()
+    A32 = A64.astype(np.float32)
+    x, total, sweeps, rr = oracle.cg.ir_solve(lambda v: A64 @ v, lambda v: A32 @ v, B[0].cpu().numpy(), tol=1e-8,
+                                              inner_tol=1e-4)
+    assert rr <= 1e-8
+    assert abs(int(info["iterations"][0]) - total) <= 0.15 * total + 5
+    assert rel(X[0], x) < 1e-6

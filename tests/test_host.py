@@ -1,0 +1,195 @@
+"""Host-side logic that needs no GPU: the C ABI library loads and exports every declared symbol,
+operator lowering, argument validation and error mapping, dispatch rules, pattern helpers."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+import torch
+
+import cola_gb300 as cola
+from cola_gb300 import _capi
+from cola_gb300.linalg import CG, Lanczos
+from cola_gb300.linalg.batched import lower_pattern, transpose_pattern
+from cola_gb300.lowering import Lowered
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def declared_symbols():
+    text = (ROOT / "include" / "colagb.h").read_text()
+    return sorted(set(re.findall(r"\b(colagb_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _capi.load()
+    names = declared_symbols()
+    assert len(names) >= 14
+    for name in names:
+        assert hasattr(lib, name), name
+        assert name in _capi.SIGNATURES, f"{name} has no ctypes signature"
+
+
+def test_version():
+    lib = _capi.load()
+    v, a = C.c_int32(), C.c_int32()
+    assert lib.colagb_version(C.byref(v), C.byref(a)) == 0
+    assert a.value == 1003
+
+
+STRUCTS = {
+    "colagb_op_node": _capi.OpNode, "colagb_cg_params": _capi.CgParams, "colagb_cg_result": _capi.CgResult,
+    "colagb_batched_csr": _capi.BatchedCsr, "colagb_ir_params": _capi.IrParams,
+    "colagb_ir_result": _capi.IrResult, "colagb_lanczos_params": _capi.LanczosParams,
+}
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """Every ctypes struct has the size and field offsets the C compiler gives the header's struct."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{ROOT / "include" / "colagb.h"}"',
+             "int main(void) {"]
+    for cname, py in STRUCTS.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for cname, py in STRUCTS.items():
+        assert got[(cname, "size")] == C.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
+
+
+def test_lowering_structure():
+    A = torch.randn(6, 6)
+    D = cola.ops.Dense(A)
+    op = cola.kron(D, cola.ops.Diagonal(torch.ones(2))) + 0.5 * cola.ops.I_like(cola.kron(D, torch.eye(2)))
+    low = Lowered(op)
+    kinds = [n.kind for n in low.nodes]
+    assert kinds[-1] == _capi.OP_SUM
+    assert _capi.OP_KRON in kinds and _capi.OP_SCALAR in kinds
+    rows, cols, cdt = C.c_int64(), C.c_int64(), C.c_int32()
+    assert _capi.load().colagb_op_info(low.handle, C.byref(rows), C.byref(cols), C.byref(cdt)) == 0
+    assert (rows.value, cols.value, cdt.value) == (12, 12, _capi.F32)
+    assert Lowered(cola.ops.Dense(A.double())).compute_dtype == torch.float64
+
+
+def test_blockdiag_and_product_lowering_and_workspace():
+    D1, D2 = cola.ops.Dense(torch.randn(3, 3)), cola.ops.Dense(torch.randn(2, 2))
+    BD = cola.ops.BlockDiag(D1, D2, multiplicities=[2, 3])
+    P = cola.ops.Product(cola.ops.Dense(torch.randn(12, 12)), BD)
+    low = Lowered(P)
+    nb = C.c_size_t()
+    assert _capi.load().colagb_matmat_workspace_bytes(low.handle, 4, C.byref(nb)) == 0
+    assert nb.value >= 12 * 4 * 4  # the product's intermediate
+
+
+def test_invalid_operator_is_value_error():
+    nd = _capi.OpNode(kind=_capi.OP_DENSE, dtype=_capi.F32, rows=4, cols=4, data=None, ld=4)
+    h = C.c_void_p()
+    st = _capi.load().colagb_op_create(C.byref(nd), 1, 0, C.byref(h))
+    assert st == _capi.ERR_INVALID
+    with pytest.raises(ValueError):
+        _capi.check(st, "op")
+    # shape mismatch in a Sum
+    with pytest.raises(ValueError):
+        cola.ops.Sum(cola.ops.Dense(torch.randn(3, 3)), cola.ops.Dense(torch.randn(4, 4)))
+    with pytest.raises(ValueError):
+        cola.ops.Product(cola.ops.Dense(torch.randn(3, 4)), cola.ops.Dense(torch.randn(3, 3)))
+
+
+def test_unknown_kind_and_cycle_rejected():
+    lib = _capi.load()
+    kids = (C.c_int32 * 1)(0)
+    nd = _capi.OpNode(kind=_capi.OP_SUM, rows=2, cols=2, children=C.cast(kids, C.POINTER(C.c_int32)), num_children=1)
+    h = C.c_void_p()
+    assert lib.colagb_op_create(C.byref(nd), 1, 0, C.byref(h)) == _capi.ERR_INVALID
+    assert b"cycle" in lib.colagb_last_error()
+    nd2 = _capi.OpNode(kind=77, rows=2, cols=2)
+    assert lib.colagb_op_create(C.byref(nd2), 1, 0, C.byref(h)) == _capi.ERR_INVALID
+
+
+def test_compute_requires_cuda_tensors():
+    op = cola.PSD(cola.ops.Dense(torch.eye(3)))
+    with pytest.raises(ValueError, match="GPU"):
+        op @ torch.ones(3)
+    with pytest.raises(ValueError, match="GPU"):
+        cola.linalg.inverse.cg(op, torch.ones(3))
+
+
+def test_dispatch_rules():
+    D = cola.ops.Dense(torch.eye(3))
+    with pytest.raises(AssertionError):
+        cola.inv(D, CG())
+    Ainv = cola.inv(cola.PSD(D), CG(tol=1e-3))
+    assert isinstance(Ainv, cola.linalg.IterativeOperatorWInfo)
+    d = cola.ops.Diagonal(torch.tensor([2.0, 4.0]))
+    assert torch.allclose(cola.inv(d, CG()).diag, torch.tensor([0.5, 0.25]))
+    K = cola.ops.Kronecker(cola.PSD(D), cola.PSD(D))
+    Kinv = cola.inv(K, CG())
+    assert isinstance(Kinv, cola.ops.Kronecker) and all(isinstance(M, cola.linalg.IterativeOperatorWInfo) for M in Kinv.Ms)
+    assert isinstance(cola.inv(cola.ops.I_like(D), CG()), cola.ops.Identity)
+    with pytest.raises(AssertionError):
+        cola.eig(D, 2, "LM", Lanczos())
+    assert cola.linalg.get_slice(3, "LM") == slice(-3, None) and cola.linalg.get_slice(2, "SM") == slice(0, 2)
+
+
+def test_annotations_inference():
+    D = cola.PSD(cola.ops.Dense(torch.eye(4)))
+    assert (D + 0.1 * cola.ops.I_like(D)).isa(cola.PSD)
+    assert cola.kron(D, D).isa(cola.PSD)
+    assert not cola.ops.Dense(torch.eye(4)).isa(cola.PSD)
+    assert (2.0 * D).isa(cola.PSD)
+
+
+def test_reference_randn_recipe():
+    from cola_gb300.linalg.prng import PRNGKey, next_key, randn, sha_hash
+    assert PRNGKey(42) == sha_hash(42) and next_key(7) == sha_hash(7)
+    torch.manual_seed(PRNGKey(42))
+    a = torch.randn(13, 4, dtype=torch.float64)
+    assert torch.equal(a, randn(13, 4, dtype=torch.float64, key=PRNGKey(42)))
+
+
+def test_pattern_helpers():
+    from cola_gb300.workloads import grid_pattern_2d
+    ip, ix, _ = grid_pattern_2d(5)
+    gip, gix, src = lower_pattern(ip, ix)
+    n = 25
+    rows = torch.repeat_interleave(torch.arange(n), (gip[1:] - gip[:-1]).long())
+    assert torch.all(gix.long() <= rows)
+    assert gix.numel() == (ix.numel() + n) // 2
+    tip, tix, perm = transpose_pattern(gip, gix)
+    # entry e of G^T at (i, tix[e]) is entry perm[e] of G at (tix[e], i)
+    trow = torch.repeat_interleave(torch.arange(n), (tip[1:] - tip[:-1]).long())
+    assert torch.all(rows[perm.long()] == tix.long()) and torch.all(gix[perm.long()].long() == trow)
+
+
+def test_sparse_csr_build_host():
+    S = cola.ops.Sparse(torch.tensor([1.0, 2.0, 3.0]), torch.tensor([1, 0, 1]), torch.tensor([0, 1, 0]), (2, 2))
+    assert S.indptr.tolist() == [0, 1, 2] and S.indices.tolist() == [1, 0]
+    assert S.values.tolist() == [2.0, 4.0]
+    assert torch.equal(S.to_dense(), torch.tensor([[0.0, 2.0], [4.0, 0.0]]))
+
+
+def test_workload_generators_small():
+    from cola_gb300.workloads import diffusion_family_2d
+    fam, B, coeff, params = diffusion_family_2d([5000, 5001], m=12, device="cpu")
+    assert fam.values.shape == (2, fam.indices.numel()) and B.shape == (2, 144)
+    for (ell, var) in params:
+        assert 0.05 <= ell <= 0.2 and 0.5 <= var <= 2.0
+    n = 144
+    for s in range(2):
+        A = torch.sparse_csr_tensor(fam.indptr.long(), fam.indices.long(), fam.values[s].double(), (n, n)).to_dense()
+        assert torch.allclose(A, A.T)
+        assert torch.linalg.eigvalsh(A)[0] > 0
