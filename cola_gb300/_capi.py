@@ -27,6 +27,7 @@ F32, F64, BF16 = 0, 1, 2
 OP_DENSE, OP_CSR, OP_DIAG, OP_SCALAR, OP_IDENTITY, OP_SUM, OP_PRODUCT, OP_KRON, OP_BLOCKDIAG = range(1, 10)
 
 PREC_NONE, PREC_JACOBI, PREC_FSAI = 0, 1, 2
+IR_RELIABLE, IR_RESTART = 0, 1
 
 SYS_RUNNING, SYS_CONVERGED, SYS_MAX_ITERS, SYS_BREAKDOWN, SYS_NAN, SYS_FALLBACK = range(6)
 SYS_STATUS_NAMES = {0: "running", 1: "converged", 2: "max_iters", 3: "breakdown", 4: "nan", 5: "fallback"}
@@ -59,14 +60,14 @@ class BatchedCsr(C.Structure):
         ("indptr", C.c_void_p), ("indices", C.c_void_p), ("values", C.c_void_p),
         ("g_nnz", C.c_int64), ("g_indptr", C.c_void_p), ("g_indices", C.c_void_p),
         ("gt_indptr", C.c_void_p), ("gt_indices", C.c_void_p), ("gt_perm", C.c_void_p),
-        ("g_values", C.c_void_p),
+        ("g_values", C.c_void_p), ("shared_values", C.c_int32), ("reserved", C.c_int32),
     ]
 
 
 class IrParams(C.Structure):
     _fields_ = [("tol", C.c_double), ("inner_tol", C.c_double), ("max_sweeps", C.c_int32),
                 ("max_inner_iters", C.c_int32), ("preconditioner", C.c_int32), ("fallback", C.c_int32),
-                ("spin_limit", C.c_int64)]
+                ("spin_limit", C.c_int64), ("mode", C.c_int32), ("reserved", C.c_int32)]
 
 
 class IrResult(C.Structure):
@@ -95,11 +96,25 @@ SIGNATURES = {
     "colagb_cg_batched_csr_workspace_bytes": (C.c_int, [_P(BatchedCsr), _P(IrParams), _P(_sz)]),
     "colagb_cg_batched_csr_solve": (C.c_int, [_P(BatchedCsr), _vp, _vp, _P(IrParams), _vp, _vp, _vp, _vp, _sz,
                                               _P(IrResult), _vp]),
+    "colagb_cg_dense_batched_workspace_bytes": (C.c_int, [_i64, _i64, _P(_sz)]),
+    "colagb_cg_dense_batched_solve": (C.c_int, [_i64, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _d, _i32, _vp, _vp, _vp,
+                                                _sz, _vp]),
     "colagb_lanczos_workspace_bytes": (C.c_int, [_vp, _i64, _i32, _P(_sz)]),
     "colagb_lanczos": (C.c_int, [_vp, _vp, _i64, _i64, _P(LanczosParams), _vp, _vp, _vp, _P(_i32), _vp, _sz,
                                  _vp]),
     "colagb_basis_combine": (C.c_int, [_vp, _i64, _i64, _i32, _vp, _i64, _vp, _i32, _vp]),
     "colagb_tridiag_eig_f64": (C.c_int, [_vp, _vp, _i64, _i64, _vp, _vp, _vp, _vp, _vp]),
+    "colagb_grid5_stencil": (C.c_int, [_vp, _vp, _vp, _i64, _i64, _i64, _vp, _vp, _vp]),
+    "colagb_fsai_features": (C.c_int, [_vp, _i64, _i64, _vp, _vp]),
+    "colagb_fsai_assemble": (C.c_int, [_vp, _vp, _i64, _i64, _vp, _vp]),
+    "colagb_fsai_compact": (C.c_int, [_vp, _vp, _i64, _i64, _i64, _vp, _vp]),
+    "colagb_conv3x3_forward": (C.c_int, [_vp, _i64, _i32, _i32, _i64, _i64, _vp, _vp, _i32, _vp, _vp]),
+    "colagb_conv3x3_backward_scratch_bytes": (C.c_int, [_i32, _i32, _P(_sz)]),
+    "colagb_conv3x3_backward": (C.c_int, [_vp, _vp, _vp, _i64, _i32, _i32, _i64, _i64, _vp, _vp, _vp, _vp, _sz,
+                                          _vp]),
+    "colagb_fsai_loss_grad": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _i64, _i64, _vp, _vp, _vp, _sz, _vp]),
+    "colagb_adam_step": (C.c_int, [_vp, _vp, _vp, _vp, _i64, C.c_float, C.c_float, C.c_float, C.c_float, _i32,
+                                   _vp]),
 }
 
 _lib = None

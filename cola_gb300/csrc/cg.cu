@@ -784,7 +784,7 @@ extern "C" int colagb_cg_workspace_bytes(const colagb_op* A, const colagb_op* P,
   CgPlan pl;
   COLAGB_TRY(plan_cg(A, P, k, pl));
   pl.fused_blocks = num_sms() * 2;
-  Bump ws(nullptr, 0);
+  Bump ws = Bump::measuring();
   void* opws;
   size_t ob;
   if (A->compute_dtype == COLAGB_F64) {

@@ -1,19 +1,26 @@
 // Batched independent SPD systems sharing one CSR sparsity pattern, solved to a true FP64 relative
-// residual by FP32 preconditioned CG inside FP64 iterative refinement -- one persistent launch.
+// residual by FP32 preconditioned CG with FP64 iterative refinement -- one persistent launch.
 //
-// Per system s (the reference runs one cola.linalg.solve(PSD(Sparse), b, CG(P=...)) per system,
-// cola/linalg/inverse/inv.py:66-69 -> cg.py:94-154; the inner loop below is that PCG step):
-//   x = 0, r64 = b
-//   sweep: rhat = r64 / |r64| (FP32) ; d = PCG_fp32(A, rhat) to |r_inner| <= inner_tol
-//          x += |r64| d (FP64) ; r64 = b - A x (FP64, from the FP32 stored values) ; relres = |r64| / |b|
-//   until relres <= tol.
-// Preconditioners: none, Jacobi (CG(P=Diagonal(1/diag A))), FSAI (P = G^T G, G lower triangular
-// on A's lower pattern).  The FP64 true residual is the judge: a system whose FSAI sweep fails to
-// halve its true residual continues with Jacobi (status COLAGB_SYS_FALLBACK).
+// Per system s the inner loop is the reference's PCG step (cola/linalg/inverse/cg.py:141-170,
+// with P = Diagonal(1/diag A) for Jacobi or P = G^T G for FSAI); the reference solves each system
+// with its own cola.linalg.solve(PSD(Sparse), b, CG(P=...)) call (inv.py:24-69).
 //
-// Work distribution: every phase splits the currently active systems into q row chunks each
-// (q*nact ~ 8 chunks per CTA) and deals chunks round-robin over the co-resident CTAs, so CTAs
-// stay busy as systems converge.  Per-system sums are CTA-reduced and added to FP64 accumulators.
+// Precision scheme (per system, b normalised to |b| = 1):
+//   FP32 vectors r, p, Ap, d, z; FP64 solution x.
+//   Every CG step: d += alpha p, r -= alpha Ap (FP32).
+//   Replacement, when |r| has dropped by inner_tol since the last one, or |r| <= tol:
+//       x += d, d = 0 (FP64);  r = b - A x  (FP64 arithmetic on the FP32 stored values);
+//       relres = |b - A x| (FP64) -- the only convergence test (relres <= tol).
+//   COLAGB_IR_RELIABLE: the CG recurrence continues with the replaced residual (reliable updates,
+//   no Krylov restart).  COLAGB_IR_RESTART: every replacement also restarts CG (p = z), the classic
+//   refinement sweep.
+// The FP64 true residual also judges the learned preconditioner: a system whose FSAI segment fails
+// to halve its true residual continues with Jacobi (status COLAGB_SYS_FALLBACK).
+//
+// Work distribution: every phase splits the active systems into q row chunks each (~8 chunks per
+// CTA) and gives each CTA a contiguous range of chunks, so a CTA mostly stays inside one system and
+// reduces its per-system sums once; rows are processed 4 per thread per step with all loads issued
+// before any store (memory-level parallelism for the HBM-bound streams).
 #include <string>
 
 #include "common.cuh"
@@ -21,12 +28,16 @@
 namespace colagb {
 
 constexpr int kMaxBatch = 1024;  // systems per launch (host splits larger batches)
+constexpr int kThreads = 256;
+constexpr int kUnroll = 4;
+constexpr int kRowUnroll = 6;    // CSR entries per row handled without a loop
 
 struct BatchedArgs {
   int64_t n, nnz, S;
-  const int32_t* indptr;
-  const int32_t* indices;
-  const float* vals;
+  int64_t vstride;  // elements between systems' value arrays (0: one shared matrix)
+  const int32_t* __restrict__ indptr;
+  const int32_t* __restrict__ indices;
+  const float* __restrict__ vals;
   int64_t g_nnz;
   const int32_t* g_indptr;
   const int32_t* g_indices;
@@ -35,34 +46,47 @@ struct BatchedArgs {
   const int32_t* gt_perm;
   const float* g_vals;
   const double* B;
-  double* X;
+  double* X;                             // FP64 solution (in units of |b| until the final scaling)
   float *r, *p, *ap, *d, *z, *t, *dinv;  // [S][n]
-  double* r64;                           // [S][n]
   double* acc;                           // [6][S]
   double* bnorm;                         // [S]
-  int* out_status;                       // [S] (may be null)
-  int* out_iters;                        // [S] (may be null)
-  double* out_relres;                    // [S] (may be null)
-  int* summary;                          // [4]: sweeps, max total inner iters, -, -
+  int* out_status;
+  int* out_iters;
+  double* out_relres;
+  int* summary;  // [0] max replacements, [1] max iterations
   double tol, inner_tol;
-  int max_sweeps, max_inner, prec_kind, fallback;
+  int max_sweeps, max_inner, prec_kind, fallback, mode;
   GridBarrier gb;
 };
 
-struct BatchedSmem {
-  int* act;        // active system list
-  double* gamma;   // <r, z>
-  float* alpha;
-  float* beta;
-  double* rn64;    // |r64|
-  double* relres;
-  int* prec;       // per-system preconditioner kind
-  int* status;     // COLAGB_SYS_*
-  int* inner_on;   // inner CG still running
-  int* it_sweep;   // inner iterations this sweep
-  int* it_total;   // inner iterations over all sweeps
-  float* rnin;     // inner |r|
+// per-system state, identical in every CTA: one shared-memory block addressed from a single base
+// pointer (FP64 fields first, then 32-bit fields), S entries per field
+struct SysState {
+  unsigned char* base;
+  int S;
+  __device__ __forceinline__ double* f64(int k) const { return reinterpret_cast<double*>(base) + (size_t)k * S; }
+  __device__ __forceinline__ float* f32(int k) const {
+    return reinterpret_cast<float*>(base + (size_t)3 * 8 * S) + (size_t)k * S;
+  }
+  __device__ __forceinline__ int* i32(int k) const {
+    return reinterpret_cast<int*>(base + (size_t)3 * 8 * S) + (size_t)(4 + k) * S;
+  }
+  __device__ __forceinline__ double& gamma(int s) const { return f64(0)[s]; }
+  __device__ __forceinline__ double& relres(int s) const { return f64(1)[s]; }
+  __device__ __forceinline__ double& relres_prev(int s) const { return f64(2)[s]; }
+  __device__ __forceinline__ float& alpha(int s) const { return f32(0)[s]; }
+  __device__ __forceinline__ float& beta(int s) const { return f32(1)[s]; }
+  __device__ __forceinline__ float& rn(int s) const { return f32(2)[s]; }
+  __device__ __forceinline__ float& rmax(int s) const { return f32(3)[s]; }
+  __device__ __forceinline__ int& status(int s) const { return i32(0)[s]; }
+  __device__ __forceinline__ int& prec(int s) const { return i32(1)[s]; }
+  __device__ __forceinline__ int& it(int s) const { return i32(2)[s]; }
+  __device__ __forceinline__ int& nrep(int s) const { return i32(3)[s]; }
+  __device__ __forceinline__ int& flags(int s) const { return i32(4)[s]; }
+  __device__ __forceinline__ int* act() const { return i32(5); }
+  __device__ __forceinline__ int* act2() const { return i32(6); }
 };
+constexpr int F_ACTIVE = 1, F_REPLACE = 2, F_RESTART = 4;
 
 __device__ __forceinline__ void chunking(int nact, int nb, int64_t n, int& q, int64_t& cs) {
   const int target = 8 * nb;
@@ -70,57 +94,317 @@ __device__ __forceinline__ void chunking(int nact, int nb, int64_t n, int& q, in
   if (q < 1) q = 1;
   if ((int64_t)q > n) q = (int)n;
   cs = (n + q - 1) / q;
+  cs = (cs + 3) / 4 * 4;  // row chunks start on 16-byte boundaries (vector phases)
+  q = (int)((n + cs - 1) / cs);
 }
 
-// f(s, i) -> float contribution, summed per system into acc_s[s] (FP64 atomics, one per chunk).
-// If acc_s is null, f is evaluated for its side effects only.
-template <class F>
-__device__ __forceinline__ void sweep_chunks(const int* act, int nact, int64_t n, double* acc_s, F f,
-                                             float* red) {
+// the per-system FP64 accumulators: acc[k][s] = base[k * S + s]
+struct AccSet {
+  double* base;
+  int S;
+  __device__ __forceinline__ double* operator[](int k) const { return base + (size_t)k * S; }
+  __device__ __forceinline__ AccSet operator+(int k) const { return AccSet{base + (size_t)k * S, S}; }
+};
+
+template <class A, int NA>
+__device__ __forceinline__ void flush(int s, A* v, const AccSet& acc, A* red) {
+#pragma unroll
+  for (int k = 0; k < NA; ++k) {
+    const A x = block_sum(v[k], red);
+    if (threadIdx.x == 0) atomicAdd(acc[k] + s, (double)x);
+    v[k] = A(0);
+  }
+}
+
+// Runs functor f over every (system, row) of the active list.  f.load(s, i) issues the loads of one
+// row, f.finish(s, i, l, v) computes, stores and adds NA contributions to v.  Per-system sums go to
+// acc[k][s] (FP64 atomics, once per CTA and system).
+template <class A, int NA, class F>
+__device__ __forceinline__ void sweep(const int* act, int nact, int64_t n, const F& f, const AccSet& acc, A* red) {
+  if (nact <= 0) return;
   int q;
   int64_t cs;
   chunking(nact, gridDim.x, n, q, cs);
-  const int total = nact * q;
-  for (int ch = blockIdx.x; ch < total; ch += gridDim.x) {
+  const int64_t total = (int64_t)nact * q;
+  const int64_t c0 = total * blockIdx.x / gridDim.x, c1 = total * (blockIdx.x + 1) / gridDim.x;
+  int cur = -1;
+  A v[NA > 0 ? NA : 1];
+#pragma unroll
+  for (int k = 0; k < (NA > 0 ? NA : 1); ++k) v[k] = A(0);
+  for (int64_t ch = c0; ch < c1; ++ch) {
     const int s = act[ch / q];
-    const int64_t i0 = (int64_t)(ch % q) * cs;
+    if (NA > 0 && s != cur) {
+      if (cur >= 0) flush<A, NA>(cur, v, acc, red);
+      cur = s;
+    }
+    const int64_t i0 = (ch % q) * cs;
     const int64_t i1 = (i0 + cs < n) ? i0 + cs : n;
-    float v = 0.f;
-    for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) v += f(s, i);
-    if (acc_s) {
-      v = block_sum(v, red);
-      if (threadIdx.x == 0) atomicAdd(acc_s + s, (double)v);
+    constexpr int U = F::kU;
+    if constexpr (F::kVec == 4) {
+      // 4 consecutive rows per thread with 128-bit loads (n % 4 == 0 is checked by the host)
+      for (int64_t base = i0 + 4 * (int64_t)threadIdx.x; base < i1; base += 4 * (int64_t)kThreads) {
+        const typename F::L l = f.load(s, base);
+        f.finish(s, base, l, v);
+      }
+    } else {
+      for (int64_t base = i0 + threadIdx.x; base < i1; base += U * kThreads) {
+        typename F::L l[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int64_t i = base + (int64_t)u * kThreads;
+          if (i < i1) l[u] = f.load(s, i);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int64_t i = base + (int64_t)u * kThreads;
+          if (i < i1) f.finish(s, i, l[u], v);
+        }
+      }
     }
   }
+  if (NA > 0 && cur >= 0) flush<A, NA>(cur, v, acc, red);
 }
 
-template <class F>
-__device__ __forceinline__ void sweep_chunks64(const int* act, int nact, int64_t n, double* acc_s, F f,
-                                               double* red) {
-  int q;
-  int64_t cs;
-  chunking(nact, gridDim.x, n, q, cs);
-  const int total = nact * q;
-  for (int ch = blockIdx.x; ch < total; ch += gridDim.x) {
-    const int s = act[ch / q];
-    const int64_t i0 = (int64_t)(ch % q) * cs;
-    const int64_t i1 = (i0 + cs < n) ? i0 + cs : n;
-    double v = 0.0;
-    for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) v += f(s, i);
-    v = block_sum(v, red);
-    if (threadIdx.x == 0) atomicAdd(acc_s + s, v);
+// CSR row dot with up to kRowUnroll entries unrolled (predicated), the rest in a loop.
+template <class T, class V>
+__device__ __forceinline__ T csr_dot(const int32_t* __restrict__ indptr, const int32_t* __restrict__ indices,
+                                     const float* __restrict__ vals, const V* __restrict__ x, int64_t i) {
+  const int32_t b = __ldg(indptr + i), e = __ldg(indptr + i + 1);
+  T acc = T(0);
+#pragma unroll
+  for (int k = 0; k < kRowUnroll; ++k) {
+    const int32_t j = b + k;
+    if (j < e) acc += (T)vals[j] * (T)x[__ldg(indices + j)];
   }
+  for (int32_t j = b + kRowUnroll; j < e; ++j) acc += (T)vals[j] * (T)x[__ldg(indices + j)];
+  return acc;
 }
 
-// Rebuild the active list from a predicate (identical in every CTA).
+__device__ __forceinline__ float apply_m_row(const BatchedArgs& a, int pk, int64_t s, int64_t i, float rv) {
+  if (pk == COLAGB_PREC_JACOBI) return a.dinv[s * a.n + i] * rv;
+  return rv;
+}
+
+// ---- phase functors -----------------------------------------------------------------------------
+struct FMatvec {
+  static constexpr int kVec = 1;
+  static constexpr int kU = 2;  // Ap = A p ; <p, Ap>
+  const BatchedArgs* a;
+  struct L { float pv, ap; };
+  __device__ __forceinline__ L load(int s, int64_t i) const {
+    const int64_t so = (int64_t)s * a->n;
+    L l;
+    l.ap = csr_dot<float, float>(a->indptr, a->indices, a->vals + (int64_t)s * a->vstride, a->p + so, i);
+    l.pv = a->p[so + i];
+    return l;
+  }
+  __device__ __forceinline__ void finish(int s, int64_t i, const L& l, float* v) const {
+    a->ap[(int64_t)s * a->n + i] = l.ap;
+    v[0] += l.pv * l.ap;
+  }
+};
+
+struct FUpdate {  // d += alpha p ; r -= alpha Ap ; |r|^2 ; <r, M r> for Jacobi / none   (4 rows)
+  static constexpr int kVec = 4;
+  static constexpr int kU = 1;
+  const BatchedArgs* a;
+  const SysState* m;
+  struct L { float4 d, p, r, ap, di; };
+  __device__ __forceinline__ L load(int s, int64_t i) const {
+    const int64_t u = (int64_t)s * a->n + i;
+    L l;
+    l.d = *reinterpret_cast<const float4*>(a->d + u);
+    l.p = *reinterpret_cast<const float4*>(a->p + u);
+    l.r = *reinterpret_cast<const float4*>(a->r + u);
+    l.ap = *reinterpret_cast<const float4*>(a->ap + u);
+    l.di = (m->prec(s) == COLAGB_PREC_JACOBI) ? *reinterpret_cast<const float4*>(a->dinv + u)
+                                              : make_float4(1.f, 1.f, 1.f, 1.f);
+    return l;
+  }
+  __device__ __forceinline__ void finish(int s, int64_t i, const L& l, float* v) const {
+    const int64_t u = (int64_t)s * a->n + i;
+    const float al = m->alpha(s);
+    float4 d, r;
+    d.x = l.d.x + al * l.p.x; d.y = l.d.y + al * l.p.y; d.z = l.d.z + al * l.p.z; d.w = l.d.w + al * l.p.w;
+    r.x = l.r.x - al * l.ap.x; r.y = l.r.y - al * l.ap.y; r.z = l.r.z - al * l.ap.z; r.w = l.r.w - al * l.ap.w;
+    *reinterpret_cast<float4*>(a->d + u) = d;
+    *reinterpret_cast<float4*>(a->r + u) = r;
+    v[0] += r.x * r.x + r.y * r.y + r.z * r.z + r.w * r.w;
+    v[1] += r.x * (l.di.x * r.x) + r.y * (l.di.y * r.y) + r.z * (l.di.z * r.z) + r.w * (l.di.w * r.w);
+  }
+};
+
+struct FFlushX {  // x += d ; d = 0   (4 rows)
+  static constexpr int kVec = 4;
+  static constexpr int kU = 1;
+  const BatchedArgs* a;
+  struct L { double2 x0, x1; float4 d; };
+  __device__ __forceinline__ L load(int s, int64_t i) const {
+    const int64_t u = (int64_t)s * a->n + i;
+    L l;
+    l.x0 = *reinterpret_cast<const double2*>(a->X + u);
+    l.x1 = *reinterpret_cast<const double2*>(a->X + u + 2);
+    l.d = *reinterpret_cast<const float4*>(a->d + u);
+    return l;
+  }
+  __device__ __forceinline__ void finish(int s, int64_t i, const L& l, double*) const {
+    const int64_t u = (int64_t)s * a->n + i;
+    *reinterpret_cast<double2*>(a->X + u) = make_double2(l.x0.x + (double)l.d.x, l.x0.y + (double)l.d.y);
+    *reinterpret_cast<double2*>(a->X + u + 2) = make_double2(l.x1.x + (double)l.d.z, l.x1.y + (double)l.d.w);
+    *reinterpret_cast<float4*>(a->d + u) = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+};
+
+struct FResidual {
+  static constexpr int kVec = 1;
+  static constexpr int kU = 1;  // r = b/|b| - A x in FP64 ; |r|^2 (FP64) ; <r, M r> for Jacobi / none
+  const BatchedArgs* a;
+  const SysState* m;
+  struct L { double ax, b; float di; };
+  __device__ __forceinline__ L load(int s, int64_t i) const {
+    const int64_t so = (int64_t)s * a->n;
+    L l;
+    l.ax = csr_dot<double, double>(a->indptr, a->indices, a->vals + (int64_t)s * a->vstride, a->X + so, i);
+    l.b = a->B[so + i];
+    l.di = (m->prec(s) == COLAGB_PREC_JACOBI) ? a->dinv[so + i] : 1.f;
+    return l;
+  }
+  __device__ __forceinline__ void finish(int s, int64_t i, const L& l, double* v) const {
+    const double rv = l.b / a->bnorm[s] - l.ax;
+    const float rf = (float)rv;
+    a->r[(int64_t)s * a->n + i] = rf;
+    v[0] += rv * rv;
+    v[1] += (double)(rf * (l.di * rf));
+  }
+};
+
+struct FFsaiT {
+  static constexpr int kVec = 1;
+  static constexpr int kU = 2;  // t = G r (FSAI systems)
+  const BatchedArgs* a;
+  const SysState* m;
+  struct L { float t; };
+  __device__ __forceinline__ L load(int s, int64_t i) const {
+    L l{0.f};
+    if (m->prec(s) != COLAGB_PREC_FSAI) return l;
+    const float* g = a->g_vals + (int64_t)s * a->g_nnz;
+    const float* rs = a->r + (int64_t)s * a->n;
+    for (int32_t e = a->g_indptr[i]; e < a->g_indptr[i + 1]; ++e) l.t += g[e] * rs[a->g_indices[e]];
+    return l;
+  }
+  __device__ __forceinline__ void finish(int s, int64_t i, const L& l, float*) const {
+    if (m->prec(s) == COLAGB_PREC_FSAI) a->t[(int64_t)s * a->n + i] = l.t;
+  }
+};
+
+struct FZ {
+  static constexpr int kVec = 1;
+  static constexpr int kU = 2;  // z = M r (G^T t for FSAI) ; <r, z>
+  const BatchedArgs* a;
+  const SysState* m;
+  struct L { float z, r; };
+  __device__ __forceinline__ L load(int s, int64_t i) const {
+    const int64_t u = (int64_t)s * a->n + i;
+    L l;
+    l.r = a->r[u];
+    const int pk = m->prec(s);
+    if (pk == COLAGB_PREC_FSAI) {
+      const float* g = a->g_vals + (int64_t)s * a->g_nnz;
+      const float* ts = a->t + (int64_t)s * a->n;
+      float v = 0.f;
+      for (int32_t e = a->gt_indptr[i]; e < a->gt_indptr[i + 1]; ++e) v += g[a->gt_perm[e]] * ts[a->gt_indices[e]];
+      l.z = v;
+    } else {
+      l.z = apply_m_row(*a, pk, s, i, l.r);
+    }
+    return l;
+  }
+  __device__ __forceinline__ void finish(int s, int64_t i, const L& l, float* v) const {
+    a->z[(int64_t)s * a->n + i] = l.z;
+    v[0] += l.r * l.z;
+  }
+};
+
+struct FPUpdate {  // p = z + beta p  (z stored, or M r recomputed)   (4 rows)
+  static constexpr int kVec = 4;
+  static constexpr int kU = 1;
+  const BatchedArgs* a;
+  const SysState* m;
+  bool zstored;
+  struct L { float4 z, p; };
+  __device__ __forceinline__ L load(int s, int64_t i) const {
+    const int64_t u = (int64_t)s * a->n + i;
+    L l;
+    if (zstored) {
+      l.z = *reinterpret_cast<const float4*>(a->z + u);
+    } else {
+      l.z = *reinterpret_cast<const float4*>(a->r + u);
+      if (m->prec(s) == COLAGB_PREC_JACOBI) {
+        const float4 di = *reinterpret_cast<const float4*>(a->dinv + u);
+        l.z.x *= di.x; l.z.y *= di.y; l.z.z *= di.z; l.z.w *= di.w;
+      }
+    }
+    l.p = *reinterpret_cast<const float4*>(a->p + u);
+    return l;
+  }
+  __device__ __forceinline__ void finish(int s, int64_t i, const L& l, float*) const {
+    const float b = m->beta(s);
+    *reinterpret_cast<float4*>(a->p + (int64_t)s * a->n + i) =
+        make_float4(l.z.x + b * l.p.x, l.z.y + b * l.p.y, l.z.z + b * l.p.z, l.z.w + b * l.p.w);
+  }
+};
+
+struct FSetup {
+  static constexpr int kVec = 1;
+  static constexpr int kU = 1;  // |b|^2 ; x = 0 ; d = 0 ; Jacobi diagonal
+  const BatchedArgs* a;
+  struct L { double b; float dg; };
+  __device__ __forceinline__ L load(int s, int64_t i) const {
+    const int64_t u = (int64_t)s * a->n + i;
+    L l;
+    l.b = a->B[u];
+    l.dg = 0.f;
+    if (a->dinv) {
+      const float* vals = a->vals + (int64_t)s * a->vstride;
+      for (int32_t j = a->indptr[i]; j < a->indptr[i + 1]; ++j)
+        if (a->indices[j] == i) l.dg += vals[j];
+    }
+    return l;
+  }
+  __device__ __forceinline__ void finish(int s, int64_t i, const L& l, double* v) const {
+    const int64_t u = (int64_t)s * a->n + i;
+    if (a->dinv) a->dinv[u] = l.dg != 0.f ? 1.f / l.dg : 1.f;
+    a->X[u] = 0.0;
+    a->d[u] = 0.f;
+    v[0] += l.b * l.b;
+  }
+};
+
+struct FScaleX {  // X = |b| x   (4 rows)
+  static constexpr int kVec = 4;
+  static constexpr int kU = 1;
+  const BatchedArgs* a;
+  struct L { double2 x0, x1; };
+  __device__ __forceinline__ L load(int s, int64_t i) const {
+    const int64_t u = (int64_t)s * a->n + i;
+    return L{*reinterpret_cast<const double2*>(a->X + u), *reinterpret_cast<const double2*>(a->X + u + 2)};
+  }
+  __device__ __forceinline__ void finish(int s, int64_t i, const L& l, double*) const {
+    const int64_t u = (int64_t)s * a->n + i;
+    const double b = a->bnorm[s];
+    *reinterpret_cast<double2*>(a->X + u) = make_double2(l.x0.x * b, l.x0.y * b);
+    *reinterpret_cast<double2*>(a->X + u + 2) = make_double2(l.x1.x * b, l.x1.y * b);
+  }
+};
+
 template <class P>
-__device__ __forceinline__ int build_active(int S, int* act, P pred) {
+__device__ __forceinline__ int build_list(int S, int* list, P pred) {
   __shared__ int s_n;
   __syncthreads();
   if (threadIdx.x == 0) {
     int c = 0;
     for (int s = 0; s < S; ++s)
-      if (pred(s)) act[c++] = s;
+      if (pred(s)) list[c++] = s;
     s_n = c;
   }
   __syncthreads();
@@ -129,311 +413,222 @@ __device__ __forceinline__ int build_active(int S, int* act, P pred) {
   return r;
 }
 
-__device__ __forceinline__ float csr_row(const BatchedArgs& a, int s, int64_t i, const float* v) {
-  const float* vals = a.vals + (int64_t)s * a.nnz;
-  const float* vs = v + (int64_t)s * a.n;
-  const int32_t b = a.indptr[i], e = a.indptr[i + 1];
-  float acc = 0.f;
-  for (int32_t j = b; j < e; ++j) acc += vals[j] * vs[a.indices[j]];
-  return acc;
-}
-
-__global__ void __launch_bounds__(256) k_batched_ir(BatchedArgs a) {
+__global__ void __launch_bounds__(kThreads, 4) k_batched_ir(const __grid_constant__ BatchedArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int S = (int)a.S;
   const int64_t n = a.n;
-  BatchedSmem m;
-  {
-    unsigned char* q = smem_raw;
-    auto takeb = [&](size_t bytes) { unsigned char* r = q; q += (bytes + 15) / 16 * 16; return r; };
-    m.gamma = reinterpret_cast<double*>(takeb(sizeof(double) * S));
-    m.rn64 = reinterpret_cast<double*>(takeb(sizeof(double) * S));
-    m.relres = reinterpret_cast<double*>(takeb(sizeof(double) * S));
-    m.act = reinterpret_cast<int*>(takeb(sizeof(int) * S));
-    m.alpha = reinterpret_cast<float*>(takeb(sizeof(float) * S));
-    m.beta = reinterpret_cast<float*>(takeb(sizeof(float) * S));
-    m.prec = reinterpret_cast<int*>(takeb(sizeof(int) * S));
-    m.status = reinterpret_cast<int*>(takeb(sizeof(int) * S));
-    m.inner_on = reinterpret_cast<int*>(takeb(sizeof(int) * S));
-    m.it_sweep = reinterpret_cast<int*>(takeb(sizeof(int) * S));
-    m.it_total = reinterpret_cast<int*>(takeb(sizeof(int) * S));
-    m.rnin = reinterpret_cast<float*>(takeb(sizeof(float) * S));
-  }
+  SysState m{smem_raw, S};
   __shared__ float redf[32];
   __shared__ double redd[32];
-  double* acc0 = a.acc;            // |b|^2, later <p, Ap>
-  double* acc1 = a.acc + S;        // <r, z>
-  double* acc2 = a.acc + 2 * S;    // |r|^2 (inner)
-  double* acc3 = a.acc + 3 * S;    // |r64|^2
+  AccSet acc{a.acc, S};
+  const float delta = (float)a.inner_tol;
+  const bool restart_mode = a.mode == COLAGB_IR_RESTART;
+
+  auto zero_acc = [&](int k) {
+    if (blockIdx.x == 0)
+      for (int s = threadIdx.x; s < S; s += blockDim.x) acc[k][s] = 0.0;
+  };
 
   // ---------------- setup ----------------
   for (int s = threadIdx.x; s < S; s += blockDim.x) {
-    m.prec[s] = a.prec_kind;
-    m.status[s] = COLAGB_SYS_RUNNING;
-    m.it_total[s] = 0;
+    m.prec(s) = a.prec_kind;
+    m.status(s) = COLAGB_SYS_RUNNING;
+    m.it(s) = 0;
+    m.nrep(s) = 0;
+    m.flags(s) = F_ACTIVE;
   }
-  int nact = build_active(S, m.act, [&](int) { return true; });
-  // Jacobi diagonal, x = 0, r64 = b, |b|^2
-  sweep_chunks64(m.act, nact, n, acc0, [&](int s, int64_t i) -> double {
-    const int64_t u = (int64_t)s * n + i;
-    if (a.dinv) {
-      const float* vals = a.vals + (int64_t)s * a.nnz;
-      float dg = 0.f;
-      for (int32_t j = a.indptr[i]; j < a.indptr[i + 1]; ++j)
-        if (a.indices[j] == i) dg += vals[j];
-      a.dinv[u] = dg != 0.f ? 1.f / dg : 1.f;
-    }
-    const double bv = a.B[u];
-    a.X[u] = 0.0;
-    a.r64[u] = bv;
-    return bv * bv;
-  }, redd);
+  int nact = build_list(S, m.act(), [&](int) { return true; });
+  sweep<double, 1>(m.act(), nact, n, FSetup{&a}, acc, redd);
   if (!grid_sync(a.gb)) return;
   for (int s = threadIdx.x; s < S; s += blockDim.x) {
-    const double bn = sqrt(__ldcg(acc0 + s));
-    m.rn64[s] = bn;
-    m.relres[s] = bn > 0.0 ? 1.0 : 0.0;
-    if (!(bn > 0.0)) m.status[s] = (bn == 0.0) ? COLAGB_SYS_CONVERGED : COLAGB_SYS_NAN;
-    if (blockIdx.x == 0) a.bnorm[s] = bn;
+    const double bn = sqrt(__ldcg(acc[0] + s));
+    if (blockIdx.x == 0) a.bnorm[s] = bn > 0.0 ? bn : 1.0;
+    m.relres(s) = bn > 0.0 ? 1.0 : 0.0;
+    m.relres_prev(s) = m.relres(s);
+    if (!(bn > 0.0)) {
+      m.status(s) = (bn == 0.0) ? COLAGB_SYS_CONVERGED : COLAGB_SYS_NAN;
+      m.flags(s) = 0;
+    }
   }
   __syncthreads();
-  if (!grid_sync(a.gb)) return;  // every CTA has read acc0
-  if (blockIdx.x == 0)
-    for (int s = threadIdx.x; s < S; s += blockDim.x) { acc0[s] = 0.0; acc1[s] = 0.0; acc2[s] = 0.0; acc3[s] = 0.0; }
+  if (!grid_sync(a.gb)) return;  // acc[0] read everywhere, bnorm visible
+  zero_acc(0);
+  nact = build_list(S, m.act(), [&](int s) { return (m.flags(s) & F_ACTIVE) != 0; });
+  // r = b/|b| (x = 0): the residual phase with x = 0 computes exactly that, in FP64
+  sweep<double, 2>(m.act(), nact, n, FResidual{&a, &m}, acc + 3, redd);
   if (!grid_sync(a.gb)) return;
-
-  int sweep = 0;
-  int max_total_inner = 0;
-  for (; sweep < a.max_sweeps; ++sweep) {
-    // systems needing another sweep
-    for (int s = threadIdx.x; s < S; s += blockDim.x)
-      if (m.status[s] == COLAGB_SYS_RUNNING && m.relres[s] <= a.tol) m.status[s] = COLAGB_SYS_CONVERGED;
-    __syncthreads();
-    nact = build_active(S, m.act, [&](int s) { return m.status[s] == COLAGB_SYS_RUNNING; });
-    if (nact == 0) break;
-    bool any_fsai = false;
-    for (int j = 0; j < nact; ++j) any_fsai |= (m.prec[m.act[j]] == COLAGB_PREC_FSAI);
-
-    // ---- inner init: r = r64/|r64|, d = 0 ----
-    sweep_chunks(m.act, nact, n, nullptr, [&](int s, int64_t i) -> float {
-      const int64_t u = (int64_t)s * n + i;
-      a.r[u] = (float)(a.r64[u] / m.rn64[s]);
-      a.d[u] = 0.f;
-      return 0.f;
-    }, redf);
-    if (!grid_sync(a.gb)) return;
-    if (any_fsai) {
-      sweep_chunks(m.act, nact, n, nullptr, [&](int s, int64_t i) -> float {
-        if (m.prec[s] != COLAGB_PREC_FSAI) return 0.f;
-        const float* g = a.g_vals + (int64_t)s * a.g_nnz;
-        const float* rs = a.r + (int64_t)s * n;
-        float v = 0.f;
-        for (int32_t e = a.g_indptr[i]; e < a.g_indptr[i + 1]; ++e) v += g[e] * rs[a.g_indices[e]];
-        a.t[(int64_t)s * n + i] = v;
-        return 0.f;
-      }, redf);
-      if (!grid_sync(a.gb)) return;
-    }
-    // z = M r ; p = z ; <r, z>, |r|^2
-    auto apply_m = [&](int s, int64_t i) -> float {
-      const int64_t u = (int64_t)s * n + i;
-      const int pk = m.prec[s];
-      if (pk == COLAGB_PREC_JACOBI) return a.dinv[u] * a.r[u];
-      if (pk == COLAGB_PREC_FSAI) {
-        const float* g = a.g_vals + (int64_t)s * a.g_nnz;
-        const float* ts = a.t + (int64_t)s * n;
-        float v = 0.f;
-        for (int32_t e = a.gt_indptr[i]; e < a.gt_indptr[i + 1]; ++e) v += g[a.gt_perm[e]] * ts[a.gt_indices[e]];
-        return v;
-      }
-      return a.r[u];
-    };
-    sweep_chunks(m.act, nact, n, acc1, [&](int s, int64_t i) -> float {
-      const int64_t u = (int64_t)s * n + i;
-      const float zv = apply_m(s, i);
-      if (a.z) a.z[u] = zv;
-      a.p[u] = zv;
-      return a.r[u] * zv;
-    }, redf);
-    sweep_chunks(m.act, nact, n, acc2, [&](int s, int64_t i) -> float {
-      const float rv = a.r[(int64_t)s * n + i];
-      return rv * rv;
-    }, redf);
-    if (!grid_sync(a.gb)) return;
-    for (int s = threadIdx.x; s < S; s += blockDim.x) {
-      m.inner_on[s] = 0;
-      m.it_sweep[s] = 0;
-    }
-    __syncthreads();
-    for (int j = threadIdx.x; j < nact; j += blockDim.x) {
-      const int s = m.act[j];
-      m.gamma[s] = __ldcg(acc1 + s);
-      m.rnin[s] = (float)sqrt(__ldcg(acc2 + s));
-      m.inner_on[s] = m.rnin[s] > (float)a.inner_tol && a.max_inner > 0;
-    }
-    __syncthreads();
-    if (!grid_sync(a.gb)) return;
-    if (blockIdx.x == 0)
-      for (int j = threadIdx.x; j < nact; j += blockDim.x) { acc1[m.act[j]] = 0.0; acc2[m.act[j]] = 0.0; }
-    int nin = build_active(S, m.act, [&](int s) { return m.inner_on[s] != 0; });
-    if (!grid_sync(a.gb)) return;
-
-    // ---- inner PCG ----
-    while (nin > 0) {
-      // A: Ap = A p ; <p, Ap>
-      sweep_chunks(m.act, nin, n, acc0, [&](int s, int64_t i) -> float {
-        const int64_t u = (int64_t)s * n + i;
-        const float v = csr_row(a, s, i, a.p);
-        a.ap[u] = v;
-        return a.p[u] * v;
-      }, redf);
-      if (!grid_sync(a.gb)) return;
-      for (int j = threadIdx.x; j < nin; j += blockDim.x) {
-        const int s = m.act[j];
-        const double pap = __ldcg(acc0 + s);
-        m.alpha[s] = pap > 0.0 ? (float)(m.gamma[s] / pap) : 0.f;
-        if (!(pap > 0.0)) {  // breakdown: not SPD in FP32 (or NaN)
-          m.inner_on[s] = 0;
-          m.status[s] = (pap == pap) ? COLAGB_SYS_BREAKDOWN : COLAGB_SYS_NAN;
-        }
-      }
-      __syncthreads();
-      // B: d += alpha p ; r -= alpha Ap ; (no FSAI: <r, z>) ; |r|^2
-      sweep_chunks(m.act, nin, n, acc2, [&](int s, int64_t i) -> float {
-        const int64_t u = (int64_t)s * n + i;
-        const float al = m.alpha[s];
-        a.d[u] += al * a.p[u];
-        const float rv = a.r[u] - al * a.ap[u];
-        a.r[u] = rv;
-        return rv * rv;
-      }, redf);
-      if (!any_fsai) {
-        sweep_chunks(m.act, nin, n, acc1, [&](int s, int64_t i) -> float {
-          const int64_t u = (int64_t)s * n + i;
-          return a.r[u] * apply_m(s, i);
-        }, redf);
-      }
-      if (!grid_sync(a.gb)) return;
-      if (any_fsai) {
-        // t = G r (FSAI systems) ; then z = G^T t and <r, z> for all systems
-        sweep_chunks(m.act, nin, n, nullptr, [&](int s, int64_t i) -> float {
-          if (m.prec[s] != COLAGB_PREC_FSAI) return 0.f;
-          const float* g = a.g_vals + (int64_t)s * a.g_nnz;
-          const float* rs = a.r + (int64_t)s * n;
-          float v = 0.f;
-          for (int32_t e = a.g_indptr[i]; e < a.g_indptr[i + 1]; ++e) v += g[e] * rs[a.g_indices[e]];
-          a.t[(int64_t)s * n + i] = v;
-          return 0.f;
-        }, redf);
-        if (!grid_sync(a.gb)) return;
-        sweep_chunks(m.act, nin, n, acc1, [&](int s, int64_t i) -> float {
-          const int64_t u = (int64_t)s * n + i;
-          const float zv = apply_m(s, i);
-          a.z[u] = zv;
-          return a.r[u] * zv;
-        }, redf);
-        if (!grid_sync(a.gb)) return;
-      }
-      // C: beta, stop tests, p = z + beta p
-      for (int j = threadIdx.x; j < nin; j += blockDim.x) {
-        const int s = m.act[j];
-        const double g1 = __ldcg(acc1 + s);
-        const float rn = (float)sqrt(__ldcg(acc2 + s));
-        m.beta[s] = m.gamma[s] != 0.0 ? (float)(g1 / m.gamma[s]) : 0.f;
-        m.gamma[s] = g1;
-        m.rnin[s] = rn;
-        m.it_sweep[s] += 1;
-        if (!(rn == rn)) { m.inner_on[s] = 0; m.status[s] = COLAGB_SYS_NAN; }
-        if (rn <= (float)a.inner_tol || m.it_sweep[s] >= a.max_inner) m.inner_on[s] = 0;
-      }
-      __syncthreads();
-      if (!grid_sync(a.gb)) return;  // all CTAs have read acc0..acc2
-      if (blockIdx.x == 0)
-        for (int j = threadIdx.x; j < nin; j += blockDim.x) {
-          const int s = m.act[j];
-          acc0[s] = 0.0; acc1[s] = 0.0; acc2[s] = 0.0;
-        }
-      nin = build_active(S, m.act, [&](int s) { return m.inner_on[s] != 0; });
-      if (nin == 0) break;
-      sweep_chunks(m.act, nin, n, nullptr, [&](int s, int64_t i) -> float {
-        const int64_t u = (int64_t)s * n + i;
-        const float zv = any_fsai ? (a.z ? a.z[u] : 0.f) : apply_m(s, i);
-        a.p[u] = zv + m.beta[s] * a.p[u];
-        return 0.f;
-      }, redf);
-      if (!grid_sync(a.gb)) return;
-    }
-
-    // ---- refinement: x += |r64| d ; r64 = b - A x ; relres ----
-    nact = build_active(S, m.act, [&](int s) { return m.status[s] == COLAGB_SYS_RUNNING; });
-    for (int s = threadIdx.x; s < S; s += blockDim.x) {
-      m.it_total[s] += m.it_sweep[s];
-    }
-    __syncthreads();
-    {
-      int mx = 0;
-      for (int s = 0; s < S; ++s) mx = m.it_sweep[s] > mx ? m.it_sweep[s] : mx;
-      max_total_inner += mx;
-    }
-    sweep_chunks(m.act, nact, n, nullptr, [&](int s, int64_t i) -> float {
-      const int64_t u = (int64_t)s * n + i;
-      a.X[u] += m.rn64[s] * (double)a.d[u];
-      return 0.f;
-    }, redf);
-    if (!grid_sync(a.gb)) return;
-    sweep_chunks64(m.act, nact, n, acc3, [&](int s, int64_t i) -> double {
-      const int64_t u = (int64_t)s * n + i;
-      const float* vals = a.vals + (int64_t)s * a.nnz;
-      const double* xs = a.X + (int64_t)s * n;
-      double ax = 0.0;
-      for (int32_t j = a.indptr[i]; j < a.indptr[i + 1]; ++j) ax += (double)vals[j] * xs[a.indices[j]];
-      const double rv = a.B[u] - ax;
-      a.r64[u] = rv;
-      return rv * rv;
-    }, redd);
-    if (!grid_sync(a.gb)) return;
-    for (int j = threadIdx.x; j < nact; j += blockDim.x) {
-      const int s = m.act[j];
-      const double rn = sqrt(__ldcg(acc3 + s));
-      const double rr = rn / a.bnorm[s];
-      if (!(rr == rr)) m.status[s] = COLAGB_SYS_NAN;
-      // the FP64 true residual judges the learned preconditioner
-      if (a.fallback && m.prec[s] == COLAGB_PREC_FSAI && rr > 0.5 * m.relres[s]) {
-        m.prec[s] = COLAGB_PREC_JACOBI;
-      }
-      m.rn64[s] = rn;
-      m.relres[s] = rr;
-    }
-    __syncthreads();
-    if (!grid_sync(a.gb)) return;
-    if (blockIdx.x == 0)
-      for (int j = threadIdx.x; j < nact; j += blockDim.x) acc3[m.act[j]] = 0.0;
+  bool any_fsai = false;
+  for (int j = 0; j < nact; ++j) any_fsai |= m.prec(m.act()[j]) == COLAGB_PREC_FSAI;
+  if (any_fsai) {
+    sweep<float, 0>(m.act(), nact, n, FFsaiT{&a, &m}, acc, redf);
     if (!grid_sync(a.gb)) return;
   }
-  // ---- results ----
+  sweep<float, 1>(m.act(), nact, n, FZ{&a, &m}, acc + 5, redf);  // z, <r, z>
+  if (!grid_sync(a.gb)) return;
+  for (int j = threadIdx.x; j < nact; j += blockDim.x) {
+    const int s = m.act()[j];
+    m.gamma(s) = __ldcg(acc[5] + s);
+    const float rn = (float)sqrt(__ldcg(acc[3] + s));
+    m.rn(s) = rn;
+    m.rmax(s) = rn;
+    m.beta(s) = 0.f;
+    if (rn <= (float)a.tol) { m.status(s) = COLAGB_SYS_CONVERGED; m.flags(s) = 0; }
+  }
+  __syncthreads();
+  nact = build_list(S, m.act(), [&](int s) { return (m.flags(s) & F_ACTIVE) != 0; });
+  sweep<float, 0>(m.act(), nact, n, FPUpdate{&a, &m, true}, acc, redf);  // p = z
+  if (!grid_sync(a.gb)) return;
+  zero_acc(3);
+  zero_acc(4);
+  zero_acc(5);
+  if (!grid_sync(a.gb)) return;
+
+  // ---------------- CG iterations ----------------
+  int max_rep = 0, max_it = 0;
+  while (nact > 0) {
+    // Every read of accumulators 1-5 happened before the barrier that closed the previous
+    // iteration, and the next writes to them follow at least one more barrier.
+    zero_acc(1);
+    zero_acc(2);
+    zero_acc(3);
+    zero_acc(4);
+    zero_acc(5);
+    // A: Ap = A p, <p, Ap>
+    sweep<float, 1>(m.act(), nact, n, FMatvec{&a}, acc, redf);
+    if (!grid_sync(a.gb)) return;
+    for (int j = threadIdx.x; j < nact; j += blockDim.x) {
+      const int s = m.act()[j];
+      const double pap = __ldcg(acc[0] + s);
+      m.alpha(s) = pap > 0.0 ? (float)(m.gamma(s) / pap) : 0.f;
+      if (!(pap > 0.0)) {  // not SPD in FP32 (or NaN): stop this system, keep its last x
+        m.status(s) = (pap == pap) ? COLAGB_SYS_BREAKDOWN : COLAGB_SYS_NAN;
+        m.flags(s) = 0;
+      }
+    }
+    __syncthreads();
+    nact = build_list(S, m.act(), [&](int s) { return (m.flags(s) & F_ACTIVE) != 0; });
+    // B: d, r updates, |r|^2, <r, M r>
+    sweep<float, 2>(m.act(), nact, n, FUpdate{&a, &m}, acc + 1, redf);
+    if (!grid_sync(a.gb)) return;
+    zero_acc(0);
+    int nrepl = 0;
+    if (threadIdx.x == 0) {
+      for (int j = 0; j < nact; ++j) {
+        const int s = m.act()[j];
+        const float rn = (float)sqrt(__ldcg(acc[2] + s));
+        m.rn(s) = rn;
+        m.it(s) += 1;
+        int f = m.flags(s) & ~(F_REPLACE | F_RESTART);
+        if (!(rn == rn)) {
+          m.status(s) = COLAGB_SYS_NAN;
+          f = 0;
+        } else if (rn <= delta * m.rmax(s) || rn <= (float)a.tol || m.it(s) >= a.max_inner) {
+          f |= F_REPLACE;
+        }
+        m.flags(s) = f;
+      }
+    }
+    __syncthreads();
+    nrepl = build_list(S, m.act2(), [&](int s) { return (m.flags(s) & F_REPLACE) != 0; });
+    if (nrepl > 0) {
+      // R1: x += d, d = 0 ; R2: r = b/|b| - A x in FP64
+      sweep<double, 0>(m.act2(), nrepl, n, FFlushX{&a}, acc, redd);
+      if (!grid_sync(a.gb)) return;
+      sweep<double, 2>(m.act2(), nrepl, n, FResidual{&a, &m}, acc + 3, redd);
+      if (!grid_sync(a.gb)) return;
+      if (threadIdx.x == 0) {
+        for (int j = 0; j < nrepl; ++j) {
+          const int s = m.act2()[j];
+          const double rr = sqrt(__ldcg(acc[3] + s));
+          m.nrep(s) += 1;
+          int f = m.flags(s);
+          if (!(rr == rr)) {
+            m.status(s) = COLAGB_SYS_NAN;
+            f = 0;
+          } else if (rr <= a.tol) {
+            m.status(s) = COLAGB_SYS_CONVERGED;
+            f = 0;
+          } else if (m.it(s) >= a.max_inner || m.nrep(s) >= a.max_sweeps) {
+            m.status(s) = COLAGB_SYS_MAX_ITERS;
+            f = 0;
+          } else {
+            if (a.fallback && m.prec(s) == COLAGB_PREC_FSAI && rr > 0.5 * m.relres_prev(s)) {
+              m.prec(s) = COLAGB_PREC_JACOBI;  // the FP64 residual judged the learned preconditioner
+              f |= F_RESTART;
+            }
+            if (restart_mode) f |= F_RESTART;
+          }
+          m.relres_prev(s) = rr;
+          m.relres(s) = rr;
+          m.rn(s) = (float)rr;
+          m.rmax(s) = (float)rr;
+          m.flags(s) = f;
+        }
+      }
+      __syncthreads();
+    }
+    nact = build_list(S, m.act(), [&](int s) { return (m.flags(s) & F_ACTIVE) != 0; });
+    if (nact == 0) break;
+    any_fsai = false;
+    bool switched = false;
+    for (int j = 0; j < nact; ++j) {
+      const int s = m.act()[j];
+      any_fsai |= m.prec(s) == COLAGB_PREC_FSAI;
+      switched |= (m.flags(s) & F_RESTART) && a.prec_kind == COLAGB_PREC_FSAI;
+    }
+    const bool zphase = any_fsai || switched;
+    if (any_fsai) {
+      sweep<float, 0>(m.act(), nact, n, FFsaiT{&a, &m}, acc, redf);
+      if (!grid_sync(a.gb)) return;
+    }
+    if (zphase) {
+      sweep<float, 1>(m.act(), nact, n, FZ{&a, &m}, acc + 5, redf);
+      if (!grid_sync(a.gb)) return;
+    }
+    for (int j = threadIdx.x; j < nact; j += blockDim.x) {
+      const int s = m.act()[j];
+      const double g1 = zphase ? __ldcg(acc[5] + s)
+                               : ((m.flags(s) & F_REPLACE) ? __ldcg(acc[4] + s) : __ldcg(acc[1] + s));
+      m.beta(s) = (m.flags(s) & F_RESTART) || m.gamma(s) == 0.0 ? 0.f : (float)(g1 / m.gamma(s));
+      m.gamma(s) = g1;
+    }
+    __syncthreads();
+    // C: p = z + beta p
+    sweep<float, 0>(m.act(), nact, n, FPUpdate{&a, &m, zphase}, acc, redf);
+    if (!grid_sync(a.gb)) return;
+  }
+  // ---------------- finish: flush d, scale x, report ----------------
+  nact = build_list(S, m.act(), [&](int) { return true; });
+  sweep<double, 0>(m.act(), nact, n, FFlushX{&a}, acc, redd);
+  if (!grid_sync(a.gb)) return;
+  sweep<double, 0>(m.act(), nact, n, FScaleX{&a}, acc, redd);
   if (blockIdx.x == 0) {
     for (int s = threadIdx.x; s < S; s += blockDim.x) {
-      int st = m.status[s];
-      if (st == COLAGB_SYS_RUNNING) st = m.relres[s] <= a.tol ? COLAGB_SYS_CONVERGED : COLAGB_SYS_MAX_ITERS;
-      if (st == COLAGB_SYS_CONVERGED && a.prec_kind == COLAGB_PREC_FSAI && m.prec[s] != COLAGB_PREC_FSAI)
+      int st = m.status(s);
+      if (st == COLAGB_SYS_RUNNING) st = COLAGB_SYS_MAX_ITERS;
+      if (st == COLAGB_SYS_CONVERGED && a.prec_kind == COLAGB_PREC_FSAI && m.prec(s) != COLAGB_PREC_FSAI)
         st = COLAGB_SYS_FALLBACK;
       if (a.out_status) a.out_status[s] = st;
-      if (a.out_iters) a.out_iters[s] = m.it_total[s];
-      if (a.out_relres) a.out_relres[s] = m.relres[s];
+      if (a.out_iters) a.out_iters[s] = m.it(s);
+      if (a.out_relres) a.out_relres[s] = m.relres(s);
     }
     if (threadIdx.x == 0) {
-      a.summary[0] = sweep;
-      a.summary[1] = max_total_inner;
+      for (int s = 0; s < S; ++s) {
+        max_rep = m.nrep(s) > max_rep ? m.nrep(s) : max_rep;
+        max_it = m.it(s) > max_it ? m.it(s) : max_it;
+      }
+      a.summary[0] = max_rep;
+      a.summary[1] = max_it;
     }
   }
 }
 
-static size_t batched_smem(int64_t S) { return (size_t)S * (3 * 8 + 9 * 4) + 16 * 12; }
+static size_t batched_smem(int64_t S) { return (size_t)S * (3 * 8 + 11 * 4) + 64; }
 
 struct BatchedWs {
   float *r, *p, *ap, *d, *z, *t, *dinv;
-  double *r64, *acc, *bnorm;
-  unsigned int* bar;  // count, generation, err
+  double *acc, *bnorm;
+  unsigned int* bar;
   int* summary;
 };
 
@@ -445,12 +640,11 @@ static BatchedWs carve_batched(Bump& ws, const colagb_batched_csr& A, const cola
   w.p = ws.take<float>(sn);
   w.ap = ws.take<float>(sn);
   w.d = ws.take<float>(sn);
+  w.z = ws.take<float>(sn);
   const bool fsai = prm.preconditioner == COLAGB_PREC_FSAI;
   const bool jac = prm.preconditioner == COLAGB_PREC_JACOBI || (fsai && prm.fallback);
-  w.z = fsai ? ws.take<float>(sn) : nullptr;
   w.t = fsai ? ws.take<float>(sn) : nullptr;
   w.dinv = jac ? ws.take<float>(sn) : nullptr;
-  w.r64 = ws.take<double>(sn);
   w.acc = ws.take<double>(6 * S);
   w.bnorm = ws.take<double>(S);
   w.bar = ws.take<unsigned int>(8);
@@ -465,10 +659,13 @@ static int validate_batched(const colagb_batched_csr* A, const colagb_ir_params*
     return fail(COLAGB_ERR_INVALID, "batched CG: missing CSR arrays");
   if (prm->preconditioner < 0 || prm->preconditioner > 2)
     return fail(COLAGB_ERR_INVALID, "batched CG: unknown preconditioner");
+  if (prm->mode != COLAGB_IR_RELIABLE && prm->mode != COLAGB_IR_RESTART)
+    return fail(COLAGB_ERR_INVALID, "batched CG: unknown refinement mode");
   if (prm->preconditioner == COLAGB_PREC_FSAI &&
       (!A->g_indptr || !A->g_indices || !A->gt_indptr || !A->gt_indices || !A->gt_perm || !A->g_values))
     return fail(COLAGB_ERR_INVALID, "batched CG: FSAI preconditioner needs G and G^T patterns and values");
-  if (!(prm->tol > 0) || !(prm->inner_tol > 0)) return fail(COLAGB_ERR_INVALID, "batched CG: tolerances must be > 0");
+  if (!(prm->tol > 0) || !(prm->inner_tol > 0) || !(prm->inner_tol < 1))
+    return fail(COLAGB_ERR_INVALID, "batched CG: need tol > 0 and 0 < inner_tol < 1");
   if (prm->max_sweeps < 0 || prm->max_inner_iters < 0) return fail(COLAGB_ERR_INVALID, "batched CG: negative limits");
   if (A->n >= (int64_t)1 << 31 || A->nnz >= (int64_t)1 << 31)
     return fail(COLAGB_ERR_INVALID, "batched CG: n and nnz must fit int32 indices");
@@ -483,7 +680,7 @@ extern "C" int colagb_cg_batched_csr_workspace_bytes(const colagb_batched_csr* A
                                                      size_t* bytes) {
   COLAGB_TRY(validate_batched(A, params));
   if (!bytes) return fail(COLAGB_ERR_INVALID, "null bytes");
-  Bump ws(nullptr, 0);
+  Bump ws = Bump::measuring();
   carve_batched(ws, *A, *params);
   *bytes = ws.peak;
   return COLAGB_OK;
@@ -501,6 +698,8 @@ extern "C" int colagb_cg_batched_csr_solve(const colagb_batched_csr* A, const do
   result->status = COLAGB_OK;
   if (S_all == 0 || A->n == 0) return COLAGB_OK;
   if (!B || !X) return fail(COLAGB_ERR_INVALID, "batched CG: null B/X");
+  if (A->n % 4 != 0 || (uintptr_t)B % 16 != 0 || (uintptr_t)X % 16 != 0)
+    return fail(COLAGB_ERR_INVALID, "batched CG: n must be a multiple of 4 and B, X 16-byte aligned");
   Bump ws(workspace, workspace_bytes);
   BatchedWs w = carve_batched(ws, *A, *params);
   if (workspace == nullptr || ws.overflow())
@@ -514,7 +713,8 @@ extern "C" int colagb_cg_batched_csr_solve(const colagb_batched_csr* A, const do
     a.S = S;
     a.indptr = A->indptr;
     a.indices = A->indices;
-    a.vals = A->values + s0 * A->nnz;
+    a.vstride = A->shared_values ? 0 : A->nnz;
+    a.vals = A->values + s0 * a.vstride;
     a.g_nnz = A->g_nnz;
     a.g_indptr = A->g_indptr;
     a.g_indices = A->g_indices;
@@ -525,7 +725,6 @@ extern "C" int colagb_cg_batched_csr_solve(const colagb_batched_csr* A, const do
     a.B = B + s0 * A->n;
     a.X = X + s0 * A->n;
     a.r = w.r; a.p = w.p; a.ap = w.ap; a.d = w.d; a.z = w.z; a.t = w.t; a.dinv = w.dinv;
-    a.r64 = w.r64;
     a.acc = w.acc;
     a.bnorm = w.bnorm;
     a.out_status = per_system_status ? per_system_status + s0 : nullptr;
@@ -538,6 +737,7 @@ extern "C" int colagb_cg_batched_csr_solve(const colagb_batched_csr* A, const do
     a.max_inner = params->max_inner_iters;
     a.prec_kind = params->preconditioner;
     a.fallback = params->fallback;
+    a.mode = params->mode;
     a.gb.count = w.bar;
     a.gb.generation = w.bar + 1;
     a.gb.err = reinterpret_cast<int*>(w.bar + 2);
@@ -546,15 +746,15 @@ extern "C" int colagb_cg_batched_csr_solve(const colagb_batched_csr* A, const do
     if (smem > 48 * 1024)
       COLAGB_CUDA(cudaFuncSetAttribute(k_batched_ir, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int occ = 0;
-    COLAGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batched_ir, 256, smem));
+    COLAGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batched_ir, kThreads, smem));
     if (occ < 1) return fail(COLAGB_ERR_UNSUPPORTED, "batched CG kernel cannot be resident");
-    const int nb = num_sms() * (occ < 4 ? occ : 4);
+    const int nb = num_sms() * (occ < 8 ? occ : 8);
     a.gb.nblocks = (unsigned)nb;
     COLAGB_CUDA(cudaMemsetAsync(w.bar, 0, 8 * sizeof(unsigned int), st));
     COLAGB_CUDA(cudaMemsetAsync(w.acc, 0, 6 * S * sizeof(double), st));
     void* args[] = {&a};
-    COLAGB_CUDA(cudaLaunchCooperativeKernel((const void*)k_batched_ir, dim3(nb), dim3(256), args, smem, st));
-    int h[4] = {0, 0, 0, 0};
+    COLAGB_CUDA(cudaLaunchCooperativeKernel((const void*)k_batched_ir, dim3(nb), dim3(kThreads), args, smem, st));
+    int h[2] = {0, 0};
     unsigned int herr = 0;
     COLAGB_CUDA(cudaMemcpyAsync(h, w.summary, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
     COLAGB_CUDA(cudaMemcpyAsync(&herr, w.bar + 2, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
@@ -564,7 +764,7 @@ extern "C" int colagb_cg_batched_csr_solve(const colagb_batched_csr* A, const do
       return fail(COLAGB_ERR_TIMEOUT, "batched CG: a grid barrier timed out");
     }
     result->sweeps = h[0] > result->sweeps ? h[0] : result->sweeps;
-    result->total_inner_iters += h[1];
+    result->total_inner_iters = h[1] > result->total_inner_iters ? h[1] : result->total_inner_iters;
   }
   return COLAGB_OK;
 }

@@ -39,9 +39,11 @@ inline size_t align_up(size_t v, size_t a = 256) { return (v + a - 1) / a * a; }
 struct Bump {
   char* base;
   size_t cap;
+  bool measure;  // size queries only: nothing is launched
   size_t used = 0;
   size_t peak = 0;
-  Bump(void* b, size_t c) : base(static_cast<char*>(b)), cap(c) {}
+  Bump(void* b, size_t c, bool measure_only = false) : base(static_cast<char*>(b)), cap(c), measure(measure_only) {}
+  static Bump measuring() { return Bump(nullptr, 0, true); }
   template <class T>
   T* take(size_t count) {
     size_t off = align_up(used);
@@ -51,7 +53,7 @@ struct Bump {
     return reinterpret_cast<T*>(base + off);
   }
   void release(size_t mark) { used = mark; }
-  bool overflow() const { return base != nullptr && peak > cap; }
+  bool overflow() const { return !measure && peak > cap; }
 };
 
 // ---- device-side element conversion ------------------------------------------------------

@@ -1,0 +1,538 @@
+// Learned factored sparse approximate inverse (FSAI) preconditioner for 5-point operators on an
+// m x m grid: a small convolutional network reads the operator's coefficients and outputs the
+// lower-triangular factor G on A's own lower pattern {N = p-m, W = p-1, C = p}; P = G^T G.
+//
+// Parametrisation: with d = diag(A), a_N = A[p, p-m], a_W = A[p, p-1] and the Schur complement
+// s_p = d_p - a_N^2 / d_N - a_W^2 / d_W, the closed-form FSAI row of this pattern is
+//   G_C = 1/sqrt(s_p),  G_N = -(a_N/d_N)/sqrt(s_p),  G_W = -(a_W/d_W)/sqrt(s_p).
+// The network's outputs o = (o0, o1, o2) per cell scale it: G_C *= e^o0, G_N *= e^o0 (1 + o1),
+// G_W *= e^o0 (1 + o2).  G_C > 0 for any o, so P is SPD whatever the network predicts.
+//
+// Training loss per system (pairs (r, e) with A e = r, e from this project's CG):
+//   l = ||P r - e||_A^2 / ||e||_A^2 = (v^T A v - 2 v^T r + e^T r) / (e^T r),  v = G^T G r.
+// Its gradient: dl/dv = 2 (A v - r) / (e^T r) =: g;  dl/dG_pq = t_p g_q + (G g)_p r_q with t = G r.
+//
+// Layouts: grid fields are (S, C, m, m) float32, row-major cells p = i*m + j.
+#include <cmath>
+#include <string>
+
+#include "common.cuh"
+
+namespace colagb {
+
+// ---------------------------------------------------------------------------------------------
+// stencil extraction: CSR values (S, nnz) on the grid's 5-point pattern -> (S, 5, m, m) [N, W, C, E, S]
+__global__ void k_grid5_stencil(const int32_t* __restrict__ indptr, const int32_t* __restrict__ indices,
+                                const float* __restrict__ values, int64_t nnz, int64_t m, int64_t S,
+                                float* __restrict__ st, int* err) {
+  const int64_t n = m * m;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < S * n; u += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s = u / n, p = u % n;
+    float o[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int32_t e = indptr[p]; e < indptr[p + 1]; ++e) {
+      const int64_t c = indices[e];
+      const float v = values[s * nnz + e];
+      const int64_t d = c - p;
+      if (d == -m) o[0] += v;
+      else if (d == -1) o[1] += v;
+      else if (d == 0) o[2] += v;
+      else if (d == 1) o[3] += v;
+      else if (d == m) o[4] += v;
+      else atomicExch(err, 1);
+    }
+    float* base = st + s * 5 * n + p;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) base[k * n] = o[k];
+  }
+}
+
+__device__ __forceinline__ float at5(const float* st, int64_t n, int k, int64_t p) { return st[k * n + p]; }
+
+// features (S, 6, m, m): -a_N/d, -a_W/d, -a_E/d, -a_S/d, log(d/d_N), log(d/d_W)  (0 where absent)
+__global__ void k_fsai_features(const float* __restrict__ st, int64_t m, int64_t S, float* __restrict__ f) {
+  const int64_t n = m * m;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < S * n; u += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s = u / n, p = u % n;
+    const int64_t i = p / m, j = p % m;
+    const float* a = st + s * 5 * n;
+    const float d = at5(a, n, 2, p);
+    float* o = f + s * 6 * n + p;
+    o[0] = -at5(a, n, 0, p) / d;
+    o[1 * n] = -at5(a, n, 1, p) / d;
+    o[2 * n] = -at5(a, n, 3, p) / d;
+    o[3 * n] = -at5(a, n, 4, p) / d;
+    o[4 * n] = i > 0 ? logf(d / at5(a, n, 2, p - m)) : 0.f;
+    o[5 * n] = j > 0 ? logf(d / at5(a, n, 2, p - 1)) : 0.f;
+  }
+}
+
+// closed-form FSAI coefficients (S, 3, m, m): [N, W, C] rows of G for o = 0
+__device__ __forceinline__ void fsai_closed_form(const float* a, int64_t n, int64_t m, int64_t p, float& fN, float& fW,
+                                                 float& fC) {
+  const int64_t i = p / m, j = p % m;
+  const float d = at5(a, n, 2, p);
+  float sch = d, cN = 0.f, cW = 0.f;
+  if (i > 0) {
+    const float aN = at5(a, n, 0, p), dN = at5(a, n, 2, p - m);
+    sch -= aN * aN / dN;
+    cN = -aN / dN;
+  }
+  if (j > 0) {
+    const float aW = at5(a, n, 1, p), dW = at5(a, n, 2, p - 1);
+    sch -= aW * aW / dW;
+    cW = -aW / dW;
+  }
+  const float is = rsqrtf(sch);
+  fC = is;
+  fN = cN * is;
+  fW = cW * is;
+}
+
+// G stencil (S, 3, m, m) [N, W, C] from the network output o (S, 3, m, m) (o may be null: o = 0)
+__global__ void k_fsai_assemble(const float* __restrict__ st, const float* __restrict__ o, int64_t m, int64_t S,
+                                float* __restrict__ g) {
+  const int64_t n = m * m;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < S * n; u += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s = u / n, p = u % n;
+    float fN, fW, fC;
+    fsai_closed_form(st + s * 5 * n, n, m, p, fN, fW, fC);
+    float o0 = 0.f, o1 = 0.f, o2 = 0.f;
+    if (o) {
+      o0 = o[s * 3 * n + p];
+      o1 = o[s * 3 * n + n + p];
+      o2 = o[s * 3 * n + 2 * n + p];
+    }
+    const float e0 = expf(o0);
+    g[s * 3 * n + p] = e0 * (1.f + o1) * fN;
+    g[s * 3 * n + n + p] = e0 * (1.f + o2) * fW;
+    g[s * 3 * n + 2 * n + p] = e0 * fC;
+  }
+}
+
+// G stencil -> compact CSR values (S, g_nnz) in the lower pattern's order [N, W, C] (absent skipped)
+__global__ void k_fsai_compact(const float* __restrict__ g, const int32_t* __restrict__ g_indptr, int64_t m, int64_t S,
+                               int64_t g_nnz, float* __restrict__ out) {
+  const int64_t n = m * m;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < S * n; u += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s = u / n, p = u % n;
+    const int64_t i = p / m, j = p % m;
+    int64_t e = g_indptr[p];
+    float* o = out + s * g_nnz;
+    if (i > 0) o[e++] = g[s * 3 * n + p];
+    if (j > 0) o[e++] = g[s * 3 * n + n + p];
+    o[e] = g[s * 3 * n + 2 * n + p];
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// 3x3 convolution, zero padding 1, stride 1.  in (B, CIN, H, W), w (COUT, CIN, 3, 3), b (COUT).
+template <int COUT>
+__global__ void __launch_bounds__(256) k_conv3_fwd(const float* __restrict__ in, int cin, int H, int W,
+                                                   const float* __restrict__ w, const float* __restrict__ bias,
+                                                   int relu, float* __restrict__ out) {
+  extern __shared__ float sw[];  // COUT * cin * 9 weights
+  __shared__ float tile[18][18];
+  const int bimg = blockIdx.z;
+  const int x0 = blockIdx.x * 16, y0 = blockIdx.y * 16;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  for (int q = threadIdx.x; q < COUT * cin * 9; q += 256) sw[q] = w[q];
+  float acc[COUT];
+#pragma unroll
+  for (int c = 0; c < COUT; ++c) acc[c] = bias ? bias[c] : 0.f;
+  const int64_t plane = (int64_t)H * W;
+  for (int ci = 0; ci < cin; ++ci) {
+    const float* src = in + ((int64_t)bimg * cin + ci) * plane;
+    __syncthreads();
+    for (int q = threadIdx.x; q < 18 * 18; q += 256) {
+      const int yy = y0 - 1 + q / 18, xx = x0 - 1 + q % 18;
+      tile[q / 18][q % 18] = (yy >= 0 && yy < H && xx >= 0 && xx < W) ? src[(int64_t)yy * W + xx] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int ky = 0; ky < 3; ++ky)
+#pragma unroll
+      for (int kx = 0; kx < 3; ++kx) {
+        const float v = tile[ty + ky][tx + kx];
+#pragma unroll
+        for (int c = 0; c < COUT; ++c) acc[c] += sw[(c * cin + ci) * 9 + ky * 3 + kx] * v;
+      }
+  }
+  const int y = y0 + ty, x = x0 + tx;
+  if (y < H && x < W) {
+#pragma unroll
+    for (int c = 0; c < COUT; ++c) {
+      const float v = acc[c];
+      out[((int64_t)bimg * COUT + c) * plane + (int64_t)y * W + x] = relu ? fmaxf(v, 0.f) : v;
+    }
+  }
+}
+
+// grad_in (B, CIN, H, W) from grad_out (B, cout, H, W); when `act` is given the forward output
+// was ReLU(act) and grad_out is masked by act > 0.
+template <int CIN>
+__global__ void __launch_bounds__(256) k_conv3_bwd_data(const float* __restrict__ gout, const float* __restrict__ act,
+                                                        int cout, int H, int W, const float* __restrict__ w,
+                                                        float* __restrict__ gin) {
+  extern __shared__ float sw[];  // cout * CIN * 9
+  __shared__ float tile[18][18];
+  const int bimg = blockIdx.z;
+  const int x0 = blockIdx.x * 16, y0 = blockIdx.y * 16;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  for (int q = threadIdx.x; q < cout * CIN * 9; q += 256) sw[q] = w[q];
+  float acc[CIN];
+#pragma unroll
+  for (int c = 0; c < CIN; ++c) acc[c] = 0.f;
+  const int64_t plane = (int64_t)H * W;
+  for (int co = 0; co < cout; ++co) {
+    const float* g = gout + ((int64_t)bimg * cout + co) * plane;
+    const float* a = act ? act + ((int64_t)bimg * cout + co) * plane : nullptr;
+    __syncthreads();
+    for (int q = threadIdx.x; q < 18 * 18; q += 256) {
+      const int yy = y0 - 1 + q / 18, xx = x0 - 1 + q % 18;
+      float v = 0.f;
+      if (yy >= 0 && yy < H && xx >= 0 && xx < W) {
+        const int64_t o = (int64_t)yy * W + xx;
+        v = g[o];
+        if (a && !(a[o] > 0.f)) v = 0.f;
+      }
+      tile[q / 18][q % 18] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int ky = 0; ky < 3; ++ky)
+#pragma unroll
+      for (int kx = 0; kx < 3; ++kx) {
+        const float v = tile[ty + 2 - ky][tx + 2 - kx];
+#pragma unroll
+        for (int c = 0; c < CIN; ++c) acc[c] += sw[(co * CIN + c) * 9 + ky * 3 + kx] * v;
+      }
+  }
+  const int y = y0 + ty, x = x0 + tx;
+  if (y < H && x < W) {
+#pragma unroll
+    for (int c = 0; c < CIN; ++c) gin[((int64_t)bimg * CIN + c) * plane + (int64_t)y * W + x] = acc[c];
+  }
+}
+
+// grad_w partials: part[blk][(co*cin + ci)*9 + k] and part_b[blk][co]; blocks stride over tiles.
+__global__ void __launch_bounds__(256) k_conv3_bwd_weight(const float* __restrict__ gout, const float* __restrict__ act,
+                                                          const float* __restrict__ in, int B, int cin, int cout,
+                                                          int H, int W, float* __restrict__ part) {
+  extern __shared__ float sm[];
+  float* gt = sm;                         // cout * 256 (masked grad_out tile)
+  float* it = sm + cout * 256;            // cin * 324 (input tile with halo)
+  const int nw = cout * cin * 9;
+  const int tiles_x = (W + 15) / 16, tiles_y = (H + 15) / 16;
+  const int ntiles = tiles_x * tiles_y * B;
+  const int64_t plane = (int64_t)H * W;
+  float accw[12];  // up to 12 entries per thread (nw <= 3072)
+  float accb = 0.f;
+#pragma unroll
+  for (int q = 0; q < 12; ++q) accw[q] = 0.f;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int bimg = tile / (tiles_x * tiles_y);
+    const int rem = tile % (tiles_x * tiles_y);
+    const int y0 = (rem / tiles_x) * 16, x0 = (rem % tiles_x) * 16;
+    __syncthreads();
+    for (int q = threadIdx.x; q < cout * 256; q += 256) {
+      const int co = q / 256, yy = y0 + (q % 256) / 16, xx = x0 + (q % 16);
+      float v = 0.f;
+      if (yy < H && xx < W) {
+        const int64_t o = ((int64_t)bimg * cout + co) * plane + (int64_t)yy * W + xx;
+        v = gout[o];
+        if (act && !(act[o] > 0.f)) v = 0.f;
+      }
+      gt[q] = v;
+    }
+    for (int q = threadIdx.x; q < cin * 324; q += 256) {
+      const int ci = q / 324, yy = y0 - 1 + (q % 324) / 18, xx = x0 - 1 + (q % 18);
+      it[q] = (yy >= 0 && yy < H && xx >= 0 && xx < W) ? in[((int64_t)bimg * cin + ci) * plane + (int64_t)yy * W + xx]
+                                                       : 0.f;
+    }
+    __syncthreads();
+    for (int q = 0; q < 12; ++q) {
+      const int e = threadIdx.x + q * 256;
+      if (e >= nw) break;
+      const int co = e / (cin * 9), ci = (e / 9) % cin, k = e % 9, ky = k / 3, kx = k % 3;
+      const float* g = gt + co * 256;
+      const float* x = it + ci * 324;
+      float s = 0.f;
+      for (int py = 0; py < 16; ++py)
+#pragma unroll 4
+        for (int px = 0; px < 16; ++px) s += g[py * 16 + px] * x[(py + ky) * 18 + px + kx];
+      accw[q] += s;
+    }
+    if (threadIdx.x < cout) {
+      const float* g = gt + threadIdx.x * 256;
+      float s = 0.f;
+      for (int q = 0; q < 256; ++q) s += g[q];
+      accb += s;
+    }
+  }
+  float* out = part + (int64_t)blockIdx.x * (nw + cout);
+  for (int q = 0; q < 12; ++q) {
+    const int e = threadIdx.x + q * 256;
+    if (e < nw) out[e] = accw[q];
+  }
+  if (threadIdx.x < cout) out[nw + threadIdx.x] = accb;
+}
+
+__global__ void k_sum_partials(const float* __restrict__ part, int nblk, int len, float* __restrict__ out, int accumulate) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < len; e += gridDim.x * blockDim.x) {
+    float s = 0.f;
+    for (int b = 0; b < nblk; ++b) s += part[(int64_t)b * len + e];
+    out[e] = accumulate ? out[e] + s : s;
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// loss and gradient.  gs: G stencil (S, 3, m, m) [N, W, C]; st: A stencil (S, 5, m, m);
+// r, e: (S, n) pairs; sc: per-system FP64 scalars [3][S] = e^T r, v^T w, v^T r.
+__device__ __forceinline__ float g_row(const float* gs, int64_t n, int64_t m, int64_t p, const float* x) {
+  const int64_t i = p / m, j = p % m;
+  float v = gs[2 * n + p] * x[p];
+  if (i > 0) v += gs[p] * x[p - m];
+  if (j > 0) v += gs[n + p] * x[p - 1];
+  return v;
+}
+__device__ __forceinline__ float gt_row(const float* gs, int64_t n, int64_t m, int64_t q, const float* x) {
+  const int64_t i = q / m, j = q % m;
+  float v = gs[2 * n + q] * x[q];
+  if (i < m - 1) v += gs[q + m] * x[q + m];
+  if (j < m - 1) v += gs[n + q + 1] * x[q + 1];
+  return v;
+}
+__device__ __forceinline__ float a_row(const float* st, int64_t n, int64_t m, int64_t p, const float* x) {
+  const int64_t i = p / m, j = p % m;
+  float v = st[2 * n + p] * x[p];
+  if (i > 0) v += st[p] * x[p - m];
+  if (j > 0) v += st[n + p] * x[p - 1];
+  if (j < m - 1) v += st[3 * n + p] * x[p + 1];
+  if (i < m - 1) v += st[4 * n + p] * x[p + m];
+  return v;
+}
+
+// t = G r ; sc[0] += e^T r
+__global__ void __launch_bounds__(256) k_fsai_loss_t(const float* __restrict__ gs, const float* __restrict__ r,
+                                                     const float* __restrict__ e, int64_t m, int64_t S,
+                                                     float* __restrict__ t, double* sc) {
+  __shared__ float red[32];
+  const int64_t n = m * m;
+  const int64_t s = blockIdx.y;
+  const float* gss = gs + s * 3 * n;
+  float acc = 0.f;
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+    t[s * n + p] = g_row(gss, n, m, p, r + s * n);
+    acc += e[s * n + p] * r[s * n + p];
+  }
+  acc = block_sum(acc, red);
+  if (threadIdx.x == 0) atomicAdd(sc + s, (double)acc);
+}
+
+// v = G^T t
+__global__ void k_fsai_loss_v(const float* __restrict__ gs, const float* __restrict__ t, int64_t m, int64_t S,
+                              float* __restrict__ v) {
+  const int64_t n = m * m;
+  const int64_t s = blockIdx.y;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+    v[s * n + q] = gt_row(gs + s * 3 * n, n, m, q, t + s * n);
+}
+
+// w = A v ; sc[1] += v^T w ; sc[2] += v^T r
+__global__ void __launch_bounds__(256) k_fsai_loss_w(const float* __restrict__ st, const float* __restrict__ v,
+                                                     const float* __restrict__ r, int64_t m, int64_t S,
+                                                     float* __restrict__ w, double* sc) {
+  __shared__ float red[32];
+  const int64_t n = m * m;
+  const int64_t s = blockIdx.y;
+  float a1 = 0.f, a2 = 0.f;
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+    const float wv = a_row(st + s * 5 * n, n, m, p, v + s * n);
+    w[s * n + p] = wv;
+    a1 += v[s * n + p] * wv;
+    a2 += v[s * n + p] * r[s * n + p];
+  }
+  a1 = block_sum(a1, red);
+  a2 = block_sum(a2, red);
+  if (threadIdx.x == 0) {
+    atomicAdd(sc + S + s, (double)a1);
+    atomicAdd(sc + 2 * S + s, (double)a2);
+  }
+}
+
+// gradient w.r.t. the network output o (S, 3, m, m), averaged over systems
+__global__ void k_fsai_loss_grad(const float* __restrict__ st, const float* __restrict__ o,
+                                 const float* __restrict__ gs, const float* __restrict__ r, const float* __restrict__ t,
+                                 const float* __restrict__ w, const double* __restrict__ sc, int64_t m, int64_t S,
+                                 float* __restrict__ dout) {
+  const int64_t n = m * m;
+  const int64_t s = blockIdx.y;
+  const float inv = (float)(2.0 / (sc[s] * (double)S));
+  const float* rs = r + s * n;
+  const float* ws = w + s * n;
+  const float* gss = gs + s * 3 * n;
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = p / m, j = p % m;
+    const float gp = inv * (ws[p] - rs[p]);
+    const float gN = i > 0 ? inv * (ws[p - m] - rs[p - m]) : 0.f;
+    const float gW = j > 0 ? inv * (ws[p - 1] - rs[p - 1]) : 0.f;
+    const float GN = gss[p], GW = gss[n + p], GC = gss[2 * n + p];
+    const float u = GC * gp + GN * gN + GW * gW;
+    const float tp = t[s * n + p];
+    const float dC = tp * gp + u * rs[p];
+    const float dN = i > 0 ? tp * gN + u * rs[p - m] : 0.f;
+    const float dW = j > 0 ? tp * gW + u * rs[p - 1] : 0.f;
+    // G_C = e^o0 fC, G_N = e^o0 (1 + o1) fN, G_W = e^o0 (1 + o2) fW
+    float fN, fW, fC;
+    fsai_closed_form(st + s * 5 * n, n, m, p, fN, fW, fC);
+    const float e0 = o ? expf(o[s * 3 * n + p]) : 1.f;
+    dout[s * 3 * n + p] = dC * GC + dN * GN + dW * GW;
+    dout[s * 3 * n + n + p] = dN * e0 * fN;
+    dout[s * 3 * n + 2 * n + p] = dW * e0 * fW;
+  }
+}
+
+// Adam (decoupled, no weight decay)
+__global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m1,
+                       float* __restrict__ m2, int64_t count, float lr, float b1, float b2, float eps, float c1, float c2) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < count; q += (int64_t)gridDim.x * blockDim.x) {
+    const float gv = g[q];
+    const float a = b1 * m1[q] + (1.f - b1) * gv;
+    const float b = b2 * m2[q] + (1.f - b2) * gv * gv;
+    m1[q] = a;
+    m2[q] = b;
+    p[q] -= lr * (a / c1) / (sqrtf(b / c2) + eps);
+  }
+}
+
+static int grid_for(int64_t total) {
+  const int64_t want = ceil_div(total, 256);
+  const int64_t cap = (int64_t)num_sms() * 16;
+  return (int)(want < 1 ? 1 : (want > cap ? cap : want));
+}
+
+}  // namespace colagb
+
+using namespace colagb;
+
+extern "C" int colagb_grid5_stencil(const int32_t* indptr, const int32_t* indices, const float* values, int64_t nnz,
+                                    int64_t m, int64_t S, float* stencil, int32_t* err_flag, void* stream) {
+  if (!indptr || !indices || !values || !stencil || !err_flag || m < 1 || S < 0)
+    return fail(COLAGB_ERR_INVALID, "colagb_grid5_stencil: bad arguments");
+  if (S == 0) return COLAGB_OK;
+  k_grid5_stencil<<<grid_for(S * m * m), 256, 0, as_stream(stream)>>>(indptr, indices, values, nnz, m, S, stencil,
+                                                                      err_flag);
+  COLAGB_CUDA(cudaGetLastError());
+  return COLAGB_OK;
+}
+
+extern "C" int colagb_fsai_features(const float* stencil, int64_t m, int64_t S, float* feats, void* stream) {
+  if (!stencil || !feats || m < 1 || S < 0) return fail(COLAGB_ERR_INVALID, "colagb_fsai_features: bad arguments");
+  if (S == 0) return COLAGB_OK;
+  k_fsai_features<<<grid_for(S * m * m), 256, 0, as_stream(stream)>>>(stencil, m, S, feats);
+  COLAGB_CUDA(cudaGetLastError());
+  return COLAGB_OK;
+}
+
+extern "C" int colagb_fsai_assemble(const float* stencil, const float* net_out, int64_t m, int64_t S, float* g_stencil,
+                                    void* stream) {
+  if (!stencil || !g_stencil || m < 1 || S < 0) return fail(COLAGB_ERR_INVALID, "colagb_fsai_assemble: bad arguments");
+  if (S == 0) return COLAGB_OK;
+  k_fsai_assemble<<<grid_for(S * m * m), 256, 0, as_stream(stream)>>>(stencil, net_out, m, S, g_stencil);
+  COLAGB_CUDA(cudaGetLastError());
+  return COLAGB_OK;
+}
+
+extern "C" int colagb_fsai_compact(const float* g_stencil, const int32_t* g_indptr, int64_t m, int64_t S, int64_t g_nnz,
+                                   float* g_values, void* stream) {
+  if (!g_stencil || !g_indptr || !g_values || m < 1 || S < 0)
+    return fail(COLAGB_ERR_INVALID, "colagb_fsai_compact: bad arguments");
+  if (S == 0) return COLAGB_OK;
+  k_fsai_compact<<<grid_for(S * m * m), 256, 0, as_stream(stream)>>>(g_stencil, g_indptr, m, S, g_nnz, g_values);
+  COLAGB_CUDA(cudaGetLastError());
+  return COLAGB_OK;
+}
+
+extern "C" int colagb_conv3x3_forward(const float* in, int64_t B, int32_t cin, int32_t cout, int64_t H, int64_t W,
+                                      const float* weight, const float* bias, int32_t relu, float* out, void* stream) {
+  if (!in || !weight || !out || B < 0 || cin < 1 || H < 1 || W < 1 || (cout != 16 && cout != 3))
+    return fail(COLAGB_ERR_INVALID, "colagb_conv3x3_forward: bad arguments (cout must be 16 or 3)");
+  if (B == 0) return COLAGB_OK;
+  const size_t smem = (size_t)cout * cin * 9 * sizeof(float);
+  if (smem > 40 * 1024) return fail(COLAGB_ERR_INVALID, "colagb_conv3x3_forward: too many weights");
+  dim3 grid((unsigned)ceil_div(W, 16), (unsigned)ceil_div(H, 16), (unsigned)B);
+  if (cout == 16)
+    k_conv3_fwd<16><<<grid, 256, smem, as_stream(stream)>>>(in, cin, (int)H, (int)W, weight, bias, relu, out);
+  else
+    k_conv3_fwd<3><<<grid, 256, smem, as_stream(stream)>>>(in, cin, (int)H, (int)W, weight, bias, relu, out);
+  COLAGB_CUDA(cudaGetLastError());
+  return COLAGB_OK;
+}
+
+extern "C" int colagb_conv3x3_backward(const float* grad_out, const float* act, const float* in, int64_t B, int32_t cin,
+                                       int32_t cout, int64_t H, int64_t W, const float* weight, float* grad_in,
+                                       float* grad_wb, float* scratch, size_t scratch_bytes, void* stream) {
+  if (!grad_out || !in || !weight || !grad_wb || B < 0 || cin < 1 || cout < 1 || H < 1 || W < 1)
+    return fail(COLAGB_ERR_INVALID, "colagb_conv3x3_backward: bad arguments");
+  if (grad_in && cin != 16 && cin != 6) return fail(COLAGB_ERR_INVALID, "colagb_conv3x3_backward: cin must be 16 or 6");
+  const int nw = cout * cin * 9;
+  if (nw > 12 * 256) return fail(COLAGB_ERR_INVALID, "colagb_conv3x3_backward: too many weights");
+  cudaStream_t st = as_stream(stream);
+  const int nblk = num_sms() * 2;
+  const size_t need = (size_t)nblk * (nw + cout) * sizeof(float);
+  if (!scratch || scratch_bytes < need)
+    return fail(COLAGB_ERR_WORKSPACE, "colagb_conv3x3_backward: scratch too small (need " + std::to_string(need) + ")");
+  if (B == 0) return COLAGB_OK;
+  const size_t smw = (size_t)(cout * 256 + cin * 324) * sizeof(float);
+  if (smw > 48 * 1024)
+    COLAGB_CUDA(cudaFuncSetAttribute(k_conv3_bwd_weight, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smw));
+  k_conv3_bwd_weight<<<nblk, 256, smw, st>>>(grad_out, act, in, (int)B, cin, cout, (int)H, (int)W, scratch);
+  k_sum_partials<<<(unsigned)ceil_div(nw + cout, 256), 256, 0, st>>>(scratch, nblk, nw + cout, grad_wb, 0);
+  if (grad_in) {
+    const size_t sm = (size_t)nw * sizeof(float);
+    dim3 grid((unsigned)ceil_div(W, 16), (unsigned)ceil_div(H, 16), (unsigned)B);
+    if (cin == 16) k_conv3_bwd_data<16><<<grid, 256, sm, st>>>(grad_out, act, cout, (int)H, (int)W, weight, grad_in);
+    else k_conv3_bwd_data<6><<<grid, 256, sm, st>>>(grad_out, act, cout, (int)H, (int)W, weight, grad_in);
+  }
+  COLAGB_CUDA(cudaGetLastError());
+  return COLAGB_OK;
+}
+
+extern "C" int colagb_conv3x3_backward_scratch_bytes(int32_t cin, int32_t cout, size_t* bytes) {
+  if (!bytes) return fail(COLAGB_ERR_INVALID, "null");
+  *bytes = (size_t)num_sms() * 2 * (cout * cin * 9 + cout) * sizeof(float);
+  return COLAGB_OK;
+}
+
+extern "C" int colagb_fsai_loss_grad(const float* stencil, const float* net_out, const float* g_stencil, const float* r,
+                                     const float* e, int64_t m, int64_t S, float* grad_out, double* loss_terms,
+                                     float* scratch, size_t scratch_bytes, void* stream) {
+  if (!stencil || !g_stencil || !r || !e || !loss_terms || !scratch || m < 1 || S < 0)
+    return fail(COLAGB_ERR_INVALID, "colagb_fsai_loss_grad: bad arguments");
+  const int64_t n = m * m;
+  const size_t need = (size_t)3 * S * n * sizeof(float);
+  if (scratch_bytes < need) return fail(COLAGB_ERR_WORKSPACE, "colagb_fsai_loss_grad: scratch too small");
+  if (S == 0) return COLAGB_OK;
+  cudaStream_t st = as_stream(stream);
+  float* t = scratch;
+  float* v = t + S * n;
+  float* w = v + S * n;
+  COLAGB_CUDA(cudaMemsetAsync(loss_terms, 0, 3 * S * sizeof(double), st));
+  dim3 grid((unsigned)std::min<int64_t>(ceil_div(n, 256), 1024), (unsigned)S);
+  k_fsai_loss_t<<<grid, 256, 0, st>>>(g_stencil, r, e, m, S, t, loss_terms);
+  k_fsai_loss_v<<<grid, 256, 0, st>>>(g_stencil, t, m, S, v);
+  k_fsai_loss_w<<<grid, 256, 0, st>>>(stencil, v, r, m, S, w, loss_terms);
+  if (grad_out) k_fsai_loss_grad<<<grid, 256, 0, st>>>(stencil, net_out, g_stencil, r, t, w, loss_terms, m, S, grad_out);
+  COLAGB_CUDA(cudaGetLastError());
+  return COLAGB_OK;
+}
+
+extern "C" int colagb_adam_step(float* param, const float* grad, float* m1, float* m2, int64_t count, float lr, float beta1,
+                                float beta2, float eps, int32_t step, void* stream) {
+  if (!param || !grad || !m1 || !m2 || count < 0 || step < 1) return fail(COLAGB_ERR_INVALID, "colagb_adam_step: bad arguments");
+  if (count == 0) return COLAGB_OK;
+  const float c1 = 1.f - powf(beta1, (float)step), c2 = 1.f - powf(beta2, (float)step);
+  k_adam<<<grid_for(count), 256, 0, as_stream(stream)>>>(param, grad, m1, m2, count, lr, beta1, beta2, eps, c1, c2);
+  COLAGB_CUDA(cudaGetLastError());
+  return COLAGB_OK;
+}

@@ -464,7 +464,7 @@ using namespace colagb;
 extern "C" int colagb_lanczos_workspace_bytes(const colagb_op* A, int64_t bs, int32_t max_iters, size_t* bytes) {
   if (!A || !bytes || bs < 1 || max_iters < 0) return fail(COLAGB_ERR_INVALID, "colagb_lanczos_workspace_bytes: bad arguments");
   const int64_t n = A->nodes[A->root].rows;
-  Bump ws(nullptr, 0);
+  Bump ws = Bump::measuring();
   if (A->compute_dtype == COLAGB_F64) lz_carve<double>(ws, bs, max_iters, lz_blocks(n, bs));
   else lz_carve<float>(ws, bs, max_iters, lz_blocks(n, bs));
   size_t opb = 0;

@@ -356,7 +356,7 @@ int op_apply(const colagb_op* op, int node, const T* X, int64_t ldx, int64_t bsx
              int64_t k, int64_t batch, T alpha, T beta, Bump& ws, const int* skip, cudaStream_t st) {
   const colagb_op_node& nd = op->nodes[node];
   const std::vector<int32_t>& ch = op->children[node];
-  const bool measuring = ws.base == nullptr;
+  const bool measuring = ws.measure;
   switch (nd.kind) {
     case COLAGB_OP_DENSE:
     case COLAGB_OP_CSR:
@@ -655,7 +655,7 @@ extern "C" int colagb_op_info(const colagb_op* op, int64_t* rows, int64_t* cols,
 
 extern "C" int colagb_matmat_workspace_bytes(const colagb_op* op, int64_t k, size_t* bytes) {
   if (!op || !bytes || k < 0) return fail(COLAGB_ERR_INVALID, "colagb_matmat_workspace_bytes: bad arguments");
-  Bump ws(nullptr, 0);
+  Bump ws = Bump::measuring();
   int s = op->compute_dtype == COLAGB_F64
               ? op_apply<double>(op, op->root, nullptr, k, 0, nullptr, k, 0, k, 1, 1.0, 0.0, ws, nullptr, 0)
               : op_apply<float>(op, op->root, nullptr, k, 0, nullptr, k, 0, k, 1, 1.f, 0.f, ws, nullptr, 0);

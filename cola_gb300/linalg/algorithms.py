@@ -69,7 +69,7 @@ class Exact(Algorithm):
     pbar: bool = False
 
     def __call__(self, A, k):
-        from .trace import exact_diag
+        from .unary import exact_diag
         return exact_diag(A, k, self.bs)
 
 
@@ -84,7 +84,7 @@ class Hutch(Algorithm):
     key: Optional[PRNGKey] = None
 
     def __call__(self, A, k):
-        from .trace import hutchinson_diag_estimate
+        from .unary import hutchinson_diag_estimate
         return hutchinson_diag_estimate(A, k, **self.__dict__)[0]
 
 

@@ -49,10 +49,14 @@ def transpose_pattern(indptr: torch.Tensor, indices: torch.Tensor):
 
 @dataclass
 class BatchedCSR:
-    """S systems on one CSR pattern: indptr (n+1), indices (nnz), values (S, nnz) float32."""
+    """S systems on one CSR pattern: indptr (n+1), indices (nnz), values (S, nnz) float32.
+
+    values of shape (1, nnz) with ``shared=True`` is one matrix used by every system (many
+    right-hand sides solved with independent convergence)."""
     indptr: torch.Tensor
     indices: torch.Tensor
     values: torch.Tensor
+    shared: bool = False
 
     @property
     def n(self) -> int:
@@ -65,11 +69,54 @@ class BatchedCSR:
     def matvec(self, X: torch.Tensor) -> torch.Tensor:
         """Y[s] = A_s X[s] in FP64 (host-side helper for checks; uses torch sparse ops)."""
         out = []
-        for s in range(self.num_systems):
+        for s in range(X.shape[0]):
             A = torch.sparse_csr_tensor(self.indptr.to(torch.int64), self.indices.to(torch.int64),
-                                        self.values[s].double(), (self.n, self.n))
+                                        self.values[0 if self.shared else s].double(), (self.n, self.n))
             out.append(A @ X[s].double())
         return torch.stack(out)
+
+
+def solve_dense_batched(matrices, rhs, tol: float = 1e-6, max_iters: int = 1000):
+    """Independent dense SPD systems of uneven sizes, all solved by FP32 CG in one persistent launch.
+
+    Each system reproduces ``cola.linalg.solve(PSD(Dense(A_s)), b_s, CG(tol, max_iters))`` with its
+    own stop test (cg.py:94-154).  ``matrices``: list of (n_s, n_s) CUDA tensors; ``rhs``: list of
+    (n_s,) tensors.  Returns (list of solutions, per-system iterations, per-system status)."""
+    if len(matrices) != len(rhs):
+        raise ValueError("one right-hand side per matrix")
+    S = len(matrices)
+    if S == 0:
+        return [], torch.zeros(0, dtype=torch.int32), torch.zeros(0, dtype=torch.int32)
+    _capi.require_cuda(*matrices, *rhs)
+    dev = matrices[0].device
+    sizes = [int(A.shape[0]) for A in matrices]
+    for A, b in zip(matrices, rhs):
+        if A.shape != (b.shape[0], b.shape[0]):
+            raise ValueError(f"matrix {tuple(A.shape)} and right-hand side {tuple(b.shape)} do not match")
+    a_off = [0]
+    v_off = [0]
+    for n in sizes[:-1]:
+        a_off.append(a_off[-1] + n * n)
+        v_off.append(v_off[-1] + n)
+    vals = torch.cat([A.to(torch.float32).reshape(-1) for A in matrices])
+    B = torch.cat([b.to(torch.float32).reshape(-1) for b in rhs])
+    X = torch.empty_like(B)
+    total = int(B.numel())
+    t_sizes = torch.tensor(sizes, dtype=torch.int32, device=dev)
+    t_aoff = torch.tensor(a_off, dtype=torch.int64, device=dev)
+    t_voff = torch.tensor(v_off, dtype=torch.int64, device=dev)
+    iters = torch.zeros(S, dtype=torch.int32, device=dev)
+    status = torch.zeros(S, dtype=torch.int32, device=dev)
+    lib = _capi.load()
+    nbytes = C.c_size_t()
+    _capi.check(lib.colagb_cg_dense_batched_workspace_bytes(S, total, C.byref(nbytes)), "dense batched cg")
+    ws = _capi.workspace(nbytes.value, dev)
+    _capi.check(lib.colagb_cg_dense_batched_solve(S, t_sizes.data_ptr(), t_aoff.data_ptr(), t_voff.data_ptr(), total,
+                                                  vals.data_ptr(), B.data_ptr(), X.data_ptr(), float(tol),
+                                                  int(max_iters), iters.data_ptr(), status.data_ptr(), ws.data_ptr(),
+                                                  nbytes.value, _capi.stream_ptr(dev)), "dense batched cg")
+    sols = list(torch.split(X, sizes))
+    return sols, iters, status
 
 
 class FsaiPattern:
@@ -85,21 +132,27 @@ _PREC = {"none": _capi.PREC_NONE, None: _capi.PREC_NONE, "jacobi": _capi.PREC_JA
 
 
 def solve_batched(A: BatchedCSR, B: torch.Tensor, precond: str = "jacobi", tol: float = 1e-8,
-                  inner_tol: float = 1e-4, max_sweeps: int = 12, max_inner_iters: int = 20000,
-                  fsai: tuple | None = None, fallback: bool = True):
+                  inner_tol: float | None = None, max_sweeps: int = 200, max_inner_iters: int = 50000,
+                  fsai: tuple | None = None, fallback: bool = True, mode: str = "reliable"):
     """Solve A_s x_s = b_s for every system s to |b_s - A_s x_s| / |b_s| <= tol (FP64 residual).
 
     Args:
-        A: the family (float32 values).
+        A: the family (float32 values); n must be a multiple of 4.
         B: (S, n) right-hand sides (any float dtype, promoted to float64).
         precond: "none", "jacobi" or "fsai" (then ``fsai=(FsaiPattern, g_values (S, g_nnz))``).
-        inner_tol: residual reduction asked of each FP32 inner PCG solve.
+        mode: "reliable" -- FP32 CG whose residual is replaced by the FP64 b - A x each time it has
+            dropped by inner_tol (default 0.1), the recurrence continues; "restart" -- classic
+            iterative refinement, every FP64 residual starts a new FP32 CG run (default inner_tol 1e-4).
+        max_sweeps: FP64 residual replacements per system; max_inner_iters: CG steps per system.
     Returns (X (S, n) float64, info) with per-system iterations, status and FP64 relative residuals.
     """
     _capi.require_cuda(A.values, B)
     lib = _capi.load()
     dev = A.values.device
-    S, n = A.num_systems, A.n
+    n = A.n
+    S = B.shape[0] if A.shared else A.num_systems
+    if A.shared and A.values.shape[0] != 1:
+        raise ValueError("a shared-values family holds exactly one value array")
     if B.shape != (S, n):
         raise ValueError(f"B must be ({S}, {n}), got {tuple(B.shape)}")
     vals = A.values.to(torch.float32).contiguous()
@@ -107,7 +160,8 @@ def solve_batched(A: BatchedCSR, B: torch.Tensor, precond: str = "jacobi", tol: 
     X = torch.empty((S, n), dtype=torch.float64, device=dev)
     pk = _PREC[precond]
     desc = _capi.BatchedCsr(n=n, nnz=A.indices.numel(), num_systems=S, indptr=A.indptr.data_ptr(),
-                            indices=A.indices.data_ptr(), values=vals.data_ptr())
+                            indices=A.indices.data_ptr(), values=vals.data_ptr(),
+                            shared_values=1 if A.shared else 0)
     keep = [vals, Bd]
     if pk == _capi.PREC_FSAI:
         if fsai is None:
@@ -119,9 +173,13 @@ def solve_batched(A: BatchedCSR, B: torch.Tensor, precond: str = "jacobi", tol: 
         desc.g_indptr, desc.g_indices = pat.g_indptr.data_ptr(), pat.g_indices.data_ptr()
         desc.gt_indptr, desc.gt_indices = pat.gt_indptr.data_ptr(), pat.gt_indices.data_ptr()
         desc.gt_perm, desc.g_values = pat.gt_perm.data_ptr(), gv.data_ptr()
+    if mode not in ("reliable", "restart"):
+        raise ValueError("mode must be 'reliable' or 'restart'")
+    if inner_tol is None:
+        inner_tol = 0.1 if mode == "reliable" else 1e-4
     prm = _capi.IrParams(tol=float(tol), inner_tol=float(inner_tol), max_sweeps=int(max_sweeps),
                          max_inner_iters=int(max_inner_iters), preconditioner=pk, fallback=1 if fallback else 0,
-                         spin_limit=0)
+                         spin_limit=0, mode=_capi.IR_RELIABLE if mode == "reliable" else _capi.IR_RESTART)
     iters = torch.zeros(S, dtype=torch.int32, device=dev)
     status = torch.zeros(S, dtype=torch.int32, device=dev)
     relres = torch.zeros(S, dtype=torch.float64, device=dev)
@@ -132,6 +190,6 @@ def solve_batched(A: BatchedCSR, B: torch.Tensor, precond: str = "jacobi", tol: 
     _capi.check(lib.colagb_cg_batched_csr_solve(C.byref(desc), Bd.data_ptr(), X.data_ptr(), C.byref(prm),
                                                 iters.data_ptr(), status.data_ptr(), relres.data_ptr(), ws.data_ptr(),
                                                 nbytes.value, C.byref(res), _capi.stream_ptr(dev)), "batched cg")
-    info = {"iterations": iters, "status": status, "relres": relres, "sweeps": int(res.sweeps),
-            "max_inner_iters_total": int(res.total_inner_iters)}
+    info = {"iterations": iters, "status": status, "relres": relres, "replacements": int(res.sweeps),
+            "sweeps": int(res.sweeps), "max_iterations": int(res.total_inner_iters)}
     return X, info

@@ -138,7 +138,9 @@ int colagb_cg_solve(const colagb_op* A, const colagb_op* P, const void* B, int64
  *  (a family of discretised operators: same mesh, different coefficients). *
  *  S systems, each n x n with nnz entries; values[s * nnz + j].            *
  *  Solved to a TRUE relative residual |b - A x| / |b| <= tol measured in   *
- *  FP64, by FP32 preconditioned CG inside FP64 iterative refinement.       *
+ *  FP64, by FP32 preconditioned CG with FP64 iterative refinement: the     *
+ *  solution accumulates in FP64 and the residual is replaced by the FP64   *
+ *  b - A x whenever the FP32 residual has dropped by inner_tol.            *
  *  The reference solves such systems one call at a time                    *
  *  (cola/linalg/inverse/inv.py:66-69 per system); here one persistent      *
  *  launch per refinement sweep advances all of them with per-system        *
@@ -161,16 +163,23 @@ typedef struct colagb_batched_csr {
   const int32_t* gt_indices;  /* g_nnz */
   const int32_t* gt_perm;     /* g_nnz: G^T entry e holds G value gt_perm[e] */
   const float* g_values;      /* num_systems * g_nnz */
+  int32_t shared_values;      /* 1: every system uses values[0 .. nnz) (one matrix, many right-hand sides) */
+  int32_t reserved;
 } colagb_batched_csr;
+
+#define COLAGB_IR_RELIABLE 0   /* FP64 residual replacement, the CG recurrence continues (default) */
+#define COLAGB_IR_RESTART 1    /* classic refinement: each FP64 residual starts a fresh inner CG */
 
 typedef struct colagb_ir_params {
   double tol;            /* target true relative residual (FP64), e.g. 1e-8 */
-  double inner_tol;      /* relative reduction asked of each inner FP32 PCG solve */
-  int32_t max_sweeps;    /* refinement sweeps */
-  int32_t max_inner_iters;
+  double inner_tol;      /* FP32 residual reduction between two FP64 residual replacements */
+  int32_t max_sweeps;    /* FP64 residual replacements per system */
+  int32_t max_inner_iters; /* CG iterations per system */
   int32_t preconditioner;/* COLAGB_PREC_* */
-  int32_t fallback;      /* 1: a system whose FSAI-PCG stalls restarts with Jacobi */
+  int32_t fallback;      /* 1: a system whose FSAI-PCG stalls continues with Jacobi */
   int64_t spin_limit;    /* grid-barrier spin bound (0 = default) */
+  int32_t mode;          /* COLAGB_IR_RELIABLE or COLAGB_IR_RESTART */
+  int32_t reserved;
 } colagb_ir_params;
 
 typedef struct colagb_ir_result {
@@ -189,6 +198,20 @@ int colagb_cg_batched_csr_solve(const colagb_batched_csr* A, const double* B, do
                                 const colagb_ir_params* params, int32_t* per_system_iters,
                                 int32_t* per_system_status, double* relres, void* workspace,
                                 size_t workspace_bytes, colagb_ir_result* result, void* stream);
+
+/* ------------------------------------------------------------------------ *
+ *  Batched independent dense SPD systems of uneven sizes (FP32 CG), one    *
+ *  persistent launch.  Each system behaves exactly like its own call of    *
+ *  cola.linalg.solve(PSD(Dense(A_s)), b_s, CG(tol, max_iters))             *
+ *  (cg.py:94-154), with its own stop test.  A_s is sizes[s] x sizes[s]     *
+ *  row-major at values + a_offsets[s]; b_s, x_s at B / X + v_offsets[s].   *
+ *  sizes, a_offsets, v_offsets are device arrays; num_systems <= 1024.     *
+ * ------------------------------------------------------------------------ */
+int colagb_cg_dense_batched_workspace_bytes(int64_t num_systems, int64_t total_rows, size_t* bytes);
+int colagb_cg_dense_batched_solve(int64_t num_systems, const int32_t* sizes, const int64_t* a_offsets,
+                                  const int64_t* v_offsets, int64_t total_rows, const float* values, const float* B,
+                                  float* X, double tol, int32_t max_iters, int32_t* per_system_iters,
+                                  int32_t* per_system_status, void* workspace, size_t workspace_bytes, void* stream);
 
 /* ======================================================================== *
  *  Lanczos with full reorthogonalisation                                   *
@@ -228,6 +251,46 @@ int colagb_basis_combine(const void* basis, int64_t n, int64_t bs, int32_t m, co
  * ======================================================================== */
 int colagb_tridiag_eig_f64(const double* a, const double* b, int64_t m, int64_t batch, double* evals,
                            double* first_row, double* evecs, int32_t* status, void* stream);
+
+/* ======================================================================== *
+ *  Learned FSAI preconditioner for 5-point operators on an m x m grid     *
+ *  (cells p = i*m + j; CSR columns sorted N = p-m, W = p-1, C, E, S).     *
+ *  A convolutional network reads the operator's coefficients and outputs  *
+ *  per-cell scalings o (S, 3, m, m) of the closed-form FSAI factor G on   *
+ *  A's lower pattern {N, W, C}; the CG preconditioner is P = G^T G.  It   *
+ *  plugs into the CG(P=...) hook of cola/linalg/inverse/cg.py:124, 150.   *
+ *  No counterpart in the reference beyond that hook (its only shipped     *
+ *  preconditioners are Nystrom, preconditioners.py:10-153).               *
+ *  Grid fields are (S, C, m, m) float32.                                   *
+ * ======================================================================== */
+/* CSR values (S, nnz) -> stencil (S, 5, m, m) [N, W, C, E, S]; *err_flag set if a column is off-stencil */
+int colagb_grid5_stencil(const int32_t* indptr, const int32_t* indices, const float* values, int64_t nnz, int64_t m,
+                         int64_t S, float* stencil, int32_t* err_flag, void* stream);
+/* network input features (S, 6, m, m) from the stencil */
+int colagb_fsai_features(const float* stencil, int64_t m, int64_t S, float* feats, void* stream);
+/* G stencil (S, 3, m, m) [N, W, C] from the stencil and the network output (NULL = closed-form FSAI) */
+int colagb_fsai_assemble(const float* stencil, const float* net_out, int64_t m, int64_t S, float* g_stencil, void* stream);
+/* G stencil -> CSR values (S, g_nnz) in the lower pattern order (for colagb_batched_csr.g_values) */
+int colagb_fsai_compact(const float* g_stencil, const int32_t* g_indptr, int64_t m, int64_t S, int64_t g_nnz,
+                        float* g_values, void* stream);
+/* 3x3 convolution (padding 1): out (B, cout, H, W) = bias + w * in (B, cin, H, W); cout in {16, 3} */
+int colagb_conv3x3_forward(const float* in, int64_t B, int32_t cin, int32_t cout, int64_t H, int64_t W,
+                           const float* weight, const float* bias, int32_t relu, float* out, void* stream);
+/* backward of one conv layer: grad_wb = [dW (cout*cin*9) | db (cout)], grad_in (may be NULL; cin in {16, 6}).
+ * act (may be NULL): the layer's forward output when it was ReLU'd (grad_out is masked by act > 0). */
+int colagb_conv3x3_backward_scratch_bytes(int32_t cin, int32_t cout, size_t* bytes);
+int colagb_conv3x3_backward(const float* grad_out, const float* act, const float* in, int64_t B, int32_t cin,
+                            int32_t cout, int64_t H, int64_t W, const float* weight, float* grad_in, float* grad_wb,
+                            float* scratch, size_t scratch_bytes, void* stream);
+/* training loss l_s = ||G^T G r - e||_A^2 / ||e||_A^2 for pairs A e = r (S, m*m); loss_terms (3, S) FP64 =
+ * [e^T r, v^T A v, v^T r] with v = G^T G r; grad_out (S, 3, m, m) = d(mean_s l_s)/d(net_out) (may be NULL).
+ * scratch: 3 * S * m * m floats. */
+int colagb_fsai_loss_grad(const float* stencil, const float* net_out, const float* g_stencil, const float* r,
+                          const float* e, int64_t m, int64_t S, float* grad_out, double* loss_terms, float* scratch,
+                          size_t scratch_bytes, void* stream);
+/* Adam update of count parameters (bias-corrected, step >= 1) */
+int colagb_adam_step(float* param, const float* grad, float* m1, float* m2, int64_t count, float lr, float beta1,
+                     float beta2, float eps, int32_t step, void* stream);
 
 #ifdef __cplusplus
 }

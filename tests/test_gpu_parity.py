@@ -332,11 +332,83 @@ def test_batched_ir_small_family(precond):
         assert rel(X[s], xs) < 1e-6
 
 
+@pytest.mark.parametrize("mode", ["reliable", "restart"])
+def test_batched_modes_converge_and_agree(mode):
+    from cola_gb300.workloads import diffusion_family_2d
+    fam, B, _, _ = diffusion_family_2d(range(20, 25), m=32, device=DEV)
+    X, info = cola.linalg.solve_batched(fam, B, precond="jacobi", tol=1e-8, mode=mode)
+    assert torch.all(info["status"] == 1) and float(info["relres"].max()) <= 1e-8
+    R = B - fam.matvec(X)
+    assert float((R.norm(dim=1) / B.norm(dim=1)).max()) <= 1.01e-8
+    # reliable updates keep the Krylov recurrence: close to the step count of an FP64 Jacobi-CG
+    n = fam.n
+    A = torch.sparse_csr_tensor(fam.indptr.long(), fam.indices.long(), fam.values[0].double(), (n, n)).to_dense()
+    A64 = A.cpu().numpy()
+    dinv = 1.0 / np.diag(A64)
+    xo, ko, info_o = oracle.cg_solve(oracle.dense_op(A64), B[0].cpu().numpy(), precond=lambda r: dinv * r, tol=5e-9,
+                                     max_iters=5000)
+    if mode == "reliable":
+        assert int(info["iterations"][0]) <= 1.15 * ko + 5, (int(info["iterations"][0]), ko)
+
+
+def test_batched_fsai_fallback_and_edge_inputs():
+    from cola_gb300.linalg.batched import FsaiPattern
+    from cola_gb300.workloads import diffusion_family_2d
+    fam, B, _, _ = diffusion_family_2d(range(30, 33), m=16, device=DEV)
+    pat = FsaiPattern(fam.indptr, fam.indices)
+    # a deliberately poor G (identity on the pattern's diagonal only): still SPD, judged by FP64 residuals
+    gv = torch.zeros((3, pat.g_nnz), device=DEV)
+    rows = torch.repeat_interleave(torch.arange(fam.n, device=DEV), (pat.g_indptr[1:] - pat.g_indptr[:-1]).long())
+    gv[:, rows == pat.g_indices.long()] = 1.0
+    X, info = cola.linalg.solve_batched(fam, B, precond="fsai", fsai=(pat, gv), tol=1e-8)
+    assert torch.all((info["status"] == 1) | (info["status"] == 5))
+    assert float(info["relres"].max()) <= 1e-8
+    with pytest.raises(ValueError):
+        cola.linalg.solve_batched(fam, B[:, :-1], precond="jacobi")
+    with pytest.raises(ValueError):
+        cola.linalg.solve_batched(fam, B, precond="fsai")
+
+
+def test_batched_shared_values_many_rhs():
+    """One 3-D 7-point operator, many right-hand sides as independent systems (values stored once)."""
+    from cola_gb300.linalg.batched import BatchedCSR
+    from cola_gb300.workloads import diffusion_3d
+    ip, ix, v = diffusion_3d(m=12, device=DEV)
+    fam = BatchedCSR(ip, ix, v[None, :], shared=True)
+    B = torch.randn(6, fam.n, device=DEV, dtype=torch.float64)
+    X, info = cola.linalg.solve_batched(fam, B, precond="jacobi", tol=1e-8)
+    assert torch.all(info["status"] == 1)
+    R = B - fam.matvec(X)
+    assert float((R.norm(dim=1) / B.norm(dim=1)).max()) <= 1.01e-8
+
+
+def test_dense_batched_uneven_matches_per_system_reference_loop():
+    """Uneven dense systems in one launch; each equals a separate reference CG call (oracle, float32)."""
+    from cola_gb300.linalg.batched import solve_dense_batched
+    rng = np.random.default_rng(5)
+    mats, rhs, np_mats = [], [], []
+    for n in (37, 64, 129, 250, 5, 1):
+        Q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+        lam = np.exp(rng.uniform(np.log(0.1), np.log(10.0), n))
+        A = ((Q * lam) @ Q.T).astype(np.float32)
+        b = rng.standard_normal(n).astype(np.float32)
+        np_mats.append((A, b))
+        mats.append(T(A))
+        rhs.append(T(b))
+    sols, iters, status = solve_dense_batched(mats, rhs, tol=1e-6, max_iters=500)
+    for (A, b), x, k in zip(np_mats, sols, iters.tolist()):
+        xo, ko, info = oracle.cg_solve(oracle.dense_op(A), b, tol=1e-6, max_iters=500)
+        assert abs(k - ko) <= 0.05 * ko + 2, (k, ko)
+        xs = np.linalg.solve(A.astype(np.float64), b.astype(np.float64))
+        assert rel(x, xs) < 1e-4
+    assert torch.all(status == 1)
+
+
 def test_batched_ir_matches_oracle_iteration_structure():
-    """The device IR loop and the oracle's IR restatement need comparable inner iterations."""
+    """The device restarted-refinement loop and the oracle's restatement need comparable inner iterations."""
     from cola_gb300.workloads import diffusion_family_2d
     fam, B, _, _ = diffusion_family_2d([11], m=20, device=DEV)
-    X, info = cola.linalg.solve_batched(fam, B, precond="none", tol=1e-8, inner_tol=1e-4)
+    X, info = cola.linalg.solve_batched(fam, B, precond="none", tol=1e-8, inner_tol=1e-4, mode="restart")
     n = fam.n
     A = torch.sparse_csr_tensor(fam.indptr.long(), fam.indices.long(), fam.values[0].double(), (n, n)).to_dense()
     A64 = A.cpu().numpy()
