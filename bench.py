@@ -175,7 +175,7 @@ def run_ours(args, world, rank, local):
             print(f"# learned preconditioner unavailable ({e}); timing jacobi", file=sys.stderr)
             method = "jacobi"
     prec = {"plain": "none", "jacobi": "jacobi", "learned": "fsai"}[method]
-    kw = dict(precond=prec, tol=1e-8, inner_tol=args.inner_tol, fsai=fsai, mode=args.mode)
+    kw = dict(precond=prec, tol=1e-8, inner_tol=args.inner_tol, fsai=fsai, mode=args.mode, schedule=args.schedule)
     st = torch.cuda.current_stream(dev)
 
     def step():
@@ -261,7 +261,7 @@ def run_ours(args, world, rank, local):
             p2 = {"plain": "none", "jacobi": "jacobi", "learned": "fsai"}[mth]
             if mth == "learned" and fsai is None:
                 continue
-            kw2 = dict(precond=p2, tol=1e-8, inner_tol=args.inner_tol, fsai=fsai, mode=args.mode)
+            kw2 = dict(precond=p2, tol=1e-8, inner_tol=args.inner_tol, fsai=fsai, mode=args.mode, schedule=args.schedule)
             solve_batched(fam, B, **kw2)
             torch.cuda.synchronize()
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -348,6 +348,7 @@ def main():
     ap.add_argument("--m", type=int, default=M)
     ap.add_argument("--inner-tol", type=float, default=None)
     ap.add_argument("--mode", default="reliable", choices=["reliable", "restart"])
+    ap.add_argument("--schedule", default="auto", choices=["auto", "grid", "cluster8", "cluster16"])
     ap.add_argument("--cpu-baseline", type=int, default=1)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-seconds", type=float, default=20.0)

@@ -67,7 +67,7 @@ class BatchedCsr(C.Structure):
 class IrParams(C.Structure):
     _fields_ = [("tol", C.c_double), ("inner_tol", C.c_double), ("max_sweeps", C.c_int32),
                 ("max_inner_iters", C.c_int32), ("preconditioner", C.c_int32), ("fallback", C.c_int32),
-                ("spin_limit", C.c_int64), ("mode", C.c_int32), ("reserved", C.c_int32)]
+                ("spin_limit", C.c_int64), ("mode", C.c_int32), ("schedule", C.c_int32)]
 
 
 class IrResult(C.Structure):

@@ -22,6 +22,7 @@
 // reduces its per-system sums once; rows are processed 4 per thread per step with all loads issued
 // before any store (memory-level parallelism for the HBM-bound streams).
 #include <string>
+#include <vector>
 
 #include "common.cuh"
 
@@ -630,6 +631,7 @@ struct BatchedWs {
   double *acc, *bnorm;
   unsigned int* bar;
   int* summary;
+  int* nrep;
 };
 
 static BatchedWs carve_batched(Bump& ws, const colagb_batched_csr& A, const colagb_ir_params& prm) {
@@ -649,7 +651,20 @@ static BatchedWs carve_batched(Bump& ws, const colagb_batched_csr& A, const cola
   w.bnorm = ws.take<double>(S);
   w.bar = ws.take<unsigned int>(8);
   w.summary = ws.take<int>(8);
+  w.nrep = ws.take<int>(S);
   return w;
+}
+
+int cluster_pcg_solve(const colagb_batched_csr* A, const double* B, double* X, const colagb_ir_params* prm,
+                      int32_t* iters, int32_t* status, double* relres, float* r, float* p, float* ap, float* d,
+                      float* z, float* t, float* dinv, int* nrep, int cluster_size, cudaStream_t st);
+
+// Cluster size for the cluster schedule: 0 = use the cooperative grid kernel.
+static int pick_cluster(const colagb_ir_params& prm, int64_t n) {
+  if (prm.schedule == COLAGB_SCHED_GRID) return 0;
+  if (prm.schedule == COLAGB_SCHED_CLUSTER8) return 8;
+  if (prm.schedule == COLAGB_SCHED_CLUSTER16) return 16;
+  return n >= 16 * 1024 ? 16 : 8;  // auto: wide clusters for large systems
 }
 
 static int validate_batched(const colagb_batched_csr* A, const colagb_ir_params* prm) {
@@ -705,8 +720,26 @@ extern "C" int colagb_cg_batched_csr_solve(const colagb_batched_csr* A, const do
   if (workspace == nullptr || ws.overflow())
     return fail(COLAGB_ERR_WORKSPACE, "batched CG: workspace too small (need " + std::to_string(ws.peak) + ")");
   cudaStream_t st = as_stream(stream);
+  const int csize = pick_cluster(*params, A->n);
   for (int64_t s0 = 0; s0 < S_all; s0 += kMaxBatch) {
     const int64_t S = (S_all - s0) < kMaxBatch ? (S_all - s0) : kMaxBatch;
+    if (csize > 0) {
+      colagb_batched_csr sub = *A;
+      sub.num_systems = S;
+      sub.values = A->values + (A->shared_values ? 0 : s0 * A->nnz);
+      sub.g_values = A->g_values ? A->g_values + s0 * A->g_nnz : nullptr;
+      COLAGB_TRY(cluster_pcg_solve(&sub, B + s0 * A->n, X + s0 * A->n, params,
+                                   per_system_iters ? per_system_iters + s0 : nullptr,
+                                   per_system_status ? per_system_status + s0 : nullptr, relres ? relres + s0 : nullptr,
+                                   w.r, w.p, w.ap, w.d, w.z, w.t, w.dinv, w.nrep, csize, st));
+      int mx[2] = {0, 0};
+      std::vector<int> hrep(S);
+      COLAGB_CUDA(cudaMemcpyAsync(hrep.data(), w.nrep, S * sizeof(int), cudaMemcpyDeviceToHost, st));
+      COLAGB_CUDA(cudaStreamSynchronize(st));
+      for (int64_t q = 0; q < S; ++q) mx[0] = hrep[q] > mx[0] ? hrep[q] : mx[0];
+      result->sweeps = mx[0] > result->sweeps ? mx[0] : result->sweeps;
+      continue;
+    }
     BatchedArgs a;
     a.n = A->n;
     a.nnz = A->nnz;

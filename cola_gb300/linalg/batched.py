@@ -129,11 +129,13 @@ class FsaiPattern:
 
 
 _PREC = {"none": _capi.PREC_NONE, None: _capi.PREC_NONE, "jacobi": _capi.PREC_JACOBI, "fsai": _capi.PREC_FSAI}
+_SCHED = {"auto": 0, "grid": 1, "cluster8": 2, "cluster16": 3}
 
 
 def solve_batched(A: BatchedCSR, B: torch.Tensor, precond: str = "jacobi", tol: float = 1e-8,
                   inner_tol: float | None = None, max_sweeps: int = 200, max_inner_iters: int = 50000,
-                  fsai: tuple | None = None, fallback: bool = True, mode: str = "reliable"):
+                  fsai: tuple | None = None, fallback: bool = True, mode: str = "reliable",
+                  schedule: str = "auto"):
     """Solve A_s x_s = b_s for every system s to |b_s - A_s x_s| / |b_s| <= tol (FP64 residual).
 
     Args:
@@ -144,6 +146,9 @@ def solve_batched(A: BatchedCSR, B: torch.Tensor, precond: str = "jacobi", tol: 
             dropped by inner_tol (default 0.1), the recurrence continues; "restart" -- classic
             iterative refinement, every FP64 residual starts a new FP32 CG run (default inner_tol 1e-4).
         max_sweeps: FP64 residual replacements per system; max_inner_iters: CG steps per system.
+        schedule: "auto" / "cluster8" / "cluster16" -- one thread-block cluster per system, launched
+            together and scheduled by the hardware; "grid" -- one cooperative grid that advances every
+            system together.
     Returns (X (S, n) float64, info) with per-system iterations, status and FP64 relative residuals.
     """
     _capi.require_cuda(A.values, B)
@@ -179,7 +184,8 @@ def solve_batched(A: BatchedCSR, B: torch.Tensor, precond: str = "jacobi", tol: 
         inner_tol = 0.1 if mode == "reliable" else 1e-4
     prm = _capi.IrParams(tol=float(tol), inner_tol=float(inner_tol), max_sweeps=int(max_sweeps),
                          max_inner_iters=int(max_inner_iters), preconditioner=pk, fallback=1 if fallback else 0,
-                         spin_limit=0, mode=_capi.IR_RELIABLE if mode == "reliable" else _capi.IR_RESTART)
+                         spin_limit=0, mode=_capi.IR_RELIABLE if mode == "reliable" else _capi.IR_RESTART,
+                         schedule=_SCHED[schedule])
     iters = torch.zeros(S, dtype=torch.int32, device=dev)
     status = torch.zeros(S, dtype=torch.int32, device=dev)
     relres = torch.zeros(S, dtype=torch.float64, device=dev)

@@ -179,8 +179,13 @@ typedef struct colagb_ir_params {
   int32_t fallback;      /* 1: a system whose FSAI-PCG stalls continues with Jacobi */
   int64_t spin_limit;    /* grid-barrier spin bound (0 = default) */
   int32_t mode;          /* COLAGB_IR_RELIABLE or COLAGB_IR_RESTART */
-  int32_t reserved;
+  int32_t schedule;      /* COLAGB_SCHED_* */
 } colagb_ir_params;
+
+#define COLAGB_SCHED_AUTO 0     /* cluster per system when the device supports it */
+#define COLAGB_SCHED_GRID 1     /* one cooperative grid advancing every system together */
+#define COLAGB_SCHED_CLUSTER8 2 /* one 8-CTA thread-block cluster per system */
+#define COLAGB_SCHED_CLUSTER16 3/* one 16-CTA cluster per system (non-portable cluster size) */
 
 typedef struct colagb_ir_result {
   int32_t sweeps;

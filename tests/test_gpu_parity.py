@@ -312,12 +312,13 @@ def test_tridiag_eigh(m):
 # ---------------------------------------------------------------------------------------------
 # batched systems on a shared pattern, FP64 iterative refinement
 
+@pytest.mark.parametrize("schedule", ["grid", "cluster8", "cluster16"])
 @pytest.mark.parametrize("precond", ["none", "jacobi"])
-def test_batched_ir_small_family(precond):
+def test_batched_ir_small_family(precond, schedule):
     from cola_gb300.workloads import diffusion_family_2d
     fam, B, _, _ = diffusion_family_2d(range(7), m=24, device=DEV)
     B[3].zero_()  # a zero right-hand side converges at once with x = 0
-    X, info = cola.linalg.solve_batched(fam, B, precond=precond, tol=1e-8, inner_tol=1e-4)
+    X, info = cola.linalg.solve_batched(fam, B, precond=precond, tol=1e-8, schedule=schedule)
     assert torch.all(info["status"] == 1), info["status"]
     assert float(info["relres"].max()) <= 1e-8
     R = B - fam.matvec(X)
