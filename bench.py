@@ -342,6 +342,8 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="c4", choices=["c1", "c2", "c3a", "c3b", "c4"],
+                    help="c4 (default): the headline family; the others print one measurement line each")
     ap.add_argument("--method", default="learned", choices=["learned", "jacobi", "plain"])
     ap.add_argument("--compare", default="plain,jacobi")
     ap.add_argument("--systems", type=int, default=SYSTEMS)
@@ -355,6 +357,12 @@ def main():
     ap.add_argument("--ref-systems", type=int, default=4)
     args = ap.parse_args()
     world, rank, local = dist_setup()
+    if args.config != "c4":
+        from cola_gb300 import _capi, configs
+        _capi.load()
+        if rank == 0:
+            print(json.dumps(configs.RUNNERS[args.config]()))
+        return
     if args.impl == "reference":
         out = run_reference(args, world, rank)
     else:

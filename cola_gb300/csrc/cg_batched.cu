@@ -516,7 +516,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_batched_ir(const __grid_constan
     if (threadIdx.x == 0) {
       for (int j = 0; j < nact; ++j) {
         const int s = m.act()[j];
-        const float rn = (float)sqrt(__ldcg(acc[2] + s));
+        const float rn = (float)sqrt(__ldcg(acc[1] + s));  // FUpdate: acc[1] = |r|^2, acc[2] = <r, M r>
         m.rn(s) = rn;
         m.it(s) += 1;
         int f = m.flags(s) & ~(F_REPLACE | F_RESTART);
@@ -589,7 +589,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_batched_ir(const __grid_constan
     for (int j = threadIdx.x; j < nact; j += blockDim.x) {
       const int s = m.act()[j];
       const double g1 = zphase ? __ldcg(acc[5] + s)
-                               : ((m.flags(s) & F_REPLACE) ? __ldcg(acc[4] + s) : __ldcg(acc[1] + s));
+                               : ((m.flags(s) & F_REPLACE) ? __ldcg(acc[4] + s) : __ldcg(acc[2] + s));
       m.beta(s) = (m.flags(s) & F_RESTART) || m.gamma(s) == 0.0 ? 0.f : (float)(g1 / m.gamma(s));
       m.gamma(s) = g1;
     }

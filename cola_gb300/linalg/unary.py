@@ -5,6 +5,7 @@ cola/linalg/tbd/slq.py:37-75).
 """
 from __future__ import annotations
 
+import math
 from functools import reduce
 from typing import Callable
 
@@ -97,6 +98,27 @@ def log(A: O.LinearOperator, alg: Algorithm = Auto()):
     if isinstance(A, O.Kronecker):
         raise NotImplementedError("log of a Kronecker product: use logdet, which factorises it")
     return apply_unary(torch.log, A, alg)
+
+
+def exp(A: O.LinearOperator, alg: Algorithm = Auto()):
+    """Matrix exponential of a self-adjoint operator (unary.py:228-246)."""
+    return apply_unary(torch.exp, A, alg)
+
+
+def sqrt(A: O.LinearOperator, alg: Algorithm = Auto()):
+    """Matrix square root of a PSD operator (unary.py:265-280); Diagonal / ScalarMul / Identity exactly."""
+    if isinstance(A, O.Diagonal):
+        return O.Diagonal(torch.sqrt(A.diag))
+    if isinstance(A, O.ScalarMul):
+        return O.ScalarMul(math.sqrt(A.c), A.shape, A.dtype, A.device)
+    if isinstance(A, O.Identity):
+        return A
+    return apply_unary(torch.sqrt, A, alg)
+
+
+def pow(A: O.LinearOperator, alpha: float, alg: Algorithm = Auto()):
+    """A ** alpha for a PSD operator (unary.py:283-334)."""
+    return apply_unary(lambda x: x ** alpha, A, alg)
 
 
 # ---------------------------------------------------------------------------------------------

@@ -103,6 +103,38 @@ def diffusion_family_2d(seeds, m: int = 512, device="cuda", ell_range=(0.05, 0.2
     return BatchedCSR(indptr, indices, torch.stack(vals)), torch.stack(Bs), torch.stack(coeffs), params
 
 
+def rbf_systems(num: int = 256, seed: int = 3, n_range=(500, 8000), device="cuda"):
+    """Dense RBF-kernel systems K + s^2 I: n_i uniform in n_range, points uniform in [0,1]^3, lengthscale
+    uniform in [0.05, 0.5], s^2 log-uniform in [1e-3, 1e-1], FP32, one N(0,1) right-hand side each."""
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    mats, rhs, meta = [], [], []
+    for _ in range(num):
+        n = int(torch.randint(n_range[0], n_range[1] + 1, (1,), generator=g))
+        ell = 0.05 + 0.45 * float(torch.rand(1, generator=g))
+        s2 = math.exp(math.log(1e-3) + (math.log(1e-1) - math.log(1e-3)) * float(torch.rand(1, generator=g)))
+        pts = torch.rand(n, 3, generator=g, dtype=torch.float64).to(device)
+        d2 = torch.cdist(pts, pts).pow(2)
+        K = torch.exp(-d2 / (2 * ell * ell))
+        K.diagonal().add_(s2)
+        mats.append(K.float())
+        rhs.append(torch.randn(n, generator=g).to(device))
+        meta.append((n, ell, s2))
+    return mats, rhs, meta
+
+
+def rbf_grid_kernel(m: int, ell: float, dtype=torch.float64, device="cuda"):
+    """m x m RBF kernel on a uniform 1-D grid of [0, 1]."""
+    x = torch.linspace(0, 1, m, dtype=dtype, device=device)
+    return torch.exp(-((x[:, None] - x[None, :]) ** 2) / (2 * ell * ell))
+
+
+def kron_rbf(seed: int = 4, m: int = 64, factors: int = 3, device="cuda", dtype=torch.float32):
+    """Factors of Kronecker(K1, K2, K3): RBF kernels on 1-D grids, lengthscales uniform in [0.05, 0.3]."""
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    ells = [0.05 + 0.25 * float(torch.rand(1, generator=g)) for _ in range(factors)]
+    return [rbf_grid_kernel(m, ell, device=device).to(dtype) for ell in ells], ells
+
+
 def diffusion_3d(m: int = 128, seed: int = 1, shift: float = 1e-3, device="cuda"):
     """7-point variable-coefficient diffusion on an m^3 grid, cell coefficients exp(g), g ~ N(0,1)
     i.i.d. per cell, harmonic-mean faces, Dirichlet walls, plus shift * I.  Returns CSR arrays."""

@@ -283,6 +283,23 @@ def test_logdet_kron_slq_golden(golden):
     assert abs(float(ld) - float(g["logdet"])) < 1e-6
 
 
+@pytest.mark.parametrize("name", ["sqrt", "exp", "pow"])
+def test_unary_family_against_eigh(name):
+    """f(A) v by Lanczos quadrature (full Krylov space: exact up to rounding) vs a dense FP64 eigh."""
+    rng = np.random.default_rng(7)
+    Q, _ = np.linalg.qr(rng.standard_normal((40, 40)))
+    lam = np.exp(rng.uniform(np.log(0.2), np.log(3.0), 40))
+    A = (Q * lam) @ Q.T
+    op = cola.PSD(cola.ops.Dense(T(A)))
+    f = {"sqrt": (lambda: cola.linalg.sqrt(op, Lanczos(max_iters=40, tol=1e-13)), np.sqrt),
+         "exp": (lambda: cola.linalg.exp(op, Lanczos(max_iters=40, tol=1e-13)), np.exp),
+         "pow": (lambda: cola.linalg.pow(op, 0.3, Lanczos(max_iters=40, tol=1e-13)), lambda x: x ** 0.3)}[name]
+    F = f[0]()
+    V = rng.standard_normal((40, 3))
+    ref = (Q * f[1](lam)) @ Q.T @ V
+    assert rel(F @ T(V), ref) < 1e-8
+
+
 def test_slq_tbd_golden(golden):
     g = golden("slq_tbd")
     est = cola.linalg.stochastic_lanczos_quad(cola.ops.Dense(T(g["A"])), torch.log, max_iters=30, tol=1e-7,
