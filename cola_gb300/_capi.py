@@ -93,6 +93,8 @@ SIGNATURES = {
     "colagb_cg_workspace_bytes": (C.c_int, [_vp, _vp, _i64, _P(_sz)]),
     "colagb_cg_solve": (C.c_int, [_vp, _vp, _vp, _i64, _vp, _i64, _i64, _P(CgParams), _vp, _vp, _sz,
                                   _P(CgResult), _vp]),
+    "colagb_cg_solve_noalloc": (C.c_int, [_vp, _vp, _vp, _i64, _vp, _i64, _i64, _P(CgParams), _vp, _P(CgResult),
+                                          _vp]),
     "colagb_cg_batched_csr_workspace_bytes": (C.c_int, [_P(BatchedCsr), _P(IrParams), _P(_sz)]),
     "colagb_cg_batched_csr_solve": (C.c_int, [_P(BatchedCsr), _vp, _vp, _P(IrParams), _vp, _vp, _vp, _vp, _sz,
                                               _P(IrResult), _vp]),

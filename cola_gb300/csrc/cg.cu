@@ -19,6 +19,7 @@
 //     syncs twice per step, torch_tqdm.py:42 and cg.py:136).
 // Column sums are reduced in a fixed order so every CTA derives bit-identical alpha / beta.
 #include <cmath>
+#include <mutex>
 #include <type_traits>
 #include <string>
 #include <vector>
@@ -810,4 +811,48 @@ extern "C" int colagb_cg_solve(const colagb_op* A, const colagb_op* P, const voi
   if (A->compute_dtype == COLAGB_F64)
     return cg_solve_t<double>(A, P, B, ldb, X, ldx, k, *params, residual_history, workspace, workspace_bytes, result, st);
   return cg_solve_t<float>(A, P, B, ldb, X, ldx, k, *params, residual_history, workspace, workspace_bytes, result, st);
+}
+
+// ---------------------------------------------------------------------------------------------
+// CG without any allocation, for callers that cannot allocate device memory themselves (for example
+// a host runtime that owns a fixed memory pool, or a driver calling from a context where
+// cudaMalloc is not allowed).  The solver's scratch lives in one file-scope device array of
+// kNoAllocScratchBytes that every GPU loading this library holds until the process exits.
+namespace colagb {
+constexpr size_t kNoAllocScratchBytes = (size_t)8 << 20;  // 8 MiB
+static __device__ __align__(256) unsigned char g_cg_noalloc_scratch[kNoAllocScratchBytes];
+
+// Device address of the scratch array on the current device, looked up once per device.
+static int noalloc_scratch(void** out) {
+  static std::mutex mu;
+  static std::vector<void*> addr;
+  int dev = 0;
+  COLAGB_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  if ((int)addr.size() <= dev) addr.resize(dev + 1, nullptr);
+  if (addr[dev] == nullptr) {
+    void* p = nullptr;
+    COLAGB_CUDA(cudaGetSymbolAddress(&p, g_cg_noalloc_scratch));
+    addr[dev] = p;
+  }
+  *out = addr[dev];
+  return COLAGB_OK;
+}
+}  // namespace colagb
+
+extern "C" int colagb_cg_solve_noalloc(const colagb_op* A, const colagb_op* P, const void* B, int64_t ldb, void* X,
+                                       int64_t ldx, int64_t k, const colagb_cg_params* params, void* residual_history,
+                                       colagb_cg_result* result, void* stream) {
+  if (!A || !params || !result) return fail(COLAGB_ERR_INVALID, "colagb_cg_solve_noalloc: null argument");
+  size_t need = 0;
+  COLAGB_TRY(colagb_cg_workspace_bytes(A, P, k, &need));
+  if (need > kNoAllocScratchBytes)
+    return fail(COLAGB_ERR_INVALID, "colagb_cg_solve_noalloc: this problem needs " + std::to_string(need) +
+                                        " bytes of scratch, more than the fixed " +
+                                        std::to_string(kNoAllocScratchBytes) + " bytes; use colagb_cg_solve");
+  void* scratch = nullptr;
+  COLAGB_TRY(noalloc_scratch(&scratch));
+  // every buffer the solver reads is written or cleared by the solver itself before use
+  return colagb_cg_solve(A, P, B, ldb, X, ldx, k, params, residual_history, scratch, kNoAllocScratchBytes, result,
+                         stream);
 }

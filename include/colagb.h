@@ -133,6 +133,19 @@ int colagb_cg_solve(const colagb_op* A, const colagb_op* P, const void* B, int64
                     int64_t k, const colagb_cg_params* params, void* residual_history,
                     void* workspace, size_t workspace_bytes, colagb_cg_result* result, void* stream);
 
+/* colagb_cg_solve for callers that cannot allocate device memory -- for example a host runtime
+ * that hands out only its own fixed pool, or code running where cudaMalloc is not allowed.  It takes
+ * no workspace: its scratch is one fixed 8 MiB device array inside this library (every GPU that loads
+ * the library keeps it until the process exits).  Problems whose colagb_cg_workspace_bytes exceeds
+ * 8 MiB (roughly n*k above 600,000 in FP32 or 300,000 in FP64) are rejected with COLAGB_ERR_INVALID.
+ * The first call on a device looks up the array's device address; make that first call before any
+ * stream capture.  All calls share the array: calls whose GPU work overlaps (other streams, other
+ * threads) race and corrupt each other's results.  This entry point has no counterpart in the
+ * reference; otherwise it behaves exactly like colagb_cg_solve. */
+int colagb_cg_solve_noalloc(const colagb_op* A, const colagb_op* P, const void* B, int64_t ldb, void* X,
+                            int64_t ldx, int64_t k, const colagb_cg_params* params, void* residual_history,
+                            colagb_cg_result* result, void* stream);
+
 /* ------------------------------------------------------------------------ *
  *  Batched independent SPD systems sharing one CSR sparsity pattern        *
  *  (a family of discretised operators: same mesh, different coefficients). *
