@@ -137,7 +137,7 @@ def bytes_per_system_iter(n, nnz, method):
     b = nnz * 4 + 6 * n * 4
     if method == "jacobi":
         b += n * 4
-    elif method == "learned":
+    elif method in ("learned", "fsai"):
         g_nnz = (nnz + n) // 2
         b += 2 * g_nnz * 4 + 2 * n * 4
     return b
@@ -149,10 +149,16 @@ def bytes_per_replacement(n, nnz):
 
 
 def make_preconditioner(method, fam, coeff, dev):
-    if method != "learned":
-        return None
+    """(pattern, G values) of the FSAI factor: trained network ("learned") or closed form ("fsai")."""
     from cola_gb300.precond import learned_fsai
-    return learned_fsai.preconditioner_for(fam, coeff)
+    if method == "learned":
+        return learned_fsai.preconditioner_for(fam, coeff)
+    if method == "fsai":
+        return learned_fsai.g_values(fam, None)
+    return None
+
+
+PRECOND = {"plain": "none", "jacobi": "jacobi", "learned": "fsai", "fsai": "fsai"}
 
 
 def run_ours(args, world, rank, local):
@@ -168,13 +174,13 @@ def run_ours(args, world, rank, local):
     n, nnz = fam.n, fam.indices.numel()
     method = args.method
     fsai = None
-    if method == "learned":
+    if method in ("learned", "fsai"):
         try:
             fsai = make_preconditioner(method, fam, coeff, dev)
-        except Exception as e:  # learned weights missing: report and fall back to Jacobi
+        except FileNotFoundError as e:  # trained weights missing: say so and time Jacobi-PCG
             print(f"# learned preconditioner unavailable ({e}); timing jacobi", file=sys.stderr)
             method = "jacobi"
-    prec = {"plain": "none", "jacobi": "jacobi", "learned": "fsai"}[method]
+    prec = PRECOND[method]
     kw = dict(precond=prec, tol=1e-8, inner_tol=args.inner_tol, fsai=fsai, mode=args.mode, schedule=args.schedule)
     st = torch.cuda.current_stream(dev)
 
@@ -258,10 +264,14 @@ def run_ours(args, world, rank, local):
         for mth in args.compare.split(","):
             if mth == method:
                 continue
-            p2 = {"plain": "none", "jacobi": "jacobi", "learned": "fsai"}[mth]
-            if mth == "learned" and fsai is None:
-                continue
-            kw2 = dict(precond=p2, tol=1e-8, inner_tol=args.inner_tol, fsai=fsai, mode=args.mode, schedule=args.schedule)
+            fsai2 = None
+            if mth in ("learned", "fsai"):
+                try:
+                    fsai2 = make_preconditioner(mth, fam, coeff, dev)
+                except FileNotFoundError:
+                    continue
+            kw2 = dict(precond=PRECOND[mth], tol=1e-8, inner_tol=args.inner_tol, fsai=fsai2, mode=args.mode,
+                       schedule=args.schedule)
             solve_batched(fam, B, **kw2)
             torch.cuda.synchronize()
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -342,15 +352,15 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c4", choices=["c1", "c2", "c3a", "c3b", "c4"],
+    ap.add_argument("--config", default="c4", choices=["c1", "c2", "c3a", "c3b", "c4", "c5"],
                     help="c4 (default): the headline family; the others print one measurement line each")
-    ap.add_argument("--method", default="learned", choices=["learned", "jacobi", "plain"])
+    ap.add_argument("--method", default="learned", choices=["learned", "fsai", "jacobi", "plain"])
     ap.add_argument("--compare", default="plain,jacobi")
     ap.add_argument("--systems", type=int, default=SYSTEMS)
     ap.add_argument("--m", type=int, default=M)
     ap.add_argument("--inner-tol", type=float, default=None)
     ap.add_argument("--mode", default="reliable", choices=["reliable", "restart"])
-    ap.add_argument("--schedule", default="auto", choices=["auto", "grid", "cluster8", "cluster16"])
+    ap.add_argument("--schedule", default="auto", choices=["auto", "grid", "cluster8", "cluster16", "onchip"])
     ap.add_argument("--cpu-baseline", type=int, default=1)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-seconds", type=float, default=20.0)

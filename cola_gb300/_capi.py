@@ -98,6 +98,7 @@ SIGNATURES = {
     "colagb_cg_batched_csr_workspace_bytes": (C.c_int, [_P(BatchedCsr), _P(IrParams), _P(_sz)]),
     "colagb_cg_batched_csr_solve": (C.c_int, [_P(BatchedCsr), _vp, _vp, _P(IrParams), _vp, _vp, _vp, _vp, _sz,
                                               _P(IrResult), _vp]),
+    "colagb_onchip_schedule_info": (C.c_int, [_i64, _i32, _vp]),
     "colagb_cg_dense_batched_workspace_bytes": (C.c_int, [_i64, _i64, _P(_sz)]),
     "colagb_cg_dense_batched_solve": (C.c_int, [_i64, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _d, _i32, _vp, _vp, _vp,
                                                 _sz, _vp]),

@@ -166,10 +166,12 @@ __device__ __forceinline__ void sweep(const int* act, int nact, int64_t n, const
   if (NA > 0 && cur >= 0) flush<A, NA>(cur, v, acc, red);
 }
 
-// CSR row dot with up to kRowUnroll entries unrolled (predicated), the rest in a loop.
+// CSR row dot with up to kRowUnroll entries unrolled (predicated), the rest in a loop.  `x` is
+// rewritten by other CTAs during the kernel, so it must not be declared __restrict__ (that would let
+// the compiler read it through the non-coherent read-only cache and see stale values).
 template <class T, class V>
 __device__ __forceinline__ T csr_dot(const int32_t* __restrict__ indptr, const int32_t* __restrict__ indices,
-                                     const float* __restrict__ vals, const V* __restrict__ x, int64_t i) {
+                                     const float* __restrict__ vals, const V* x, int64_t i) {
   const int32_t b = __ldg(indptr + i), e = __ldg(indptr + i + 1);
   T acc = T(0);
 #pragma unroll
@@ -350,8 +352,10 @@ struct FPUpdate {  // p = z + beta p  (z stored, or M r recomputed)   (4 rows)
   }
   __device__ __forceinline__ void finish(int s, int64_t i, const L& l, float*) const {
     const float b = m->beta(s);
+    // beta = 0 (first direction, restarts): p = z without touching the old p, which is
+    // uninitialised workspace before the first step (0 * NaN would be NaN)
     *reinterpret_cast<float4*>(a->p + (int64_t)s * a->n + i) =
-        make_float4(l.z.x + b * l.p.x, l.z.y + b * l.p.y, l.z.z + b * l.p.z, l.z.w + b * l.p.w);
+        b == 0.f ? l.z : make_float4(l.z.x + b * l.p.x, l.z.y + b * l.p.y, l.z.z + b * l.p.z, l.z.w + b * l.p.w);
   }
 };
 
@@ -632,7 +636,14 @@ struct BatchedWs {
   unsigned int* bar;
   int* summary;
   int* nrep;
+  float* onchip;
+  size_t onchip_bytes;
 };
+
+size_t onchip_workspace_floats(int64_t n, bool fsai);
+int onchip_pcg_solve(const colagb_batched_csr* A, const double* B, double* X, const colagb_ir_params* prm,
+                     int32_t* iters, int32_t* status, double* relres, int* nrep, void* ws, size_t ws_bytes,
+                     bool* used, cudaStream_t st);
 
 static BatchedWs carve_batched(Bump& ws, const colagb_batched_csr& A, const colagb_ir_params& prm) {
   const int64_t S = A.num_systems < kMaxBatch ? A.num_systems : kMaxBatch;
@@ -652,6 +663,10 @@ static BatchedWs carve_batched(Bump& ws, const colagb_batched_csr& A, const cola
   w.bar = ws.take<unsigned int>(8);
   w.summary = ws.take<int>(8);
   w.nrep = ws.take<int>(S);
+  const bool onchip = prm.schedule == COLAGB_SCHED_AUTO || prm.schedule == COLAGB_SCHED_ONCHIP;
+  const size_t nf = onchip ? onchip_workspace_floats(A.n, fsai) : 0;
+  w.onchip = nf ? ws.take<float>(nf) : nullptr;
+  w.onchip_bytes = nf * sizeof(float);
   return w;
 }
 
@@ -661,7 +676,7 @@ int cluster_pcg_solve(const colagb_batched_csr* A, const double* B, double* X, c
 
 // Cluster size for the cluster schedule: 0 = use the cooperative grid kernel.
 static int pick_cluster(const colagb_ir_params& prm, int64_t n) {
-  if (prm.schedule == COLAGB_SCHED_GRID) return 0;
+  if (prm.schedule == COLAGB_SCHED_GRID || prm.schedule == COLAGB_SCHED_ONCHIP) return 0;
   if (prm.schedule == COLAGB_SCHED_CLUSTER8) return 8;
   if (prm.schedule == COLAGB_SCHED_CLUSTER16) return 16;
   return n >= 16 * 1024 ? 16 : 8;  // auto: wide clusters for large systems
@@ -674,6 +689,8 @@ static int validate_batched(const colagb_batched_csr* A, const colagb_ir_params*
     return fail(COLAGB_ERR_INVALID, "batched CG: missing CSR arrays");
   if (prm->preconditioner < 0 || prm->preconditioner > 2)
     return fail(COLAGB_ERR_INVALID, "batched CG: unknown preconditioner");
+  if (prm->schedule < COLAGB_SCHED_AUTO || prm->schedule > COLAGB_SCHED_ONCHIP)
+    return fail(COLAGB_ERR_INVALID, "batched CG: unknown schedule");
   if (prm->mode != COLAGB_IR_RELIABLE && prm->mode != COLAGB_IR_RESTART)
     return fail(COLAGB_ERR_INVALID, "batched CG: unknown refinement mode");
   if (prm->preconditioner == COLAGB_PREC_FSAI &&
@@ -721,17 +738,31 @@ extern "C" int colagb_cg_batched_csr_solve(const colagb_batched_csr* A, const do
     return fail(COLAGB_ERR_WORKSPACE, "batched CG: workspace too small (need " + std::to_string(ws.peak) + ")");
   cudaStream_t st = as_stream(stream);
   const int csize = pick_cluster(*params, A->n);
+  const bool try_onchip = params->schedule == COLAGB_SCHED_AUTO || params->schedule == COLAGB_SCHED_ONCHIP;
   for (int64_t s0 = 0; s0 < S_all; s0 += kMaxBatch) {
     const int64_t S = (S_all - s0) < kMaxBatch ? (S_all - s0) : kMaxBatch;
-    if (csize > 0) {
-      colagb_batched_csr sub = *A;
-      sub.num_systems = S;
-      sub.values = A->values + (A->shared_values ? 0 : s0 * A->nnz);
-      sub.g_values = A->g_values ? A->g_values + s0 * A->g_nnz : nullptr;
-      COLAGB_TRY(cluster_pcg_solve(&sub, B + s0 * A->n, X + s0 * A->n, params,
-                                   per_system_iters ? per_system_iters + s0 : nullptr,
-                                   per_system_status ? per_system_status + s0 : nullptr, relres ? relres + s0 : nullptr,
-                                   w.r, w.p, w.ap, w.d, w.z, w.t, w.dinv, w.nrep, csize, st));
+    colagb_batched_csr sub = *A;
+    sub.num_systems = S;
+    sub.values = A->values + (A->shared_values ? 0 : s0 * A->nnz);
+    sub.g_values = A->g_values ? A->g_values + s0 * A->g_nnz : nullptr;
+    bool used = false;
+    if (try_onchip)
+      COLAGB_TRY(onchip_pcg_solve(&sub, B + s0 * A->n, X + s0 * A->n, params,
+                                  per_system_iters ? per_system_iters + s0 : nullptr,
+                                  per_system_status ? per_system_status + s0 : nullptr, relres ? relres + s0 : nullptr,
+                                  w.nrep, w.onchip, w.onchip_bytes, &used, st));
+    if (!used && params->schedule == COLAGB_SCHED_ONCHIP)
+      return fail(COLAGB_ERR_UNSUPPORTED,
+                  "batched CG: the on-chip schedule needs a pattern of at most 9 diagonals (FSAI: G lower "
+                  "triangular, at most 5 diagonals) and p, r, d of one system within the shared memory of a "
+                  "16-CTA cluster");
+    if (used || csize > 0) {
+      if (!used)
+        COLAGB_TRY(cluster_pcg_solve(&sub, B + s0 * A->n, X + s0 * A->n, params,
+                                     per_system_iters ? per_system_iters + s0 : nullptr,
+                                     per_system_status ? per_system_status + s0 : nullptr,
+                                     relres ? relres + s0 : nullptr, w.r, w.p, w.ap, w.d, w.z, w.t, w.dinv, w.nrep,
+                                     csize, st));
       int mx[2] = {0, 0};
       std::vector<int> hrep(S);
       COLAGB_CUDA(cudaMemcpyAsync(hrep.data(), w.nrep, S * sizeof(int), cudaMemcpyDeviceToHost, st));

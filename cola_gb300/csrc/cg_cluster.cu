@@ -15,6 +15,7 @@
 
 #include <string>
 
+#include "cluster.cuh"
 #include "common.cuh"
 
 namespace cg = cooperative_groups;
@@ -46,33 +47,10 @@ struct ClusterArgs {
   int max_sweeps, max_inner, prec_kind, fallback, mode;
 };
 
-// Cluster-wide sums of NQ values: CTA partials go to this CTA's `slot`, a cluster barrier publishes
-// them, and every CTA adds all ranks' slots in rank order.  `slot` alternates between two buffers
-// so that a CTA can only overwrite a buffer after the next barrier, by which time every reader of
-// the previous round has finished.
-template <int NQ, int CL>
-__device__ __forceinline__ void cluster_sum(cg::cluster_group& cl, double (&v)[NQ], double* slot, double* red,
-                                            double* bcast) {
-#pragma unroll
-  for (int k = 0; k < NQ; ++k) {
-    const double x = block_sum(v[k], red);
-    if (threadIdx.x == 0) slot[k] = x;
-  }
-  cl.sync();
-  if (threadIdx.x < NQ) {
-    double s = 0.0;
-#pragma unroll
-    for (int r = 0; r < CL; ++r) s += *cl.map_shared_rank(slot + threadIdx.x, r);
-    bcast[threadIdx.x] = s;
-  }
-  __syncthreads();
-#pragma unroll
-  for (int k = 0; k < NQ; ++k) v[k] = bcast[k];
-  __syncthreads();
-}
-
-__device__ __forceinline__ float row_dot_f(const ClusterArgs& a, const float* __restrict__ vals,
-                                           const float* __restrict__ x, int64_t i) {
+// `x` (the search direction) is rewritten by the other CTAs of the cluster during the kernel: no
+// __restrict__, so it is never read through the non-coherent read-only cache.
+__device__ __forceinline__ float row_dot_f(const ClusterArgs& a, const float* __restrict__ vals, const float* x,
+                                           int64_t i) {
   const int32_t b = __ldg(a.indptr + i), e = __ldg(a.indptr + i + 1);
   float acc = 0.f;
 #pragma unroll
@@ -100,13 +78,14 @@ __global__ void __launch_bounds__(kCT, 1) k_cluster_pcg(const __grid_constant__ 
   const int64_t i1 = (rank + 1) * rows < n ? (rank + 1) * rows : n;
   const int64_t so = s * n;
   const float* __restrict__ vals = a.vals + s * a.vstride;
-  float* __restrict__ r = a.r + so;
-  float* __restrict__ p = a.p + so;
-  float* __restrict__ ap = a.ap + so;
-  float* __restrict__ d = a.d + so;
-  float* __restrict__ z = a.z + so;
-  float* __restrict__ dinv = a.dinv ? a.dinv + so : nullptr;
-  double* __restrict__ X = a.X + so;
+  // vectors written by several CTAs of the cluster: plain pointers (see row_dot_f)
+  float* r = a.r + so;
+  float* p = a.p + so;
+  float* ap = a.ap + so;
+  float* d = a.d + so;
+  float* z = a.z + so;
+  float* dinv = a.dinv ? a.dinv + so : nullptr;
+  double* X = a.X + so;
   const double* __restrict__ B = a.B + so;
   const float* g = a.g_vals ? a.g_vals + s * a.g_nnz : nullptr;
   float* t = a.t ? a.t + so : nullptr;

@@ -1,0 +1,633 @@
+// Batched shared-pattern PCG with the Krylov vectors held on chip: one thread-block cluster per
+// system, the system's p, r and FP32 solution correction d spread over the shared memory of the
+// cluster's CTAs, the matrix streamed from diagonal storage.
+//
+// Same algorithm and stop rule as the other batched schedules (cg_batched.cu, cg_cluster.cu: FP32
+// PCG, FP64 solution, FP64 residual replacement, Jacobi / FSAI, the FP64 true residual as the only
+// convergence test and as the judge of a learned FSAI factor).  What changes is where data lives:
+//   * a pattern made of a few constant-offset diagonals (any stencil on a structured grid) is
+//     stored as diagonals: values[k][i] = A(i, i + off[k]), one coalesced stream per diagonal, no
+//     column indices, no row pointers;
+//   * CTA `rank` of the cluster owns rows [rank * R, rank * R + R); its p and r (plus a halo of H
+//     rows on each side) and d live in its shared memory for the whole solve, so the only memory
+//     traffic per iteration is the matrix (and the FSAI operator M = G^T G, also diagonal);
+//   * halos are copied from the neighbouring CTAs' shared memory (distributed shared memory) after
+//     the cluster barrier that follows their update;
+//   * per-row values that stay with the same thread between phases (A p, then z) stay in registers;
+//   * clusters are persistent: each takes the next system from an atomic counter, converts that
+//     system's CSR values into its own diagonal slot, solves it and moves on.
+// Results are per system and independent of the scheduling order.
+#include <cooperative_groups.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "cluster.cuh"
+#include "common.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace colagb {
+
+constexpr int kOT = 512;         // threads per CTA
+constexpr int kMaxDiagA = 9;     // diagonals of A
+constexpr int kMaxDiagG = 5;     // diagonals of the FSAI factor G
+constexpr int kMaxDiagM = 17;    // diagonals of M = G^T G
+constexpr int kMaxPairs = 32;    // (G diagonal, G diagonal) products that make up M
+constexpr size_t kOnchipSmemMax = 227 * 1024 - 1024;
+
+struct OnchipArgs {
+  int64_t n, S, np;  // rows, systems, rows padded to the cluster (CL * R)
+  int R, H;          // rows per CTA, halo rows on each side
+  int nd, center;    // diagonals of A and the index of offset 0 (-1: no main diagonal)
+  int off[kMaxDiagA];
+  int ng, nm;
+  int goff[kMaxDiagG];
+  int moff[kMaxDiagM];
+  int pstart[kMaxDiagM + 1];
+  int pa[kMaxPairs], pb[kMaxPairs];  // M(i, i + moff[m]) = sum G(k, i) G(k, i + moff[m]), k = i - goff[pa]
+  const int32_t* indptr;
+  const int32_t* indices;
+  const float* vals;
+  int64_t vstride;
+  const int32_t* g_indptr;
+  const int32_t* g_indices;
+  const float* g_vals;
+  int64_t g_nnz;
+  float* adia;  // [slot][nd][np]
+  float* gdia;  // [slot][ng][np]
+  float* mdia;  // [slot][nm][np]
+  unsigned int* next;
+  const double* B;
+  double* X;
+  int* out_status;
+  int* out_iters;
+  double* out_relres;
+  int* out_nrep;
+  double tol, inner_tol;
+  int max_sweeps, max_inner, prec_kind, fallback, mode;
+};
+
+// One CSR row as a dense value on diagonal `o` (entries with the same column are summed).
+__device__ __forceinline__ float csr_diag_value(const int32_t* indptr, const int32_t* indices, const float* vals,
+                                                int64_t i, int o) {
+  float v = 0.f;
+  for (int32_t e = indptr[i]; e < indptr[i + 1]; ++e)
+    if ((int64_t)indices[e] - i == o) v += vals[e];
+  return v;
+}
+
+// Data written inside this kernel by other CTAs (the G diagonals, X) is read with plain loads after
+// a cluster barrier; nothing written here is read through the non-coherent read-only path.
+template <int CL, int G>
+__global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ OnchipArgs a) {
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = (int)cl.block_rank();
+  const int64_t slot = blockIdx.x / CL;
+  extern __shared__ __align__(16) float smem[];
+  __shared__ double slots[2][8];
+  __shared__ double red[32];
+  __shared__ double bcast[8];
+  __shared__ unsigned int s_sys;
+  int buf = 0;
+  auto next_slot = [&]() { double* q = slots[buf]; buf ^= 1; return q; };
+
+  const int R = a.R, H = a.H;
+  const int64_t n = a.n, np = a.np;
+  float* ps = smem + H;                  // p: local rows [-H, R + H)
+  float* rs = smem + (R + 2 * H) + H;    // r: local rows [-H, R + H)
+  float* ds = smem + 2 * (R + 2 * H);    // d: local rows [0, R)
+  const int tid = threadIdx.x;
+  const int64_t i0 = (int64_t)rank * R;  // first row of this CTA (rows >= n are zero padding)
+  float* A = a.adia + slot * a.nd * np;
+  float* Gd = a.gdia ? a.gdia + slot * a.ng * np : nullptr;
+  float* M = a.mdia ? a.mdia + slot * a.nm * np : nullptr;
+
+  // halo rows of v (own rows at v[0, R)) from the neighbouring CTAs' shared memory
+  auto fill_halo = [&](float* v) {
+    for (int h = tid; h < H; h += kOT) {
+      const float lv = rank > 0 ? *cl.map_shared_rank(v + (R - H + h), rank - 1) : 0.f;
+      const float rv = rank + 1 < CL ? *cl.map_shared_rank(v + h, rank + 1) : 0.f;
+      v[h - H] = lv;
+      v[R + h] = rv;
+    }
+  };
+
+  while (true) {
+    if (rank == 0 && tid == 0) s_sys = atomicAdd(a.next, 1u);
+    cl.sync();
+    const int64_t s = *cl.map_shared_rank(&s_sys, 0);
+    cl.sync();  // every CTA has read the system index before rank 0 may replace it or leave
+    if (s >= a.S) break;
+
+    const float* vals = a.vals + s * a.vstride;
+    const double* B = a.B + s * n;
+    double* X = a.X + s * n;
+    int prec = a.prec_kind;
+
+    // ---- setup: diagonal slots, x = 0, on-chip vectors zero, |b|^2 ----
+    double v1[1] = {0.0};
+#pragma unroll 1
+    for (int l = tid; l < R; l += kOT) {
+      const int64_t i = i0 + l;
+      const bool live = i < n;
+      for (int k = 0; k < a.nd; ++k)
+        A[k * np + i] = live ? csr_diag_value(a.indptr, a.indices, vals, i, a.off[k]) : 0.f;
+      if (Gd) {
+        const float* gv = a.g_vals + s * a.g_nnz;
+        for (int k = 0; k < a.ng; ++k)
+          Gd[k * np + i] = live ? csr_diag_value(a.g_indptr, a.g_indices, gv, i, a.goff[k]) : 0.f;
+      }
+      ps[l] = 0.f;
+      rs[l] = 0.f;
+      ds[l] = 0.f;
+      if (live) {
+        const double bv = B[i];
+        v1[0] += bv * bv;
+        X[i] = 0.0;
+      }
+    }
+    cluster_sum<1, CL>(cl, v1, next_slot(), red, bcast);  // also publishes G's diagonals and x = 0
+    if (M) {  // M = G^T G on this CTA's rows, from G's diagonals (rows k >= i may belong to the next CTA)
+#pragma unroll 1
+      for (int l = tid; l < R; l += kOT) {
+        const int64_t i = i0 + l;
+        for (int m = 0; m < a.nm; ++m) {
+          float v = 0.f;
+          if (i < n)
+            for (int q = a.pstart[m]; q < a.pstart[m + 1]; ++q) {
+              const int64_t k = i - a.goff[a.pa[q]];
+              if (k < n) v += Gd[a.pa[q] * np + k] * Gd[a.pb[q] * np + k];
+            }
+          M[m * np + i] = v;
+        }
+      }
+    }
+    const double bnorm = sqrt(v1[0]);
+    int status = COLAGB_SYS_RUNNING;
+    double relres = bnorm > 0.0 ? 1.0 : 0.0;
+    if (!(bnorm > 0.0)) status = bnorm == 0.0 ? COLAGB_SYS_CONVERGED : COLAGB_SYS_NAN;
+    const double binv = bnorm > 0.0 ? 1.0 / bnorm : 1.0;
+
+    auto dinv_at = [&](int64_t i) -> float {
+      if (a.center < 0) return 1.f;
+      const float c = A[a.center * np + i];
+      return c != 0.f ? 1.f / c : 1.f;
+    };
+    // r = b/|b| - A x in FP64 (x gathered from global memory), |r|^2
+    auto residual = [&](double& rr) {
+      rr = 0.0;
+#pragma unroll 1
+      for (int l = tid; l < R; l += kOT) {
+        const int64_t i = i0 + l;
+        if (i < n) {
+          double ax = 0.0;
+          for (int k = 0; k < a.nd; ++k) {
+            const int64_t c = i + a.off[k];
+            if (c >= 0 && c < n) ax += (double)A[k * np + i] * X[c];
+          }
+          const double rv = B[i] * binv - ax;
+          rs[l] = (float)rv;
+          rr += rv * rv;
+        }
+      }
+    };
+    float zq[G];  // per-row register values: A p in phase A, z in phases B/C
+    // z = M r into zq, returns <r, z>; FSAI needs r's halo filled
+    auto apply_z = [&]() -> double {
+      double rz = 0.0;
+      if (prec == COLAGB_PREC_FSAI) {
+#pragma unroll
+        for (int j = 0; j < G; ++j) zq[j] = 0.f;
+        for (int m = 0; m < a.nm; ++m) {
+          const float* Mm = M + m * np + i0 + tid;
+          const float* rm = rs + tid + a.moff[m];
+#pragma unroll
+          for (int j = 0; j < G; ++j) zq[j] = fmaf(Mm[j * kOT], rm[j * kOT], zq[j]);
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < G; ++j) {
+          const int l = tid + j * kOT;
+          zq[j] = prec == COLAGB_PREC_JACOBI ? dinv_at(i0 + l) * rs[l] : rs[l];
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < G; ++j) rz += (double)(rs[tid + j * kOT] * zq[j]);
+      return rz;
+    };
+
+    double q2[1];
+    residual(q2[0]);
+    cluster_sum<1, CL>(cl, q2, next_slot(), red, bcast);
+    float rn = (float)sqrt(q2[0]);
+    float rmax = rn;
+    double relres_prev = relres;
+    if (prec == COLAGB_PREC_FSAI) fill_halo(rs);
+    __syncthreads();
+    double q1[1] = {apply_z()};
+    cluster_sum<1, CL>(cl, q1, next_slot(), red, bcast);
+    double gamma = q1[0];
+    if (status == COLAGB_SYS_RUNNING && rn <= (float)a.tol) status = COLAGB_SYS_CONVERGED;
+#pragma unroll
+    for (int j = 0; j < G; ++j) ps[tid + j * kOT] = zq[j];
+    cl.sync();
+
+    int it = 0, nrep = 0;
+    const float delta = (float)a.inner_tol;
+    while (status == COLAGB_SYS_RUNNING) {
+      // A: halo of p ; A p into zq ; <p, A p>
+      fill_halo(ps);
+      __syncthreads();
+#pragma unroll
+      for (int j = 0; j < G; ++j) zq[j] = 0.f;
+      for (int k = 0; k < a.nd; ++k) {
+        const float* Ak = A + k * np + i0 + tid;
+        const float* pk = ps + tid + a.off[k];
+#pragma unroll
+        for (int j = 0; j < G; ++j) zq[j] = fmaf(Ak[j * kOT], pk[j * kOT], zq[j]);
+      }
+      double qa[1] = {0.0};
+#pragma unroll
+      for (int j = 0; j < G; ++j) qa[0] += (double)(ps[tid + j * kOT] * zq[j]);
+      cluster_sum<1, CL>(cl, qa, next_slot(), red, bcast);
+      const double pap = qa[0];
+      if (!(pap > 0.0)) {  // not SPD in FP32 (or NaN)
+        status = (pap == pap) ? COLAGB_SYS_BREAKDOWN : COLAGB_SYS_NAN;
+        break;
+      }
+      const float alpha = (float)(gamma / pap);
+      // B: r -= alpha A p ; |r|^2 ; z and <r, z> (FSAI: after r's halo is published)
+      double qb[2] = {0.0, 0.0};
+#pragma unroll
+      for (int j = 0; j < G; ++j) {
+        const int l = tid + j * kOT;
+        const float rv = rs[l] - alpha * zq[j];
+        rs[l] = rv;
+        qb[0] += (double)(rv * rv);
+        if (prec != COLAGB_PREC_FSAI) {
+          const float zv = prec == COLAGB_PREC_JACOBI ? dinv_at(i0 + l) * rv : rv;
+          zq[j] = zv;
+          qb[1] += (double)(rv * zv);
+        }
+      }
+      if (prec == COLAGB_PREC_FSAI) {
+        cl.sync();
+        fill_halo(rs);
+        __syncthreads();
+        qb[1] = apply_z();
+      }
+      cluster_sum<2, CL>(cl, qb, next_slot(), red, bcast);
+      ++it;
+      rn = (float)sqrt(qb[0]);
+      double gamma_new = qb[1];
+      bool restart = false, dpend = true;
+      if (!(rn == rn)) {
+#pragma unroll 1
+        for (int l = tid; l < R; l += kOT) ds[l] += alpha * ps[l];
+        status = COLAGB_SYS_NAN;
+        break;
+      }
+      if (rn <= delta * rmax || rn <= (float)a.tol || it >= a.max_inner) {
+        // FP64 replacement: x += d + alpha p, d = 0 ; r = b/|b| - A x
+#pragma unroll 1
+        for (int l = tid; l < R; l += kOT) {
+          const int64_t i = i0 + l;
+          const float dn = ds[l] + alpha * ps[l];
+          if (i < n) X[i] += (double)dn;
+          ds[l] = 0.f;
+        }
+        dpend = false;
+        cl.sync();
+        residual(q2[0]);
+        cluster_sum<1, CL>(cl, q2, next_slot(), red, bcast);
+        ++nrep;
+        const double rr = sqrt(q2[0]);
+        relres = rr;
+        if (!(rr == rr)) { status = COLAGB_SYS_NAN; break; }
+        if (rr <= a.tol) { status = COLAGB_SYS_CONVERGED; break; }
+        if (it >= a.max_inner || nrep >= a.max_sweeps) { status = COLAGB_SYS_MAX_ITERS; break; }
+        if (a.fallback && prec == COLAGB_PREC_FSAI && rr > 0.5 * relres_prev) {
+          prec = COLAGB_PREC_JACOBI;  // the FP64 residual judged the learned factor
+          restart = true;
+        }
+        if (a.mode == COLAGB_IR_RESTART) restart = true;
+        relres_prev = rr;
+        rn = (float)rr;
+        rmax = rn;
+        if (prec == COLAGB_PREC_FSAI) fill_halo(rs);
+        __syncthreads();
+        q1[0] = apply_z();
+        cluster_sum<1, CL>(cl, q1, next_slot(), red, bcast);
+        gamma_new = q1[0];
+      }
+      const float beta = restart || gamma == 0.0 ? 0.f : (float)(gamma_new / gamma);
+      gamma = gamma_new;
+      // C: d += alpha p (unless flushed) ; p = z + beta p
+#pragma unroll
+      for (int j = 0; j < G; ++j) {
+        const int l = tid + j * kOT;
+        const float po = ps[l];
+        if (dpend) ds[l] += alpha * po;
+        ps[l] = zq[j] + beta * po;
+      }
+      cl.sync();
+    }
+    // finish: x += d, scale by |b|
+#pragma unroll 1
+    for (int l = tid; l < R; l += kOT) {
+      const int64_t i = i0 + l;
+      if (i < n) X[i] = (X[i] + (double)ds[l]) * (bnorm > 0.0 ? bnorm : 1.0);
+    }
+    if (rank == 0 && tid == 0) {
+      int st = status == COLAGB_SYS_RUNNING ? COLAGB_SYS_MAX_ITERS : status;
+      if (st == COLAGB_SYS_CONVERGED && a.prec_kind == COLAGB_PREC_FSAI && prec != COLAGB_PREC_FSAI)
+        st = COLAGB_SYS_FALLBACK;
+      if (a.out_status) a.out_status[s] = st;
+      if (a.out_iters) a.out_iters[s] = it;
+      if (a.out_relres) a.out_relres[s] = relres;
+      if (a.out_nrep) a.out_nrep[s] = nrep;
+    }
+  }
+}
+
+// ---- pattern analysis: the set of diagonals (column - row) a CSR pattern occupies ----
+__global__ void k_offset_bitmap(const int32_t* __restrict__ indptr, const int32_t* __restrict__ indices, int64_t n,
+                                unsigned int* bits) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    for (int32_t e = indptr[i]; e < indptr[i + 1]; ++e) {
+      const int64_t o = (int64_t)indices[e] - i + (n - 1);  // [0, 2n - 2] for valid columns
+      if (o >= 0 && o < 2 * n - 1) atomicOr(bits + (o >> 5), 1u << (o & 31));
+    }
+}
+
+// out[0] = number of distinct diagonals, out[1 .. 32] = the first 32 offsets in ascending order.
+__global__ void k_offset_collect(const unsigned int* __restrict__ bits, int64_t nwords, int64_t n, int* out) {
+  __shared__ int cnt[1024];
+  const int t = threadIdx.x;
+  const int64_t per = (nwords + blockDim.x - 1) / blockDim.x;
+  const int64_t w0 = t * per, w1 = (w0 + per < nwords) ? w0 + per : nwords;
+  int c = 0;
+  for (int64_t w = w0; w < w1; ++w) c += __popc(bits[w]);
+  cnt[t] = c;
+  __syncthreads();
+  if (t == 0) {
+    int acc = 0;
+    for (int u = 0; u < (int)blockDim.x; ++u) {
+      const int v = cnt[u];
+      cnt[u] = acc;
+      acc += v;
+    }
+    out[0] = acc;
+  }
+  __syncthreads();
+  int rnk = cnt[t];
+  for (int64_t w = w0; w < w1 && rnk < 32; ++w) {
+    unsigned int b = bits[w];
+    while (b && rnk < 32) {
+      const int bit = __ffs(b) - 1;
+      b &= b - 1;
+      out[1 + rnk] = (int)(w * 32 + bit - (n - 1));
+      ++rnk;
+    }
+  }
+}
+
+static int diag_offsets(const int32_t* indptr, const int32_t* indices, int64_t n, unsigned int* bits, int* dout,
+                        std::vector<int>& offs, cudaStream_t st) {
+  const int64_t nwords = (2 * n - 1 + 31) / 32;
+  COLAGB_CUDA(cudaMemsetAsync(bits, 0, nwords * sizeof(unsigned int), st));
+  const int nb = (int)std::min<int64_t>((n + 255) / 256, 4 * (int64_t)num_sms());
+  k_offset_bitmap<<<nb, 256, 0, st>>>(indptr, indices, n, bits);
+  COLAGB_CUDA(cudaGetLastError());
+  k_offset_collect<<<1, 1024, 0, st>>>(bits, nwords, n, dout);
+  COLAGB_CUDA(cudaGetLastError());
+  int h[33];
+  COLAGB_CUDA(cudaMemcpyAsync(h, dout, sizeof(h), cudaMemcpyDeviceToHost, st));
+  COLAGB_CUDA(cudaStreamSynchronize(st));
+  offs.assign(h + 1, h + 1 + std::min(h[0], 32));
+  if (h[0] > 32) offs.push_back(0);  // more than 32: marks the pattern as not diagonal-structured
+  return COLAGB_OK;
+}
+
+// Cluster size and rows per CTA for the on-chip schedule, from n alone (also used to size the
+// workspace).  Returns 0 when n is too large to keep p, r and d on chip.
+static int onchip_cluster(int64_t n, int* rows_per_cta, int* groups) {
+  for (int cl : {8, 16}) {
+    const int64_t r = (n + cl - 1) / cl;
+    for (int g : {8, 16, 32}) {
+      if (r <= (int64_t)kOT * g) {
+        if (rows_per_cta) *rows_per_cta = kOT * g;
+        if (groups) *groups = g;
+        if ((size_t)3 * kOT * g * sizeof(float) <= kOnchipSmemMax) return cl;
+      }
+    }
+  }
+  return 0;
+}
+
+static int onchip_slots(int cl) { return (num_sms() + cl - 1) / cl; }
+
+// Workspace of the on-chip schedule (diagonal slots + pattern scratch); 0 when not applicable.
+size_t onchip_workspace_floats(int64_t n, bool fsai) {
+  int R = 0;
+  const int cl = onchip_cluster(n, &R, nullptr);
+  if (cl == 0) return 0;
+  const int64_t np = (int64_t)cl * R;
+  const int64_t per = kMaxDiagA + (fsai ? kMaxDiagG + kMaxDiagM : 0);
+  return (size_t)onchip_slots(cl) * per * np + (size_t)(2 * n + 31) / 32 + 64 + 64;
+}
+
+template <int CL, int G>
+static int launch_onchip(const OnchipArgs& a, size_t smem, cudaStream_t st) {
+  auto kern = k_onchip_pcg<CL, G>;
+  COLAGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (CL > 8) COLAGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CL;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cfg.blockDim = dim3(kOT);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cfg.gridDim = dim3((unsigned)(CL * onchip_slots(CL)));
+  int nclusters = 0;
+  if (cudaOccupancyMaxActiveClusters(&nclusters, kern, &cfg) != cudaSuccess || nclusters < 1) {
+    cudaGetLastError();
+    return fail(COLAGB_ERR_UNSUPPORTED, "on-chip PCG: cluster not schedulable");
+  }
+  int64_t nc = std::min<int64_t>(std::min<int64_t>(nclusters, onchip_slots(CL)), a.S);
+  cfg.gridDim = dim3((unsigned)(CL * nc));
+  COLAGB_CUDA(cudaLaunchKernelEx(&cfg, kern, a));
+  return COLAGB_OK;
+}
+
+template <int CL, int G>
+static int onchip_active_clusters(size_t smem, int* nclusters) {
+  auto kern = k_onchip_pcg<CL, G>;
+  COLAGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (CL > 8) COLAGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CL;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cfg.blockDim = dim3(kOT);
+  cfg.dynamicSmemBytes = smem;
+  cfg.gridDim = dim3((unsigned)(CL * onchip_slots(CL)));
+  *nclusters = 0;
+  if (cudaOccupancyMaxActiveClusters(nclusters, kern, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    *nclusters = 0;
+  }
+  return COLAGB_OK;
+}
+
+// Called by colagb_cg_batched_csr_solve.  Returns COLAGB_ERR_UNSUPPORTED (without launching) when
+// the pattern is not a handful of diagonals or the system does not fit on chip; `*used` tells the
+// caller whether it ran.
+int onchip_pcg_solve(const colagb_batched_csr* Acsr, const double* B, double* X, const colagb_ir_params* prm,
+                     int32_t* iters, int32_t* status, double* relres, int* nrep, void* ws, size_t ws_bytes,
+                     bool* used, cudaStream_t st) {
+  *used = false;
+  const int64_t n = Acsr->n;
+  const bool fsai = prm->preconditioner == COLAGB_PREC_FSAI;
+  int R = 0, G = 0;
+  const int CL = onchip_cluster(n, &R, &G);
+  if (CL == 0 || n < 1) return COLAGB_OK;
+  const size_t need = onchip_workspace_floats(n, fsai) * sizeof(float);
+  if (ws_bytes < need || ws == nullptr) return COLAGB_OK;
+  const int64_t np = (int64_t)CL * R;
+  const int64_t per = kMaxDiagA + (fsai ? kMaxDiagG + kMaxDiagM : 0);
+  float* base = static_cast<float*>(ws);
+  const size_t slots = (size_t)onchip_slots(CL);
+  float* adia = base;
+  float* gdia = fsai ? adia + slots * kMaxDiagA * np : nullptr;
+  float* mdia = fsai ? gdia + slots * kMaxDiagG * np : nullptr;
+  unsigned int* bits = reinterpret_cast<unsigned int*>(base + slots * per * np);
+  int* dout = reinterpret_cast<int*>(bits + (2 * n + 31) / 32);
+  unsigned int* counter = reinterpret_cast<unsigned int*>(dout + 64);
+
+  std::vector<int> off, goff;
+  COLAGB_TRY(diag_offsets(Acsr->indptr, Acsr->indices, n, bits, dout, off, st));
+  if (off.empty() || (int)off.size() > kMaxDiagA) return COLAGB_OK;
+  OnchipArgs a = {};
+  a.nd = (int)off.size();
+  a.center = -1;
+  int H = 0;
+  for (int k = 0; k < a.nd; ++k) {
+    a.off[k] = off[k];
+    if (off[k] == 0) a.center = k;
+    H = std::max(H, std::abs(off[k]));
+  }
+  if (fsai) {
+    COLAGB_TRY(diag_offsets(Acsr->g_indptr, Acsr->g_indices, n, bits, dout, goff, st));
+    if (goff.empty() || (int)goff.size() > kMaxDiagG) return COLAGB_OK;
+    for (int o : goff)
+      if (o > 0) return COLAGB_OK;  // G must be lower triangular
+    std::vector<int> moff;
+    for (int o1 : goff)
+      for (int o2 : goff) moff.push_back(o2 - o1);
+    std::sort(moff.begin(), moff.end());
+    moff.erase(std::unique(moff.begin(), moff.end()), moff.end());
+    if ((int)moff.size() > kMaxDiagM) return COLAGB_OK;
+    a.ng = (int)goff.size();
+    a.nm = (int)moff.size();
+    for (int k = 0; k < a.ng; ++k) a.goff[k] = goff[k];
+    int q = 0;
+    for (int m = 0; m < a.nm; ++m) {
+      a.moff[m] = moff[m];
+      H = std::max(H, std::abs(moff[m]));
+      a.pstart[m] = q;
+      for (int i1 = 0; i1 < a.ng; ++i1)
+        for (int i2 = 0; i2 < a.ng; ++i2)
+          if (goff[i2] - goff[i1] == moff[m]) {
+            if (q >= kMaxPairs) return COLAGB_OK;
+            a.pa[q] = i1;
+            a.pb[q] = i2;
+            ++q;
+          }
+    }
+    a.pstart[a.nm] = q;
+  }
+  if (H > R) return COLAGB_OK;
+  const size_t smem = (size_t)(3 * R + 4 * H) * sizeof(float);
+  if (smem > kOnchipSmemMax) return COLAGB_OK;
+
+  a.n = n;
+  a.S = Acsr->num_systems;
+  a.np = np;
+  a.R = R;
+  a.H = H;
+  a.indptr = Acsr->indptr;
+  a.indices = Acsr->indices;
+  a.vals = Acsr->values;
+  a.vstride = Acsr->shared_values ? 0 : Acsr->nnz;
+  a.g_indptr = Acsr->g_indptr;
+  a.g_indices = Acsr->g_indices;
+  a.g_vals = Acsr->g_values;
+  a.g_nnz = Acsr->g_nnz;
+  a.adia = adia;
+  a.gdia = gdia;
+  a.mdia = mdia;
+  a.next = counter;
+  a.B = B;
+  a.X = X;
+  a.out_status = status;
+  a.out_iters = iters;
+  a.out_relres = relres;
+  a.out_nrep = nrep;
+  a.tol = prm->tol;
+  a.inner_tol = prm->inner_tol;
+  a.max_sweeps = prm->max_sweeps;
+  a.max_inner = prm->max_inner_iters;
+  a.prec_kind = prm->preconditioner;
+  a.fallback = prm->fallback;
+  a.mode = prm->mode;
+  COLAGB_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned int), st));
+  int rc;
+  if (CL == 8)
+    rc = G == 8 ? launch_onchip<8, 8>(a, smem, st)
+                : G == 16 ? launch_onchip<8, 16>(a, smem, st) : launch_onchip<8, 32>(a, smem, st);
+  else
+    rc = G == 8 ? launch_onchip<16, 8>(a, smem, st)
+                : G == 16 ? launch_onchip<16, 16>(a, smem, st) : launch_onchip<16, 32>(a, smem, st);
+  if (rc == COLAGB_OK) *used = true;
+  return rc == COLAGB_ERR_UNSUPPORTED ? COLAGB_OK : rc;
+}
+
+}  // namespace colagb
+
+using namespace colagb;
+
+extern "C" int colagb_onchip_schedule_info(int64_t n, int32_t halo, int32_t* info) {
+  if (!info || n < 0 || halo < 0) return fail(COLAGB_ERR_INVALID, "onchip info: bad argument");
+  int R = 0, G = 0;
+  const int CL = onchip_cluster(n, &R, &G);
+  info[0] = CL;
+  info[1] = R;
+  info[2] = 0;
+  info[3] = 0;
+  if (CL == 0) return COLAGB_OK;
+  const size_t smem = (size_t)(3 * R + 4 * halo) * sizeof(float);
+  info[3] = (int32_t)smem;
+  if (smem > kOnchipSmemMax || halo > R) return COLAGB_OK;
+  int nc = 0, rc;
+  if (CL == 8)
+    rc = G == 8 ? onchip_active_clusters<8, 8>(smem, &nc)
+                : G == 16 ? onchip_active_clusters<8, 16>(smem, &nc) : onchip_active_clusters<8, 32>(smem, &nc);
+  else
+    rc = G == 8 ? onchip_active_clusters<16, 8>(smem, &nc)
+                : G == 16 ? onchip_active_clusters<16, 16>(smem, &nc) : onchip_active_clusters<16, 32>(smem, &nc);
+  COLAGB_TRY(rc);
+  info[2] = std::min(nc, onchip_slots(CL));
+  return COLAGB_OK;
+}

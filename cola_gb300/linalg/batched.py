@@ -129,7 +129,17 @@ class FsaiPattern:
 
 
 _PREC = {"none": _capi.PREC_NONE, None: _capi.PREC_NONE, "jacobi": _capi.PREC_JACOBI, "fsai": _capi.PREC_FSAI}
-_SCHED = {"auto": 0, "grid": 1, "cluster8": 2, "cluster16": 3}
+_SCHED = {"auto": 0, "grid": 1, "cluster8": 2, "cluster16": 3, "onchip": 4}
+
+
+def onchip_schedule_info(n: int, halo: int) -> dict:
+    """Geometry of the on-chip schedule for n-row systems whose diagonals reach `halo` rows off the
+    main diagonal: cluster size (0: does not fit), rows per CTA, clusters resident at once, shared
+    memory per CTA in bytes."""
+    info = (C.c_int32 * 4)()
+    _capi.check(_capi.load().colagb_onchip_schedule_info(int(n), int(halo), info), "onchip info")
+    return {"cluster_size": info[0], "rows_per_cta": info[1], "clusters_in_flight": info[2],
+            "smem_per_cta": info[3]}
 
 
 def solve_batched(A: BatchedCSR, B: torch.Tensor, precond: str = "jacobi", tol: float = 1e-8,
@@ -146,9 +156,11 @@ def solve_batched(A: BatchedCSR, B: torch.Tensor, precond: str = "jacobi", tol: 
             dropped by inner_tol (default 0.1), the recurrence continues; "restart" -- classic
             iterative refinement, every FP64 residual starts a new FP32 CG run (default inner_tol 1e-4).
         max_sweeps: FP64 residual replacements per system; max_inner_iters: CG steps per system.
-        schedule: "auto" / "cluster8" / "cluster16" -- one thread-block cluster per system, launched
-            together and scheduled by the hardware; "grid" -- one cooperative grid that advances every
-            system together.
+        schedule: "onchip" -- one thread-block cluster per system with p, r and the FP32 correction in
+            the cluster's shared memory and the matrix stored by diagonals (patterns of at most 9
+            constant-offset diagonals, n <= 262144); "cluster8" / "cluster16" -- one cluster per system
+            on the CSR pattern, vectors in global memory; "grid" -- one cooperative grid that advances
+            every system together; "auto" (default) -- "onchip" when it applies, else a cluster.
     Returns (X (S, n) float64, info) with per-system iterations, status and FP64 relative residuals.
     """
     _capi.require_cuda(A.values, B)

@@ -33,11 +33,17 @@ def make_pairs(seeds, m, device, chunk=256, k_steps=150):
                               fallback=False)
         E = X - Xk
         R = B - fam.matvec(Xk)
-        nrm = torch.sqrt((E * R).sum(dim=1, keepdim=True)).clamp_min(1e-300)  # |e|_A
-        sts.append(L.stencil(fam, m))
-        rs.append((R / nrm).float().view(-1, m, m))
-        es.append((E / nrm).float().view(-1, m, m))
-        del fam, B, X, Xk, E, R
+        # plus a white-noise error per instance, so that the loss also sees the high-frequency part of
+        # the spectrum (a factor tuned only on smooth errors could inflate the largest eigenvalues)
+        W = torch.randn_like(E)
+        RW = fam.matvec(W)
+        st = L.stencil(fam, m)
+        for e_, r_ in ((E, R), (W, RW)):
+            nrm = torch.sqrt((e_ * r_).sum(dim=1, keepdim=True)).clamp_min(1e-300)  # |e|_A
+            sts.append(st)
+            rs.append((r_ / nrm).float().view(-1, m, m))
+            es.append((e_ / nrm).float().view(-1, m, m))
+        del fam, B, X, Xk, E, R, W, RW
     return torch.cat(sts), torch.cat(rs), torch.cat(es)
 
 

@@ -135,6 +135,53 @@ def kron_rbf(seed: int = 4, m: int = 64, factors: int = 3, device="cuda", dtype=
     return [rbf_grid_kernel(m, ell, device=device).to(dtype) for ell in ells], ells
 
 
+def rgg_laplacian(num_points: int = 1 << 20, radius: float = 0.002, seed: int = 7, device="cuda"):
+    """Unweighted graph Laplacian D - W of a random geometric graph: points uniform in [0,1]^2, an edge
+    between points closer than `radius`.  Neighbours are found by binning points into cells of side
+    >= radius and testing the 3x3 surrounding cells.  Returns CSR (indptr, indices, values float32)."""
+    g = torch.Generator(device=device).manual_seed(seed)
+    pts = torch.rand(num_points, 2, generator=g, device=device, dtype=torch.float64)
+    nc = max(1, int(1.0 / radius))
+    cell = (pts * nc).long().clamp_(0, nc - 1)
+    cid = cell[:, 0] * nc + cell[:, 1]
+    order = torch.argsort(cid)
+    cid_sorted = cid[order]
+    counts = torch.bincount(cid_sorted, minlength=nc * nc)
+    start = torch.zeros(nc * nc + 1, dtype=torch.int64, device=device)
+    start[1:] = torch.cumsum(counts, 0)
+    maxc = int(counts.max())
+    rows, cols = [], []
+    for dx in (-1, 0, 1):
+        for dy in (-1, 0, 1):
+            cx, cy = cell[:, 0] + dx, cell[:, 1] + dy
+            ok = (cx >= 0) & (cx < nc) & (cy >= 0) & (cy < nc)
+            nb = (cx.clamp(0, nc - 1) * nc + cy.clamp(0, nc - 1))
+            s0, cnt = start[nb], counts[nb] * ok
+            for k in range(maxc):
+                has = cnt > k
+                idx = torch.nonzero(has).flatten()
+                if idx.numel() == 0:
+                    break
+                j = order[s0[idx] + k]
+                d2 = ((pts[idx] - pts[j]) ** 2).sum(1)
+                keep = (d2 < radius * radius) & (j != idx)
+                rows.append(idx[keep])
+                cols.append(j[keep])
+    r = torch.cat(rows)
+    c = torch.cat(cols)
+    deg = torch.bincount(r, minlength=num_points).to(torch.float32)
+    # CSR of D - W with columns sorted per row
+    r_all = torch.cat([r, torch.arange(num_points, device=device)])
+    c_all = torch.cat([c, torch.arange(num_points, device=device)])
+    v_all = torch.cat([-torch.ones(r.numel(), device=device), deg])
+    key = r_all * num_points + c_all
+    o = torch.argsort(key)
+    r_all, c_all, v_all = r_all[o], c_all[o], v_all[o]
+    indptr = torch.zeros(num_points + 1, dtype=torch.int64, device=device)
+    indptr[1:] = torch.cumsum(torch.bincount(r_all, minlength=num_points), 0)
+    return indptr.to(torch.int32), c_all.to(torch.int32), v_all.to(torch.float32)
+
+
 def diffusion_3d(m: int = 128, seed: int = 1, shift: float = 1e-3, device="cuda"):
     """7-point variable-coefficient diffusion on an m^3 grid, cell coefficients exp(g), g ~ N(0,1)
     i.i.d. per cell, harmonic-mean faces, Dirichlet walls, plus shift * I.  Returns CSR arrays."""

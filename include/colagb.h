@@ -195,10 +195,19 @@ typedef struct colagb_ir_params {
   int32_t schedule;      /* COLAGB_SCHED_* */
 } colagb_ir_params;
 
-#define COLAGB_SCHED_AUTO 0     /* cluster per system when the device supports it */
+#define COLAGB_SCHED_AUTO 0     /* on-chip when the pattern allows it, else a cluster per system */
 #define COLAGB_SCHED_GRID 1     /* one cooperative grid advancing every system together */
 #define COLAGB_SCHED_CLUSTER8 2 /* one 8-CTA thread-block cluster per system */
 #define COLAGB_SCHED_CLUSTER16 3/* one 16-CTA cluster per system (non-portable cluster size) */
+#define COLAGB_SCHED_ONCHIP 4   /* one cluster per system with p, r and the FP32 correction held in the
+                                   cluster's shared memory and the matrix in diagonal storage; needs a
+                                   pattern of <= 9 constant-offset diagonals (FSAI: a lower G of <= 5),
+                                   n <= 262144.  AUTO takes it whenever those hold. */
+
+/* Geometry of the on-chip schedule for systems of n rows whose diagonals reach `halo` rows off the
+ * main diagonal: info[0] cluster size (0: n too large), info[1] rows per CTA, info[2] clusters that
+ * can be resident at once on this device (systems in flight), info[3] shared memory per CTA. */
+int colagb_onchip_schedule_info(int64_t n, int32_t halo, int32_t* info);
 
 typedef struct colagb_ir_result {
   int32_t sweeps;

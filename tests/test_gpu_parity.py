@@ -329,7 +329,7 @@ def test_tridiag_eigh(m):
 # ---------------------------------------------------------------------------------------------
 # batched systems on a shared pattern, FP64 iterative refinement
 
-@pytest.mark.parametrize("schedule", ["grid", "cluster8", "cluster16"])
+@pytest.mark.parametrize("schedule", ["grid", "cluster8", "cluster16", "onchip"])
 @pytest.mark.parametrize("precond", ["none", "jacobi"])
 def test_batched_ir_small_family(precond, schedule):
     from cola_gb300.workloads import diffusion_family_2d
@@ -395,6 +395,55 @@ def test_batched_shared_values_many_rhs():
     fam = BatchedCSR(ip, ix, v[None, :], shared=True)
     B = torch.randn(6, fam.n, device=DEV, dtype=torch.float64)
     X, info = cola.linalg.solve_batched(fam, B, precond="jacobi", tol=1e-8)
+    assert torch.all(info["status"] == 1)
+    R = B - fam.matvec(X)
+    assert float((R.norm(dim=1) / B.norm(dim=1)).max()) <= 1.01e-8
+
+
+def _closed_form_fsai(fam):
+    from cola_gb300.precond.learned_fsai import g_values
+    return g_values(fam, None)
+
+
+@pytest.mark.parametrize("m,S", [(32, 5), (30, 3), (256, 2)])
+@pytest.mark.parametrize("precond", ["none", "jacobi", "fsai"])
+def test_onchip_schedule_matches_cluster_schedule(precond, m, S):
+    """On-chip vectors + diagonal storage against the CSR cluster schedule: same algorithm, same stop
+    rule; both reach the FP64 tolerance and take about the same number of CG steps (their reductions
+    sum in different orders, and over ~1000 FP32 steps that moves the count by up to ~10%)."""
+    from cola_gb300.workloads import diffusion_family_2d
+    fam, B, _, _ = diffusion_family_2d(range(40, 40 + S), m=m, device=DEV)
+    kw = dict(precond=precond, tol=1e-8, fsai=_closed_form_fsai(fam) if precond == "fsai" else None)
+    X1, i1 = cola.linalg.solve_batched(fam, B, schedule="onchip", **kw)
+    X2, i2 = cola.linalg.solve_batched(fam, B, schedule="cluster8", **kw)
+    assert torch.all(i1["status"] == 1) and torch.all(i2["status"] == 1), (i1["status"], i2["status"])
+    R = B - fam.matvec(X1)
+    assert float((R.norm(dim=1) / B.norm(dim=1)).max()) <= 1.01e-8
+    assert float(i1["relres"].max()) <= 1e-8
+    k1, k2 = i1["iterations"].double(), i2["iterations"].double()
+    assert float(((k1 - k2).abs() - (0.15 * k2 + 3)).max()) <= 0, (k1.tolist(), k2.tolist())
+    assert rel(X1, X2) < 1e-6
+
+
+def test_onchip_three_d_shared_values_and_unsupported_patterns():
+    from cola_gb300.linalg.batched import BatchedCSR
+    from cola_gb300.workloads import diffusion_3d, rgg_laplacian
+    ip, ix, v = diffusion_3d(m=12, device=DEV)  # 7 diagonals, offsets up to 144
+    fam = BatchedCSR(ip, ix, v[None, :], shared=True)
+    B = torch.randn(5, fam.n, device=DEV, dtype=torch.float64, generator=torch.Generator(DEV).manual_seed(3))
+    X, info = cola.linalg.solve_batched(fam, B, precond="jacobi", tol=1e-8, schedule="onchip")
+    assert torch.all(info["status"] == 1)
+    R = B - fam.matvec(X)
+    assert float((R.norm(dim=1) / B.norm(dim=1)).max()) <= 1.01e-8
+    # an unstructured pattern (random geometric graph Laplacian + I): not diagonal-structured
+    ip, ix, v = rgg_laplacian(400, 0.12, seed=1, device=DEV)
+    rows = torch.repeat_interleave(torch.arange(400, device=DEV), (ip[1:] - ip[:-1]).long())
+    v = v + 0.5 * (rows == ix.long()).float()
+    fam = BatchedCSR(ip, ix, torch.stack([v, 2 * v]))
+    B = torch.randn(2, 400, device=DEV, dtype=torch.float64)
+    with pytest.raises(NotImplementedError):
+        cola.linalg.solve_batched(fam, B, precond="jacobi", tol=1e-8, schedule="onchip")
+    X, info = cola.linalg.solve_batched(fam, B, precond="jacobi", tol=1e-8)  # auto: cluster schedule
     assert torch.all(info["status"] == 1)
     R = B - fam.matvec(X)
     assert float((R.norm(dim=1) / B.norm(dim=1)).max()) <= 1.01e-8
