@@ -130,10 +130,31 @@ def shard_seeds(rank: int, systems: int) -> range:
     return range(TEST_SEEDS0 + rank * systems, TEST_SEEDS0 + (rank + 1) * systems)
 
 
-def bytes_per_system_iter(n, nnz, method):
-    """Algorithmic HBM bytes of one FP32 PCG step of one system: its CSR values (the batch shares one
-    pattern, read from L2) + 6 vector streams (p read, x r/w, r r/w, p write) + the preconditioner
-    (Jacobi: the diagonal; FSAI: G and G^T values and the intermediate t written and read)."""
+def diagonal_counts(fam):
+    """Diagonals of the family's pattern and of the FSAI operator G^T G on its lower pattern."""
+    ip = fam.indptr.cpu().long()
+    rows = torch.repeat_interleave(torch.arange(fam.n), ip[1:] - ip[:-1])
+    off = torch.unique(fam.indices.cpu().long() - rows)
+    low = off[off <= 0]
+    moff = torch.unique((low[None, :] - low[:, None]).flatten())
+    return int(off.numel()), int(moff.numel())
+
+
+def bytes_per_system_iter(n, nnz, method, schedule="cluster8", nd=5, nm=7):
+    """Algorithmic memory bytes of one FP32 PCG step of one system.
+
+    On-chip schedule: the Krylov vectors stay in the cluster's shared memory, so a step moves only
+    the matrix diagonals (nd n 4 bytes; Jacobi adds 1/diag, n 4; FSAI adds the nm diagonals of
+    M = G^T G).  Other schedules: the CSR values (the batch shares one pattern, read from L2) + 6
+    vector streams (p read, x r/w, r r/w, p write) + the preconditioner (Jacobi: the diagonal; FSAI:
+    G and G^T values and the intermediate t written and read)."""
+    if schedule == "onchip":
+        b = nd * n * 4
+        if method == "jacobi":
+            b += n * 4
+        elif method in ("learned", "fsai"):
+            b += nm * n * 4
+        return b
     b = nnz * 4 + 6 * n * 4
     if method == "jacobi":
         b += n * 4
@@ -159,6 +180,18 @@ def make_preconditioner(method, fam, coeff, dev):
 
 
 PRECOND = {"plain": "none", "jacobi": "jacobi", "learned": "fsai", "fsai": "fsai"}
+KERNEL_OF = {"onchip": "k_onchip_pcg", "cluster8": "k_cluster_pcg", "cluster16": "k_cluster_pcg",
+             "grid": "k_batched_ir"}
+
+
+def launches_per_solve(schedule, method, systems):
+    """This library's kernels per solve call: per chunk of <= 1024 systems the on-chip schedule runs
+    the pattern analysis (bitmap + collect, for A and, with FSAI, for G) and the solve kernel; the
+    other schedules one solve kernel."""
+    chunks = (systems + 1023) // 1024
+    if schedule == "onchip":
+        return chunks * (1 + 2 * (2 if PRECOND[method] == "fsai" else 1))
+    return chunks
 
 
 def run_ours(args, world, rank, local):
@@ -237,7 +270,9 @@ def run_ours(args, world, rank, local):
     peak, peak_kind = peaks()
     # CG steps only: the FP64 residual replacements (about 1 % of the traffic) are left out, so the
     # achieved figure is a lower bound
-    alg_bytes_step = (iters_total / args.steps) * bytes_per_system_iter(n, nnz, method)
+    sched_ran = info.get("schedule", args.schedule)
+    nd, nm = diagonal_counts(fam)
+    alg_bytes_step = (iters_total / args.steps) * bytes_per_system_iter(n, nnz, method, sched_ran, nd, nm)
     achieved = alg_bytes_step / (t_dev / args.steps) / 1e9
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -245,15 +280,18 @@ def run_ours(args, world, rank, local):
         "vs_baseline": None, "dtype": "f32-inner/f64-refinement", "data": "synthetic",
         "config": {"workload": WORKLOAD, "systems_per_gpu": args.systems, "grid": f"{args.m}x{args.m}", "n": n,
                    "nnz": nnz, "method": method, "tol": 1e-8, "refinement": args.mode, "inner_tol": args.inner_tol,
-                   "l2": "inputs larger than L2 (values + vectors > 1 GB per step)", "parallelism": f"replicas{world}"},
+                   "schedule": sched_ran,
+                   "l2": "inputs larger than L2 (CSR values + right-hand sides > 1.5 GB per step)",
+                   "parallelism": f"replicas{world}"},
         "quality": {"max_true_relres_fp64": relres_max, "all_converged": status_ok,
                     "mean_inner_iters_per_system": iters_total / args.steps / args.systems,
                     "max_fp64_replacements": max(sweeps)},
         "e2e": e2e,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
-                     "kernel": "k_batched_ir", "alg_bytes_per_launch": alg_bytes_step},
-        "gpu_launches": args.steps * ((args.systems + 1023) // 1024),
+                     "kernel": KERNEL_OF.get(sched_ran, "k_cluster_pcg"), "schedule": sched_ran,
+                     "alg_bytes_per_launch": alg_bytes_step},
+        "gpu_launches": args.steps * launches_per_solve(sched_ran, method, args.systems),
         "wall_s_timed": wall,
     }
     clk_s = clk.summary()

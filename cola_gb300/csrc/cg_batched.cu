@@ -728,6 +728,7 @@ extern "C" int colagb_cg_batched_csr_solve(const colagb_batched_csr* A, const do
   result->sweeps = 0;
   result->total_inner_iters = 0;
   result->status = COLAGB_OK;
+  result->schedule = params->schedule;
   if (S_all == 0 || A->n == 0) return COLAGB_OK;
   if (!B || !X) return fail(COLAGB_ERR_INVALID, "batched CG: null B/X");
   if (A->n % 4 != 0 || (uintptr_t)B % 16 != 0 || (uintptr_t)X % 16 != 0)
@@ -756,6 +757,8 @@ extern "C" int colagb_cg_batched_csr_solve(const colagb_batched_csr* A, const do
                   "batched CG: the on-chip schedule needs a pattern of at most 9 diagonals (FSAI: G lower "
                   "triangular, at most 5 diagonals) and p, r, d of one system within the shared memory of a "
                   "16-CTA cluster");
+    result->schedule = used ? COLAGB_SCHED_ONCHIP
+                            : csize == 16 ? COLAGB_SCHED_CLUSTER16 : csize == 8 ? COLAGB_SCHED_CLUSTER8 : COLAGB_SCHED_GRID;
     if (used || csize > 0) {
       if (!used)
         COLAGB_TRY(cluster_pcg_solve(&sub, B + s0 * A->n, X + s0 * A->n, params,

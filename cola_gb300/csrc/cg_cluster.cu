@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(kCT, 1) k_cluster_pcg(const __grid_constant__ 
   };
   // z = M r, <r, z>
   auto apply_z = [&](double (&q)[1]) {
-    q[0] = 0.0;
+    float qf = 0.f;  // per-thread partials in FP32, block / cluster sums in FP64
     for (int64_t i = i0 + tid; i < i1; i += kCT) {
       float zv;
       if (prec == COLAGB_PREC_FSAI) {
@@ -150,8 +150,9 @@ __global__ void __launch_bounds__(kCT, 1) k_cluster_pcg(const __grid_constant__ 
         zv = prec == COLAGB_PREC_JACOBI ? dinv[i] * r[i] : r[i];
       }
       z[i] = zv;
-      q[0] += (double)(r[i] * zv);
+      qf += r[i] * zv;
     }
+    q[0] = (double)qf;
   };
 
   cl.sync();  // x, d zero and bnorm known everywhere before the residual reads x
@@ -177,7 +178,7 @@ __global__ void __launch_bounds__(kCT, 1) k_cluster_pcg(const __grid_constant__ 
   const float delta = (float)a.inner_tol;
   while (status == COLAGB_SYS_RUNNING) {
     // A: Ap = A p ; <p, Ap>
-    double qa[1] = {0.0};
+    float qaf = 0.f;
     for (int64_t i = i0 + tid; i < i1; i += 2 * kCT) {
       const int64_t i2 = i + kCT;
       const float y0 = row_dot_f(a, vals, p, i);
@@ -188,8 +189,9 @@ __global__ void __launch_bounds__(kCT, 1) k_cluster_pcg(const __grid_constant__ 
         ap[i2] = y1;
         acc += p[i2] * y1;
       }
-      qa[0] += (double)acc;
+      qaf += acc;
     }
+    double qa[1] = {(double)qaf};
     cluster_sum<1, CL>(cl, qa, next_slot(), red, bcast);
     const double pap = qa[0];
     if (!(pap > 0.0)) {  // not SPD in FP32 (or NaN)
@@ -198,7 +200,7 @@ __global__ void __launch_bounds__(kCT, 1) k_cluster_pcg(const __grid_constant__ 
     }
     const float alpha = (float)(gamma / pap);
     // B: d += alpha p ; r -= alpha Ap ; |r|^2 ; <r, M r>  (own rows, 128-bit)
-    double qb[2] = {0.0, 0.0};
+    float qb0 = 0.f, qb1 = 0.f;
     for (int64_t i = v0; i < i1; i += vstep) {
       if (i + 3 < i1) {
         const float4 dv = *reinterpret_cast<const float4*>(d + i);
@@ -212,18 +214,19 @@ __global__ void __launch_bounds__(kCT, 1) k_cluster_pcg(const __grid_constant__ 
         rnv.x = rv.x - alpha * av.x; rnv.y = rv.y - alpha * av.y; rnv.z = rv.z - alpha * av.z; rnv.w = rv.w - alpha * av.w;
         *reinterpret_cast<float4*>(d + i) = dn;
         *reinterpret_cast<float4*>(r + i) = rnv;
-        qb[0] += (double)(rnv.x * rnv.x + rnv.y * rnv.y + rnv.z * rnv.z + rnv.w * rnv.w);
-        qb[1] += (double)(rnv.x * di.x * rnv.x + rnv.y * di.y * rnv.y + rnv.z * di.z * rnv.z + rnv.w * di.w * rnv.w);
+        qb0 += rnv.x * rnv.x + rnv.y * rnv.y + rnv.z * rnv.z + rnv.w * rnv.w;
+        qb1 += rnv.x * di.x * rnv.x + rnv.y * di.y * rnv.y + rnv.z * di.z * rnv.z + rnv.w * di.w * rnv.w;
       } else {
         for (int64_t k = i; k < i1; ++k) {
           d[k] += alpha * p[k];
           const float rv = r[k] - alpha * ap[k];
           r[k] = rv;
-          qb[0] += (double)(rv * rv);
-          qb[1] += (double)(rv * (prec == COLAGB_PREC_JACOBI ? dinv[k] : 1.f) * rv);
+          qb0 += rv * rv;
+          qb1 += rv * (prec == COLAGB_PREC_JACOBI ? dinv[k] : 1.f) * rv;
         }
       }
     }
+    double qb[2] = {(double)qb0, (double)qb1};
     cluster_sum<2, CL>(cl, qb, next_slot(), red, bcast);
     ++it;
     rn = (float)sqrt(qb[0]);

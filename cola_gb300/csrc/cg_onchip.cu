@@ -21,6 +21,7 @@
 
 #include <algorithm>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "cluster.cuh"
@@ -58,6 +59,7 @@ struct OnchipArgs {
   float* adia;  // [slot][nd][np]
   float* gdia;  // [slot][ng][np]
   float* mdia;  // [slot][nm][np]
+  float* dinv;  // [slot][np]: 1 / A(i, i) (1 where the diagonal is absent or zero)
   unsigned int* next;
   const double* B;
   double* X;
@@ -78,6 +80,113 @@ __device__ __forceinline__ float csr_diag_value(const int32_t* indptr, const int
   return v;
 }
 
+// Per-CTA geometry of the on-chip schedule.
+struct OnchipCta {
+  int rank, R, H, tid;
+  int64_t np, i0;  // padded rows per diagonal, first row of this CTA
+};
+
+// Thread `tid` owns row groups q = tid + j kOT (j < G4) of its CTA, i.e. local rows 4q .. 4q + 3:
+// every load and store of the hot loops is 128 bits wide and consecutive threads touch consecutive
+// 16-byte words (coalesced global accesses, conflict-free shared-memory accesses).
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
+__device__ __forceinline__ float dot4(float4 a, float4 b) { return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w; }
+
+// v[l + o .. l + o + 3] for a 4-aligned l: one aligned 128-bit load when o is a multiple of 4, else
+// two aligned loads and a register shuffle (o & 3 is the same for every thread).  Loads of the same
+// aligned block by neighbouring offsets (-1, 0, +1) are merged by the compiler.
+__device__ __forceinline__ float4 ld4_off(const float* v, int l, int o) {
+  const int rem = o & 3;
+  const float* b = v + l + (o - rem);
+  const float4 x = ld4(b);
+  if (rem == 0) return x;
+  const float4 y = ld4(b + 4);
+  if (rem == 1) return make_float4(x.y, x.z, x.w, y.x);
+  if (rem == 2) return make_float4(x.z, x.w, y.x, y.y);
+  return make_float4(x.w, y.x, y.y, y.z);
+}
+
+// Halo rows of v (own rows at v[0, R), H a multiple of 4) from the neighbouring CTAs' shared memory.
+template <int CL>
+__device__ __forceinline__ void fill_halo(cg::cluster_group& cl, const OnchipCta& c, float* v) {
+  for (int h = 4 * c.tid; h < c.H; h += 4 * kOT) {
+    const float4 lv = c.rank > 0 ? ld4(cl.map_shared_rank(v + (c.R - c.H + h), c.rank - 1)) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 rv = c.rank + 1 < CL ? ld4(cl.map_shared_rank(v + h, c.rank + 1)) : make_float4(0.f, 0.f, 0.f, 0.f);
+    st4(v + h - c.H, lv);
+    st4(v + c.R + h, rv);
+  }
+}
+
+// zq[j] = sum_k D[k][rows of group j] * v[rows + off[k]], k ascending (the CSR column order); returns
+// this thread's part of <v, D v>.  One diagonal at a time over all of the thread's groups (G4 128-bit
+// loads in flight per thread, ~64 KB per SM).  Measured on GB300: each diagonal costs about one L2
+// round trip plus its transfer (~1.9k cycles for 64 KB per SM); deeper software pipelining needs more
+// registers than the 128 a thread has here next to the G4 result registers.  `pending`: a
+// cluster_arrive() publishing v's own rows is outstanding; the first diagonal's loads are issued
+// before waiting on it (the matrix does not depend on it), then v's halo is filled.
+template <int CL, int G4>
+__device__ __forceinline__ float diag_product(cg::cluster_group& cl, const OnchipCta& c, float4 (&zq)[G4],
+                                              const float* D, const int* off, int nk, float* v, bool pending) {
+  float4 a4[G4];
+  const float* D0 = D + c.i0;
+#pragma unroll
+  for (int j = 0; j < G4; ++j) a4[j] = ld4(D0 + 4 * (c.tid + j * kOT));
+  if (pending) {
+    cluster_wait();
+    fill_halo<CL>(cl, c, v);
+    __syncthreads();
+  }
+#pragma unroll
+  for (int j = 0; j < G4; ++j) zq[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int k = 0; k < nk; ++k) {
+    if (k > 0) {
+      const float* Dk = D + k * c.np + c.i0;
+#pragma unroll
+      for (int j = 0; j < G4; ++j) a4[j] = ld4(Dk + 4 * (c.tid + j * kOT));
+    }
+    const int o = off[k];
+#pragma unroll
+    for (int j = 0; j < G4; ++j) {
+      const float4 pv = ld4_off(v, 4 * (c.tid + j * kOT), o);
+      zq[j].x = fmaf(a4[j].x, pv.x, zq[j].x);
+      zq[j].y = fmaf(a4[j].y, pv.y, zq[j].y);
+      zq[j].z = fmaf(a4[j].z, pv.z, zq[j].z);
+      zq[j].w = fmaf(a4[j].w, pv.w, zq[j].w);
+    }
+  }
+  float dotv = 0.f;
+#pragma unroll
+  for (int j = 0; j < G4; ++j) dotv += dot4(ld4(v + 4 * (c.tid + j * kOT)), zq[j]);
+  return dotv;
+}
+
+// z = M r into zq, returns this thread's part of <r, z>.  The per-iteration inner products are FP32
+// like the vectors (FP64 arithmetic runs at 1/64 of the FP32 rate on this GPU and would sit on the
+// critical path of every step); FP64 is kept for |b|, the true residual that judges convergence, and
+// x.  FSAI: `published` says a cluster_arrive() publishing r's own rows is outstanding.
+template <int CL, int G4>
+__device__ __forceinline__ float apply_z(cg::cluster_group& cl, const OnchipCta& c, float4 (&zq)[G4], int prec,
+                                         const OnchipArgs& a, const float* M, const float* Dv, float* rs,
+                                         bool published) {
+  if (prec == COLAGB_PREC_FSAI) return diag_product<CL, G4>(cl, c, zq, M, a.moff, a.nm, rs, published);
+  if (prec == COLAGB_PREC_JACOBI) {
+#pragma unroll
+    for (int j = 0; j < G4; ++j) {
+      const int l = 4 * (c.tid + j * kOT);
+      const float4 d = ld4(Dv + c.i0 + l), r = ld4(rs + l);
+      zq[j] = make_float4(d.x * r.x, d.y * r.y, d.z * r.z, d.w * r.w);
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < G4; ++j) zq[j] = ld4(rs + 4 * (c.tid + j * kOT));
+  }
+  float rz = 0.f;
+#pragma unroll
+  for (int j = 0; j < G4; ++j) rz += dot4(ld4(rs + 4 * (c.tid + j * kOT)), zq[j]);
+  return rz;
+}
+
 // Data written inside this kernel by other CTAs (the G diagonals, X) is read with plain loads after
 // a cluster barrier; nothing written here is read through the non-coherent read-only path.
 template <int CL, int G>
@@ -89,9 +198,12 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
   __shared__ double slots[2][8];
   __shared__ double red[32];
   __shared__ double bcast[8];
+  __shared__ float fslots[2][4];
+  __shared__ float wpart[2 * 32];
   __shared__ unsigned int s_sys;
-  int buf = 0;
+  int buf = 0, fbuf = 0;
   auto next_slot = [&]() { double* q = slots[buf]; buf ^= 1; return q; };
+  auto next_fslot = [&]() { float* q = fslots[fbuf]; fbuf ^= 1; return q; };
 
   const int R = a.R, H = a.H;
   const int64_t n = a.n, np = a.np;
@@ -103,16 +215,9 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
   float* A = a.adia + slot * a.nd * np;
   float* Gd = a.gdia ? a.gdia + slot * a.ng * np : nullptr;
   float* M = a.mdia ? a.mdia + slot * a.nm * np : nullptr;
-
-  // halo rows of v (own rows at v[0, R)) from the neighbouring CTAs' shared memory
-  auto fill_halo = [&](float* v) {
-    for (int h = tid; h < H; h += kOT) {
-      const float lv = rank > 0 ? *cl.map_shared_rank(v + (R - H + h), rank - 1) : 0.f;
-      const float rv = rank + 1 < CL ? *cl.map_shared_rank(v + h, rank + 1) : 0.f;
-      v[h - H] = lv;
-      v[R + h] = rv;
-    }
-  };
+  float* Dv = a.dinv + slot * np;
+  const OnchipCta ctx{rank, R, H, tid, np, i0};
+  constexpr int G4 = G / 4;  // 4-row groups per thread
 
   while (true) {
     if (rank == 0 && tid == 0) s_sys = atomicAdd(a.next, 1u);
@@ -132,8 +237,12 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
     for (int l = tid; l < R; l += kOT) {
       const int64_t i = i0 + l;
       const bool live = i < n;
-      for (int k = 0; k < a.nd; ++k)
-        A[k * np + i] = live ? csr_diag_value(a.indptr, a.indices, vals, i, a.off[k]) : 0.f;
+      for (int k = 0; k < a.nd; ++k) {
+        const float v = live ? csr_diag_value(a.indptr, a.indices, vals, i, a.off[k]) : 0.f;
+        A[k * np + i] = v;
+        if (k == a.center) Dv[i] = v != 0.f ? 1.f / v : 1.f;
+      }
+      if (a.center < 0) Dv[i] = 1.f;
       if (Gd) {
         const float* gv = a.g_vals + s * a.g_nnz;
         for (int k = 0; k < a.ng; ++k)
@@ -170,12 +279,8 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
     if (!(bnorm > 0.0)) status = bnorm == 0.0 ? COLAGB_SYS_CONVERGED : COLAGB_SYS_NAN;
     const double binv = bnorm > 0.0 ? 1.0 / bnorm : 1.0;
 
-    auto dinv_at = [&](int64_t i) -> float {
-      if (a.center < 0) return 1.f;
-      const float c = A[a.center * np + i];
-      return c != 0.f ? 1.f / c : 1.f;
-    };
     // r = b/|b| - A x in FP64 (x gathered from global memory), |r|^2
+    float4 zq[G4];  // per-row register values: A p in phase A, z in phases B/C
     auto residual = [&](double& rr) {
       rr = 0.0;
 #pragma unroll 1
@@ -193,95 +298,78 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
         }
       }
     };
-    float zq[G];  // per-row register values: A p in phase A, z in phases B/C
-    // z = M r into zq, returns <r, z>; FSAI needs r's halo filled
-    auto apply_z = [&]() -> double {
-      double rz = 0.0;
-      if (prec == COLAGB_PREC_FSAI) {
-#pragma unroll
-        for (int j = 0; j < G; ++j) zq[j] = 0.f;
-        for (int m = 0; m < a.nm; ++m) {
-          const float* Mm = M + m * np + i0 + tid;
-          const float* rm = rs + tid + a.moff[m];
-#pragma unroll
-          for (int j = 0; j < G; ++j) zq[j] = fmaf(Mm[j * kOT], rm[j * kOT], zq[j]);
-        }
-      } else {
-#pragma unroll
-        for (int j = 0; j < G; ++j) {
-          const int l = tid + j * kOT;
-          zq[j] = prec == COLAGB_PREC_JACOBI ? dinv_at(i0 + l) * rs[l] : rs[l];
-        }
-      }
-#pragma unroll
-      for (int j = 0; j < G; ++j) rz += (double)(rs[tid + j * kOT] * zq[j]);
-      return rz;
-    };
-
     double q2[1];
     residual(q2[0]);
     cluster_sum<1, CL>(cl, q2, next_slot(), red, bcast);
     float rn = (float)sqrt(q2[0]);
     float rmax = rn;
     double relres_prev = relres;
-    if (prec == COLAGB_PREC_FSAI) fill_halo(rs);
+    if (prec == COLAGB_PREC_FSAI) fill_halo<CL>(cl, ctx, rs);
     __syncthreads();
-    double q1[1] = {apply_z()};
-    cluster_sum<1, CL>(cl, q1, next_slot(), red, bcast);
-    double gamma = q1[0];
+    float q1[1] = {apply_z<CL, G4>(cl, ctx, zq, prec, a, M, Dv, rs, false)};
+    cluster_sum_f<1, CL>(cl, q1, wpart, next_fslot());
+    float gamma = q1[0];
     if (status == COLAGB_SYS_RUNNING && rn <= (float)a.tol) status = COLAGB_SYS_CONVERGED;
 #pragma unroll
-    for (int j = 0; j < G; ++j) ps[tid + j * kOT] = zq[j];
-    cl.sync();
+    for (int j = 0; j < G4; ++j) st4(ps + 4 * (tid + j * kOT), zq[j]);
+    __syncthreads();
+    cluster_arrive();  // p published; waited for inside the first step
+    bool arrived = true;
 
     int it = 0, nrep = 0;
     const float delta = (float)a.inner_tol;
     while (status == COLAGB_SYS_RUNNING) {
-      // A: halo of p ; A p into zq ; <p, A p>
-      fill_halo(ps);
-      __syncthreads();
-#pragma unroll
-      for (int j = 0; j < G; ++j) zq[j] = 0.f;
-      for (int k = 0; k < a.nd; ++k) {
-        const float* Ak = A + k * np + i0 + tid;
-        const float* pk = ps + tid + a.off[k];
-#pragma unroll
-        for (int j = 0; j < G; ++j) zq[j] = fmaf(Ak[j * kOT], pk[j * kOT], zq[j]);
-      }
-      double qa[1] = {0.0};
-#pragma unroll
-      for (int j = 0; j < G; ++j) qa[0] += (double)(ps[tid + j * kOT] * zq[j]);
-      cluster_sum<1, CL>(cl, qa, next_slot(), red, bcast);
-      const double pap = qa[0];
-      if (!(pap > 0.0)) {  // not SPD in FP32 (or NaN)
+      // A: A p into zq ; <p, A p>
+      const float paf = diag_product<CL, G4>(cl, ctx, zq, A, a.off, a.nd, ps, true);
+      arrived = false;
+      float qa[1] = {paf};
+      cluster_sum_f<1, CL>(cl, qa, wpart, next_fslot());
+      const float pap = qa[0];
+      if (!(pap > 0.f)) {  // not SPD in FP32 (or NaN)
         status = (pap == pap) ? COLAGB_SYS_BREAKDOWN : COLAGB_SYS_NAN;
         break;
       }
-      const float alpha = (float)(gamma / pap);
-      // B: r -= alpha A p ; |r|^2 ; z and <r, z> (FSAI: after r's halo is published)
-      double qb[2] = {0.0, 0.0};
+      const float alpha = gamma / pap;
+      // B: r -= alpha A p ; |r|^2 ; z and <r, z> (FSAI: after r's halo is published).  All loads of
+      // a phase are issued before its first store: the compiler cannot prove that the shared-memory
+      // stores do not alias the global loads, and interleaving them would serialise one L2 round
+      // trip per row.
+      float rrf = 0.f, rzf = 0.f;
+      {
+        float4 rv[G4], dv[G4];
 #pragma unroll
-      for (int j = 0; j < G; ++j) {
-        const int l = tid + j * kOT;
-        const float rv = rs[l] - alpha * zq[j];
-        rs[l] = rv;
-        qb[0] += (double)(rv * rv);
-        if (prec != COLAGB_PREC_FSAI) {
-          const float zv = prec == COLAGB_PREC_JACOBI ? dinv_at(i0 + l) * rv : rv;
-          zq[j] = zv;
-          qb[1] += (double)(rv * zv);
+        for (int j = 0; j < G4; ++j) {
+          rv[j] = ld4(rs + 4 * (tid + j * kOT));
+          dv[j] = prec == COLAGB_PREC_JACOBI ? ld4(Dv + i0 + 4 * (tid + j * kOT)) : make_float4(1.f, 1.f, 1.f, 1.f);
         }
+#pragma unroll
+        for (int j = 0; j < G4; ++j) {
+          rv[j].x -= alpha * zq[j].x;
+          rv[j].y -= alpha * zq[j].y;
+          rv[j].z -= alpha * zq[j].z;
+          rv[j].w -= alpha * zq[j].w;
+          rrf += dot4(rv[j], rv[j]);
+          if (prec != COLAGB_PREC_FSAI) {
+            const float4 zv = prec == COLAGB_PREC_JACOBI
+                                  ? make_float4(dv[j].x * rv[j].x, dv[j].y * rv[j].y, dv[j].z * rv[j].z, dv[j].w * rv[j].w)
+                                  : rv[j];
+            zq[j] = zv;
+            rzf += dot4(rv[j], zv);
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < G4; ++j) st4(rs + 4 * (tid + j * kOT), rv[j]);
       }
+      float qb[2] = {rrf, rzf};
       if (prec == COLAGB_PREC_FSAI) {
-        cl.sync();
-        fill_halo(rs);
         __syncthreads();
-        qb[1] = apply_z();
+        cluster_arrive();
+        qb[1] = apply_z<CL, G4>(cl, ctx, zq, prec, a, M, Dv, rs, true);
       }
-      cluster_sum<2, CL>(cl, qb, next_slot(), red, bcast);
+      cluster_sum_f<2, CL>(cl, qb, wpart, next_fslot());
       ++it;
-      rn = (float)sqrt(qb[0]);
-      double gamma_new = qb[1];
+      rn = sqrtf(qb[0]);
+      float gamma_new = qb[1];
       bool restart = false, dpend = true;
       if (!(rn == rn)) {
 #pragma unroll 1
@@ -316,24 +404,38 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
         relres_prev = rr;
         rn = (float)rr;
         rmax = rn;
-        if (prec == COLAGB_PREC_FSAI) fill_halo(rs);
+        if (prec == COLAGB_PREC_FSAI) fill_halo<CL>(cl, ctx, rs);
         __syncthreads();
-        q1[0] = apply_z();
-        cluster_sum<1, CL>(cl, q1, next_slot(), red, bcast);
+        q1[0] = apply_z<CL, G4>(cl, ctx, zq, prec, a, M, Dv, rs, false);
+        cluster_sum_f<1, CL>(cl, q1, wpart, next_fslot());
         gamma_new = q1[0];
       }
-      const float beta = restart || gamma == 0.0 ? 0.f : (float)(gamma_new / gamma);
+      const float beta = restart || gamma == 0.f ? 0.f : gamma_new / gamma;
       gamma = gamma_new;
       // C: d += alpha p (unless flushed) ; p = z + beta p
+      {
+        float4 po[G4], dd[G4];
 #pragma unroll
-      for (int j = 0; j < G; ++j) {
-        const int l = tid + j * kOT;
-        const float po = ps[l];
-        if (dpend) ds[l] += alpha * po;
-        ps[l] = zq[j] + beta * po;
+        for (int j = 0; j < G4; ++j) {
+          po[j] = ld4(ps + 4 * (tid + j * kOT));
+          dd[j] = ld4(ds + 4 * (tid + j * kOT));
+        }
+#pragma unroll
+        for (int j = 0; j < G4; ++j) {
+          st4(ps + 4 * (tid + j * kOT), make_float4(zq[j].x + beta * po[j].x, zq[j].y + beta * po[j].y,
+                                                    zq[j].z + beta * po[j].z, zq[j].w + beta * po[j].w));
+          if (dpend)
+            st4(ds + 4 * (tid + j * kOT), make_float4(dd[j].x + alpha * po[j].x, dd[j].y + alpha * po[j].y,
+                                                      dd[j].z + alpha * po[j].z, dd[j].w + alpha * po[j].w));
+        }
       }
-      cl.sync();
+      __syncthreads();
+      cluster_arrive();  // p published; waited for at the start of the next step
+      arrived = true;
     }
+    // every break leaves the loop with no arrive outstanding; a system that needs no step (zero or
+    // already-converged right-hand side) still owes the wait for the arrive issued before the loop
+    if (arrived) cluster_wait();
     // finish: x += d, scale by |b|
 #pragma unroll 1
     for (int l = tid; l < R; l += kOT) {
@@ -435,7 +537,7 @@ size_t onchip_workspace_floats(int64_t n, bool fsai) {
   const int cl = onchip_cluster(n, &R, nullptr);
   if (cl == 0) return 0;
   const int64_t np = (int64_t)cl * R;
-  const int64_t per = kMaxDiagA + (fsai ? kMaxDiagG + kMaxDiagM : 0);
+  const int64_t per = kMaxDiagA + 1 + (fsai ? kMaxDiagG + kMaxDiagM : 0);
   return (size_t)onchip_slots(cl) * per * np + (size_t)(2 * n + 31) / 32 + 64 + 64;
 }
 
@@ -506,12 +608,13 @@ int onchip_pcg_solve(const colagb_batched_csr* Acsr, const double* B, double* X,
   const size_t need = onchip_workspace_floats(n, fsai) * sizeof(float);
   if (ws_bytes < need || ws == nullptr) return COLAGB_OK;
   const int64_t np = (int64_t)CL * R;
-  const int64_t per = kMaxDiagA + (fsai ? kMaxDiagG + kMaxDiagM : 0);
+  const int64_t per = kMaxDiagA + 1 + (fsai ? kMaxDiagG + kMaxDiagM : 0);
   float* base = static_cast<float*>(ws);
   const size_t slots = (size_t)onchip_slots(CL);
   float* adia = base;
   float* gdia = fsai ? adia + slots * kMaxDiagA * np : nullptr;
   float* mdia = fsai ? gdia + slots * kMaxDiagG * np : nullptr;
+  float* dinv = adia + slots * (kMaxDiagA + (fsai ? kMaxDiagG + kMaxDiagM : 0)) * np;
   unsigned int* bits = reinterpret_cast<unsigned int*>(base + slots * per * np);
   int* dout = reinterpret_cast<int*>(bits + (2 * n + 31) / 32);
   unsigned int* counter = reinterpret_cast<unsigned int*>(dout + 64);
@@ -558,6 +661,7 @@ int onchip_pcg_solve(const colagb_batched_csr* Acsr, const double* B, double* X,
     }
     a.pstart[a.nm] = q;
   }
+  H = (H + 3) / 4 * 4;  // halo rows in whole 16-byte words
   if (H > R) return COLAGB_OK;
   const size_t smem = (size_t)(3 * R + 4 * H) * sizeof(float);
   if (smem > kOnchipSmemMax) return COLAGB_OK;
@@ -578,6 +682,7 @@ int onchip_pcg_solve(const colagb_batched_csr* Acsr, const double* B, double* X,
   a.adia = adia;
   a.gdia = gdia;
   a.mdia = mdia;
+  a.dinv = dinv;
   a.next = counter;
   a.B = B;
   a.X = X;

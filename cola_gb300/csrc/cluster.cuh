@@ -32,4 +32,40 @@ __device__ __forceinline__ void cluster_sum(cooperative_groups::cluster_group& c
   __syncthreads();
 }
 
+// Split cluster barrier: arrive (release) publishes this thread's prior writes, wait (acquire)
+// returns once every thread of the cluster has arrived.  Work placed between the two overlaps the
+// barrier's latency.  Every thread must call them in strict arrive / wait alternation.
+__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory"); }
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory"); }
+
+// FP32 cluster-wide sums for the per-iteration inner products, built for latency: a butterfly in
+// each warp, one block barrier, one cluster barrier, then every warp reads the CL per-CTA partials
+// through distributed shared memory and combines them with the same butterfly.  Every thread of
+// every CTA ends with bit-identical sums (fixed combination order; a + b == b + a in IEEE
+// arithmetic).  `wpart` holds NQ x 32 floats; `slot` NQ floats and must alternate between two
+// buffers across consecutive calls (the same rule as cluster_sum).
+template <int NQ, int CL>
+__device__ __forceinline__ void cluster_sum_f(cooperative_groups::cluster_group& cl, float (&v)[NQ], float* wpart,
+                                              float* slot) {
+  static_assert(CL <= 32, "one warp combines the CTA partials");
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nw = blockDim.x >> 5;
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    const float x = warp_sum(v[q]);
+    if (lane == 0) wpart[q * 32 + warp] = x;
+  }
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      const float x = warp_sum(lane < nw ? wpart[q * 32 + lane] : 0.f);
+      if (lane == 0) slot[q] = x;
+    }
+  }
+  cl.sync();
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) v[q] = warp_sum(lane < CL ? *cl.map_shared_rank(slot + q, lane) : 0.f);
+}
+
 }  // namespace colagb

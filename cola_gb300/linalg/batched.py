@@ -130,6 +130,7 @@ class FsaiPattern:
 
 _PREC = {"none": _capi.PREC_NONE, None: _capi.PREC_NONE, "jacobi": _capi.PREC_JACOBI, "fsai": _capi.PREC_FSAI}
 _SCHED = {"auto": 0, "grid": 1, "cluster8": 2, "cluster16": 3, "onchip": 4}
+_SCHED_NAME = {v: k for k, v in _SCHED.items()}
 
 
 def onchip_schedule_info(n: int, halo: int) -> dict:
@@ -209,5 +210,6 @@ def solve_batched(A: BatchedCSR, B: torch.Tensor, precond: str = "jacobi", tol: 
                                                 iters.data_ptr(), status.data_ptr(), relres.data_ptr(), ws.data_ptr(),
                                                 nbytes.value, C.byref(res), _capi.stream_ptr(dev)), "batched cg")
     info = {"iterations": iters, "status": status, "relres": relres, "replacements": int(res.sweeps),
-            "sweeps": int(res.sweeps), "max_iterations": int(res.total_inner_iters)}
+            "sweeps": int(res.sweeps), "max_iterations": int(res.total_inner_iters),
+            "schedule": _SCHED_NAME.get(int(res.schedule), "auto")}
     return X, info
