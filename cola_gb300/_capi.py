@@ -116,6 +116,7 @@ SIGNATURES = {
     "colagb_conv3x3_backward": (C.c_int, [_vp, _vp, _vp, _i64, _i32, _i32, _i64, _i64, _vp, _vp, _vp, _vp, _sz,
                                           _vp]),
     "colagb_fsai_loss_grad": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _i64, _i64, _vp, _vp, _vp, _sz, _vp]),
+    "colagb_fsai_rq_loss_grad": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _i64, _i64, _vp, _vp, _vp, _sz, _vp]),
     "colagb_adam_step": (C.c_int, [_vp, _vp, _vp, _vp, _i64, C.c_float, C.c_float, C.c_float, C.c_float, _i32,
                                    _vp]),
 }

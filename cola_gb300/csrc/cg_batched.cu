@@ -86,6 +86,7 @@ struct SysState {
   __device__ __forceinline__ int& flags(int s) const { return i32(4)[s]; }
   __device__ __forceinline__ int* act() const { return i32(5); }
   __device__ __forceinline__ int* act2() const { return i32(6); }
+  __device__ __forceinline__ int& it_rep(int s) const { return i32(7)[s]; }
 };
 constexpr int F_ACTIVE = 1, F_REPLACE = 2, F_RESTART = 4;
 
@@ -440,6 +441,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_batched_ir(const __grid_constan
     m.status(s) = COLAGB_SYS_RUNNING;
     m.it(s) = 0;
     m.nrep(s) = 0;
+    m.it_rep(s) = 0;
     m.flags(s) = F_ACTIVE;
   }
   int nact = build_list(S, m.act(), [&](int) { return true; });
@@ -527,7 +529,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_batched_ir(const __grid_constan
         if (!(rn == rn)) {
           m.status(s) = COLAGB_SYS_NAN;
           f = 0;
-        } else if (rn <= delta * m.rmax(s) || rn <= (float)a.tol || m.it(s) >= a.max_inner) {
+        } else if (rn <= delta * m.rmax(s) || rn <= (float)a.tol || m.it(s) >= a.max_inner ||
+                   (a.fallback && m.prec(s) == COLAGB_PREC_FSAI && m.it(s) - m.it_rep(s) >= kJudgeSteps)) {
           f |= F_REPLACE;
         }
         m.flags(s) = f;
@@ -546,6 +549,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_batched_ir(const __grid_constan
           const int s = m.act2()[j];
           const double rr = sqrt(__ldcg(acc[3] + s));
           m.nrep(s) += 1;
+          m.it_rep(s) = m.it(s);
           int f = m.flags(s);
           if (!(rr == rr)) {
             m.status(s) = COLAGB_SYS_NAN;
@@ -628,7 +632,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_batched_ir(const __grid_constan
   }
 }
 
-static size_t batched_smem(int64_t S) { return (size_t)S * (3 * 8 + 11 * 4) + 64; }
+static size_t batched_smem(int64_t S) { return (size_t)S * (3 * 8 + 12 * 4) + 64; }
 
 struct BatchedWs {
   float *r, *p, *ap, *d, *z, *t, *dinv;

@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(kCT, 1) k_cluster_pcg(const __grid_constant__ 
   for (int64_t i = i0 + tid; i < i1; i += kCT) p[i] = z[i];
   cl.sync();
 
-  int it = 0, nrep = 0;
+  int it = 0, nrep = 0, it_rep = 0;
   const float delta = (float)a.inner_tol;
   while (status == COLAGB_SYS_RUNNING) {
     // A: Ap = A p ; <p, Ap>
@@ -236,8 +236,10 @@ __global__ void __launch_bounds__(kCT, 1) k_cluster_pcg(const __grid_constant__ 
       status = COLAGB_SYS_NAN;
       break;
     }
-    if (rn <= delta * rmax || rn <= (float)a.tol || it >= a.max_inner) {
+    if (rn <= delta * rmax || rn <= (float)a.tol || it >= a.max_inner ||
+        (a.fallback && prec == COLAGB_PREC_FSAI && it - it_rep >= kJudgeSteps)) {
       // FP64 replacement: x += d, d = 0 ; r = b/|b| - A x
+      it_rep = it;
       for (int64_t i = i0 + tid; i < i1; i += kCT) {
         X[i] += (double)d[i];
         d[i] = 0.f;

@@ -147,12 +147,19 @@ __device__ __forceinline__ float diag_product(cg::cluster_group& cl, const Onchi
     }
     const int o = off[k];
 #pragma unroll
-    for (int j = 0; j < G4; ++j) {
-      const float4 pv = ld4_off(v, 4 * (c.tid + j * kOT), o);
-      zq[j].x = fmaf(a4[j].x, pv.x, zq[j].x);
-      zq[j].y = fmaf(a4[j].y, pv.y, zq[j].y);
-      zq[j].z = fmaf(a4[j].z, pv.z, zq[j].z);
-      zq[j].w = fmaf(a4[j].w, pv.w, zq[j].w);
+    for (int h = 0; h < 2; ++h) {
+      // the shared-memory operands in two halves, so at most half of them are held at once
+      float4 pv[G4 / 2];
+#pragma unroll
+      for (int jj = 0; jj < G4 / 2; ++jj) pv[jj] = ld4_off(v, 4 * (c.tid + (h * (G4 / 2) + jj) * kOT), o);
+#pragma unroll
+      for (int jj = 0; jj < G4 / 2; ++jj) {
+        const int j = h * (G4 / 2) + jj;
+        zq[j].x = fmaf(a4[j].x, pv[jj].x, zq[j].x);
+        zq[j].y = fmaf(a4[j].y, pv[jj].y, zq[j].y);
+        zq[j].z = fmaf(a4[j].z, pv[jj].z, zq[j].z);
+        zq[j].w = fmaf(a4[j].w, pv[jj].w, zq[j].w);
+      }
     }
   }
   float dotv = 0.f;
@@ -316,7 +323,7 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
     cluster_arrive();  // p published; waited for inside the first step
     bool arrived = true;
 
-    int it = 0, nrep = 0;
+    int it = 0, nrep = 0, it_rep = 0;
     const float delta = (float)a.inner_tol;
     while (status == COLAGB_SYS_RUNNING) {
       // A: A p into zq ; <p, A p>
@@ -335,30 +342,35 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
       // stores do not alias the global loads, and interleaving them would serialise one L2 round
       // trip per row.
       float rrf = 0.f, rzf = 0.f;
-      {
-        float4 rv[G4], dv[G4];
 #pragma unroll
-        for (int j = 0; j < G4; ++j) {
-          rv[j] = ld4(rs + 4 * (tid + j * kOT));
-          dv[j] = prec == COLAGB_PREC_JACOBI ? ld4(Dv + i0 + 4 * (tid + j * kOT)) : make_float4(1.f, 1.f, 1.f, 1.f);
+      for (int h = 0; h < 2; ++h) {  // two halves of the groups: half the registers in flight
+        constexpr int H4 = G4 / 2;
+        float4 rv[H4], dv[H4];
+#pragma unroll
+        for (int jj = 0; jj < H4; ++jj) {
+          const int j = h * H4 + jj;
+          rv[jj] = ld4(rs + 4 * (tid + j * kOT));
+          dv[jj] = prec == COLAGB_PREC_JACOBI ? ld4(Dv + i0 + 4 * (tid + j * kOT)) : make_float4(1.f, 1.f, 1.f, 1.f);
         }
 #pragma unroll
-        for (int j = 0; j < G4; ++j) {
-          rv[j].x -= alpha * zq[j].x;
-          rv[j].y -= alpha * zq[j].y;
-          rv[j].z -= alpha * zq[j].z;
-          rv[j].w -= alpha * zq[j].w;
-          rrf += dot4(rv[j], rv[j]);
+        for (int jj = 0; jj < H4; ++jj) {
+          const int j = h * H4 + jj;
+          rv[jj].x -= alpha * zq[j].x;
+          rv[jj].y -= alpha * zq[j].y;
+          rv[jj].z -= alpha * zq[j].z;
+          rv[jj].w -= alpha * zq[j].w;
+          rrf += dot4(rv[jj], rv[jj]);
           if (prec != COLAGB_PREC_FSAI) {
             const float4 zv = prec == COLAGB_PREC_JACOBI
-                                  ? make_float4(dv[j].x * rv[j].x, dv[j].y * rv[j].y, dv[j].z * rv[j].z, dv[j].w * rv[j].w)
-                                  : rv[j];
+                                  ? make_float4(dv[jj].x * rv[jj].x, dv[jj].y * rv[jj].y, dv[jj].z * rv[jj].z,
+                                                dv[jj].w * rv[jj].w)
+                                  : rv[jj];
             zq[j] = zv;
-            rzf += dot4(rv[j], zv);
+            rzf += dot4(rv[jj], zv);
           }
         }
 #pragma unroll
-        for (int j = 0; j < G4; ++j) st4(rs + 4 * (tid + j * kOT), rv[j]);
+        for (int jj = 0; jj < H4; ++jj) st4(rs + 4 * (tid + (h * H4 + jj) * kOT), rv[jj]);
       }
       float qb[2] = {rrf, rzf};
       if (prec == COLAGB_PREC_FSAI) {
@@ -377,7 +389,8 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
         status = COLAGB_SYS_NAN;
         break;
       }
-      if (rn <= delta * rmax || rn <= (float)a.tol || it >= a.max_inner) {
+      if (rn <= delta * rmax || rn <= (float)a.tol || it >= a.max_inner ||
+          (a.fallback && prec == COLAGB_PREC_FSAI && it - it_rep >= kJudgeSteps)) {
         // FP64 replacement: x += d + alpha p, d = 0 ; r = b/|b| - A x
 #pragma unroll 1
         for (int l = tid; l < R; l += kOT) {
@@ -387,6 +400,7 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
           ds[l] = 0.f;
         }
         dpend = false;
+        it_rep = it;
         cl.sync();
         residual(q2[0]);
         cluster_sum<1, CL>(cl, q2, next_slot(), red, bcast);
@@ -413,20 +427,23 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
       const float beta = restart || gamma == 0.f ? 0.f : gamma_new / gamma;
       gamma = gamma_new;
       // C: d += alpha p (unless flushed) ; p = z + beta p
-      {
-        float4 po[G4], dd[G4];
 #pragma unroll
-        for (int j = 0; j < G4; ++j) {
-          po[j] = ld4(ps + 4 * (tid + j * kOT));
-          dd[j] = ld4(ds + 4 * (tid + j * kOT));
+      for (int h = 0; h < 2; ++h) {  // two halves of the groups: half the registers in flight
+        constexpr int H4 = G4 / 2;
+        float4 po[H4], dd[H4];
+#pragma unroll
+        for (int jj = 0; jj < H4; ++jj) {
+          po[jj] = ld4(ps + 4 * (tid + (h * H4 + jj) * kOT));
+          dd[jj] = ld4(ds + 4 * (tid + (h * H4 + jj) * kOT));
         }
 #pragma unroll
-        for (int j = 0; j < G4; ++j) {
-          st4(ps + 4 * (tid + j * kOT), make_float4(zq[j].x + beta * po[j].x, zq[j].y + beta * po[j].y,
-                                                    zq[j].z + beta * po[j].z, zq[j].w + beta * po[j].w));
+        for (int jj = 0; jj < H4; ++jj) {
+          const int j = h * H4 + jj;
+          st4(ps + 4 * (tid + j * kOT), make_float4(zq[j].x + beta * po[jj].x, zq[j].y + beta * po[jj].y,
+                                                    zq[j].z + beta * po[jj].z, zq[j].w + beta * po[jj].w));
           if (dpend)
-            st4(ds + 4 * (tid + j * kOT), make_float4(dd[j].x + alpha * po[j].x, dd[j].y + alpha * po[j].y,
-                                                      dd[j].z + alpha * po[j].z, dd[j].w + alpha * po[j].w));
+            st4(ds + 4 * (tid + j * kOT), make_float4(dd[jj].x + alpha * po[jj].x, dd[jj].y + alpha * po[jj].y,
+                                                      dd[jj].z + alpha * po[jj].z, dd[jj].w + alpha * po[jj].w));
         }
       }
       __syncthreads();

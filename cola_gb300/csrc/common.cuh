@@ -151,6 +151,12 @@ __device__ __forceinline__ bool grid_sync(const GridBarrier& gb) {
   return s_ok != 0;
 }
 
+// A learned (FSAI) preconditioner whose FP32 residual stalls would never reach the 10x drop that
+// triggers an FP64 residual replacement, and so would never be judged: while a system runs with
+// the FSAI factor and the Jacobi fallback is enabled, a replacement (and with it the judge) is also
+// forced after this many steps without one.  Converging FSAI-PCG replaces far more often.
+constexpr int kJudgeSteps = 1000;
+
 constexpr long long kDefaultSpinLimit = 20000000LL;  // ~ a few seconds of 20 ns naps
 
 }  // namespace colagb

@@ -5,8 +5,10 @@
 // Parametrisation: with d = diag(A), a_N = A[p, p-m], a_W = A[p, p-1] and the Schur complement
 // s_p = d_p - a_N^2 / d_N - a_W^2 / d_W, the closed-form FSAI row of this pattern is
 //   G_C = 1/sqrt(s_p),  G_N = -(a_N/d_N)/sqrt(s_p),  G_W = -(a_W/d_W)/sqrt(s_p).
-// The network's outputs o = (o0, o1, o2) per cell scale it: G_C *= e^o0, G_N *= e^o0 (1 + o1),
-// G_W *= e^o0 (1 + o2).  G_C > 0 for any o, so P is SPD whatever the network predicts.
+// The network's outputs (o1, o2) per cell reshape it, H = (G_N (1 + o1), G_W (1 + o2), G_C), and each
+// row is renormalised so that (G A G^T)_pp = 1 (the FSAI normalisation; the closed form already
+// satisfies it, so o = 0 reproduces closed-form FSAI).  G_C > 0 for any o, so P is SPD whatever the
+// network predicts, and diag(G A G^T) = 1 keeps its largest eigenvalue bounded.
 //
 // Training loss per system (pairs (r, e) with A e = r, e from this project's CG):
 //   l = ||P r - e||_A^2 / ||e||_A^2 = (v^T A v - 2 v^T r + e^T r) / (e^T r),  v = G^T G r.
@@ -88,24 +90,46 @@ __device__ __forceinline__ void fsai_closed_form(const float* a, int64_t n, int6
   fW = cW * is;
 }
 
-// G stencil (S, 3, m, m) [N, W, C] from the network output o (S, 3, m, m) (o may be null: o = 0)
+// One row of G from the network output (o1, o2): H = (fN (1 + tanh o1), fW (1 + tanh o2), fC) -- each
+// off-diagonal between 0 and twice its closed-form value -- then the FSAI
+// normalisation G = H / sqrt(s), s = (H A H^T)_pp, so that diag(G A G^T) = 1 whatever the network
+// predicts (the largest eigenvalue of G A G^T stays bounded; only the shape of each row is learned).
+// For o = 0, H is the closed-form row and s = 1.  Also returns the pieces the gradient needs.
+struct FsaiRow {
+  float fN, fW, fC;  // closed form
+  float hN, hW, hC;  // before normalisation
+  float d, dN, dW, aN, aW;
+  float s;
+};
+__device__ __forceinline__ FsaiRow fsai_row(const float* a, int64_t n, int64_t m, int64_t p, float o1, float o2) {
+  FsaiRow r;
+  fsai_closed_form(a, n, m, p, r.fN, r.fW, r.fC);
+  const int64_t i = p / m, j = p % m;
+  r.d = at5(a, n, 2, p);
+  r.dN = i > 0 ? at5(a, n, 2, p - m) : 0.f;
+  r.dW = j > 0 ? at5(a, n, 2, p - 1) : 0.f;
+  r.aN = i > 0 ? at5(a, n, 0, p) : 0.f;
+  r.aW = j > 0 ? at5(a, n, 1, p) : 0.f;
+  r.hN = r.fN * (1.f + tanhf(o1));
+  r.hW = r.fW * (1.f + tanhf(o2));
+  r.hC = r.fC;
+  r.s = r.hC * r.hC * r.d + r.hN * r.hN * r.dN + r.hW * r.hW * r.dW + 2.f * r.hC * (r.hN * r.aN + r.hW * r.aW);
+  return r;
+}
+
+// G stencil (S, 3, m, m) [N, W, C] from the network output o (S, 3, m, m) (o may be null: o = 0);
+// channel 0 of o is not used (the normalisation fixes each row's scale).
 __global__ void k_fsai_assemble(const float* __restrict__ st, const float* __restrict__ o, int64_t m, int64_t S,
                                 float* __restrict__ g) {
   const int64_t n = m * m;
   for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < S * n; u += (int64_t)gridDim.x * blockDim.x) {
     const int64_t s = u / n, p = u % n;
-    float fN, fW, fC;
-    fsai_closed_form(st + s * 5 * n, n, m, p, fN, fW, fC);
-    float o0 = 0.f, o1 = 0.f, o2 = 0.f;
-    if (o) {
-      o0 = o[s * 3 * n + p];
-      o1 = o[s * 3 * n + n + p];
-      o2 = o[s * 3 * n + 2 * n + p];
-    }
-    const float e0 = expf(o0);
-    g[s * 3 * n + p] = e0 * (1.f + o1) * fN;
-    g[s * 3 * n + n + p] = e0 * (1.f + o2) * fW;
-    g[s * 3 * n + 2 * n + p] = e0 * fC;
+    const float o1 = o ? o[s * 3 * n + n + p] : 0.f, o2 = o ? o[s * 3 * n + 2 * n + p] : 0.f;
+    const FsaiRow r = fsai_row(st + s * 5 * n, n, m, p, o1, o2);
+    const float is = o ? rsqrtf(r.s) : 1.f;
+    g[s * 3 * n + p] = r.hN * is;
+    g[s * 3 * n + n + p] = r.hW * is;
+    g[s * 3 * n + 2 * n + p] = r.hC * is;
   }
 }
 
@@ -312,6 +336,71 @@ __device__ __forceinline__ float a_row(const float* st, int64_t n, int64_t m, in
   return v;
 }
 
+// d(loss)/d(o) of one row from d(loss)/d(G_C, G_N, G_W) at row p.  G = H / sqrt(s(H)),
+// H = (fN (1 + tanh o1), fW (1 + tanh o2), fC):
+//   dl/dH_b = dl/dG_b / sqrt(s) - (sum_a dl/dG_a H_a) / (2 s^1.5) ds/dH_b,  dH_N/do1 = fN (1 - tanh^2 o1).
+__device__ __forceinline__ void fsai_chain(const float* st, const float* o, int64_t s, int64_t n, int64_t m, int64_t p,
+                                           float dC, float dN, float dW, float* dout) {
+  const float o1 = o ? o[s * 3 * n + n + p] : 0.f, o2 = o ? o[s * 3 * n + 2 * n + p] : 0.f;
+  const FsaiRow fr = fsai_row(st + s * 5 * n, n, m, p, o1, o2);
+  float hN_g = dN, hW_g = dW;
+  if (o) {
+    const float is = rsqrtf(fr.s);
+    const float k = 0.5f * (dC * fr.hC + dN * fr.hN + dW * fr.hW) * is * is * is;
+    hN_g = dN * is - k * 2.f * (fr.hN * fr.dN + fr.hC * fr.aN);
+    hW_g = dW * is - k * 2.f * (fr.hW * fr.dW + fr.hC * fr.aW);
+  }
+  const float t1 = tanhf(o1), t2 = tanhf(o2);
+  dout[s * 3 * n + p] = 0.f;
+  dout[s * 3 * n + n + p] = hN_g * fr.fN * (1.f - t1 * t1);
+  dout[s * 3 * n + 2 * n + p] = hW_g * fr.fW * (1.f - t2 * t2);
+}
+
+// ---- spectral (Rayleigh-quotient) loss -------------------------------------------------------
+// For a pair (r = A e, e): R = (A e)^T P (A e) / e^T A e = |G r|^2 / e^T r, the Rayleigh quotient of
+// P A in the A inner product.  loss = sum_s w_s log R_s with w_s = +1/#high for white-noise errors
+// (the top of the spectrum) and -1/#low for the smooth errors PCG leaves behind (the bottom): a
+// scale-free proxy of log cond(P A).  d log R / dG_pq = 2 t_p r_q / |t|^2 with t = G r.
+// sc[s] = e^T r, sc[S + s] = |t|^2.
+__global__ void __launch_bounds__(256) k_fsai_rq_t(const float* __restrict__ gs, const float* __restrict__ r,
+                                                   const float* __restrict__ e, int64_t m, int64_t S,
+                                                   float* __restrict__ t, double* sc) {
+  __shared__ float red[32];
+  const int64_t n = m * m;
+  const int64_t s = blockIdx.y;
+  const float* gss = gs + s * 3 * n;
+  float er = 0.f, tt = 0.f;
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+    const float tv = g_row(gss, n, m, p, r + s * n);
+    t[s * n + p] = tv;
+    er += e[s * n + p] * r[s * n + p];
+    tt += tv * tv;
+  }
+  er = block_sum(er, red);
+  tt = block_sum(tt, red);
+  if (threadIdx.x == 0) {
+    atomicAdd(sc + s, (double)er);
+    atomicAdd(sc + S + s, (double)tt);
+  }
+}
+
+__global__ void k_fsai_rq_grad(const float* __restrict__ st, const float* __restrict__ o, const float* __restrict__ r,
+                               const float* __restrict__ t, const double* __restrict__ sc,
+                               const float* __restrict__ w, int64_t m, int64_t S, float* __restrict__ dout) {
+  const int64_t n = m * m;
+  const int64_t s = blockIdx.y;
+  const float coef = (float)(2.0 * (double)w[s] / sc[S + s]);
+  const float* rs = r + s * n;
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = p / m, j = p % m;
+    const float ct = coef * t[s * n + p];
+    const float dC = ct * rs[p];
+    const float dN = i > 0 ? ct * rs[p - m] : 0.f;
+    const float dW = j > 0 ? ct * rs[p - 1] : 0.f;
+    fsai_chain(st, o, s, n, m, p, dC, dN, dW, dout);
+  }
+}
+
 // t = G r ; sc[0] += e^T r
 __global__ void __launch_bounds__(256) k_fsai_loss_t(const float* __restrict__ gs, const float* __restrict__ r,
                                                      const float* __restrict__ e, int64_t m, int64_t S,
@@ -382,13 +471,7 @@ __global__ void k_fsai_loss_grad(const float* __restrict__ st, const float* __re
     const float dC = tp * gp + u * rs[p];
     const float dN = i > 0 ? tp * gN + u * rs[p - m] : 0.f;
     const float dW = j > 0 ? tp * gW + u * rs[p - 1] : 0.f;
-    // G_C = e^o0 fC, G_N = e^o0 (1 + o1) fN, G_W = e^o0 (1 + o2) fW
-    float fN, fW, fC;
-    fsai_closed_form(st + s * 5 * n, n, m, p, fN, fW, fC);
-    const float e0 = o ? expf(o[s * 3 * n + p]) : 1.f;
-    dout[s * 3 * n + p] = dC * GC + dN * GN + dW * GW;
-    dout[s * 3 * n + n + p] = dN * e0 * fN;
-    dout[s * 3 * n + 2 * n + p] = dW * e0 * fW;
+    fsai_chain(st, o, s, n, m, p, dC, dN, dW, dout);
   }
 }
 
@@ -523,6 +606,25 @@ extern "C" int colagb_fsai_loss_grad(const float* stencil, const float* net_out,
   k_fsai_loss_v<<<grid, 256, 0, st>>>(g_stencil, t, m, S, v);
   k_fsai_loss_w<<<grid, 256, 0, st>>>(stencil, v, r, m, S, w, loss_terms);
   if (grad_out) k_fsai_loss_grad<<<grid, 256, 0, st>>>(stencil, net_out, g_stencil, r, t, w, loss_terms, m, S, grad_out);
+  COLAGB_CUDA(cudaGetLastError());
+  return COLAGB_OK;
+}
+
+extern "C" int colagb_fsai_rq_loss_grad(const float* stencil, const float* net_out, const float* g_stencil,
+                                        const float* r, const float* e, const float* weights, int64_t m, int64_t S,
+                                        float* grad_out, double* loss_terms, float* scratch, size_t scratch_bytes,
+                                        void* stream) {
+  if (!stencil || !g_stencil || !r || !e || !weights || !loss_terms || !scratch || m < 1 || S < 0)
+    return fail(COLAGB_ERR_INVALID, "colagb_fsai_rq_loss_grad: bad arguments");
+  const int64_t n = m * m;
+  if (scratch_bytes < (size_t)S * n * sizeof(float))
+    return fail(COLAGB_ERR_WORKSPACE, "colagb_fsai_rq_loss_grad: scratch too small");
+  if (S == 0) return COLAGB_OK;
+  cudaStream_t st = as_stream(stream);
+  COLAGB_CUDA(cudaMemsetAsync(loss_terms, 0, 2 * S * sizeof(double), st));
+  dim3 grid((unsigned)std::min<int64_t>(ceil_div(n, 256), 1024), (unsigned)S);
+  k_fsai_rq_t<<<grid, 256, 0, st>>>(g_stencil, r, e, m, S, scratch, loss_terms);
+  if (grad_out) k_fsai_rq_grad<<<grid, 256, 0, st>>>(stencil, net_out, r, scratch, loss_terms, weights, m, S, grad_out);
   COLAGB_CUDA(cudaGetLastError());
   return COLAGB_OK;
 }

@@ -174,6 +174,21 @@ def loss_and_grad(st, o, gst, r, e, want_grad=True):
     return loss, dout
 
 
+def rq_loss_and_grad(st, o, gst, r, e, w, want_grad=True):
+    """Spectral loss sum_s w_s log(|G r_s|^2 / e_s^T r_s) and d(loss)/d(o)."""
+    S, _, m, _ = st.shape
+    n = m * m
+    terms = torch.empty((2, S), dtype=torch.float64, device=st.device)
+    scratch = _capi.workspace(S * n * 4, st.device)
+    dout = torch.empty((S, 3, m, m), dtype=torch.float32, device=st.device) if want_grad else None
+    _capi.check(_lib().colagb_fsai_rq_loss_grad(st.data_ptr(), o.data_ptr() if o is not None else None, gst.data_ptr(),
+                                                r.data_ptr(), e.data_ptr(), w.data_ptr(), m, S,
+                                                dout.data_ptr() if dout is not None else None, terms.data_ptr(),
+                                                scratch.data_ptr(), scratch.numel(), _sp(st)), "fsai rq loss")
+    loss = (w.double() * torch.log(terms[1] / terms[0])).sum()
+    return loss, dout
+
+
 # ---------------------------------------------------------------------------------------------
 # inference and training
 
@@ -205,18 +220,32 @@ def adam_step(params, grad, m1, m2, step, lr, b1=0.9, b2=0.999, eps=1e-8):
 
 
 def train(net: FsaiNet, st_train: torch.Tensor, r_train: torch.Tensor, e_train: torch.Tensor, epochs: int = 10,
-          batch: int = 16, lr: float = 3e-3, seed: int = 0, log=print):
-    """Minimise the pair loss over training systems (stencils st_train (N, 5, m, m), pairs (N, m*m))."""
+          batch: int = 16, lr: float = 3e-3, seed: int = 0, log=print, on_epoch=None, kind=None, state=None):
+    """Minimise a loss over training systems (stencils st_train (N, 5, m, m), pairs (N, m*m)).
+    kind None: the A-norm pair loss; kind (N,) int tensor: the spectral loss with kind 1 = white-noise
+    error (top of the spectrum), 0 = smooth error (bottom); every batch holds both kinds.
+    `on_epoch(ep, mean_loss)` runs after every epoch (validation, checkpointing).  `state`: a dict
+    carrying the Adam moments and step count across calls (created when empty)."""
     N = st_train.shape[0]
-    m1 = torch.zeros_like(net.params)
-    m2 = torch.zeros_like(net.params)
+    state = {} if state is None else state
+    if "m1" not in state:
+        state.update(m1=torch.zeros_like(net.params), m2=torch.zeros_like(net.params), step=0)
+    m1, m2 = state["m1"], state["m2"]
     g = torch.Generator(device="cpu").manual_seed(seed)
-    step = 0
+    step = state["step"]
     hist = []
     for ep in range(epochs):
         perm = torch.randperm(N, generator=g)
+        if kind is not None:  # alternate the two kinds so every batch holds both
+            k_cpu = kind.cpu()
+            hi, lo = perm[k_cpu[perm] == 1], perm[k_cpu[perm] == 0]
+            q = min(hi.numel(), lo.numel())
+            perm = torch.stack([hi[:q], lo[:q]], 1).flatten()
+            N_eff = perm.numel()
+        else:
+            N_eff = N
         tot, cnt = 0.0, 0
-        for s0 in range(0, N - batch + 1, batch):
+        for s0 in range(0, N_eff - batch + 1, batch):
             idx = perm[s0: s0 + batch].to(st_train.device)
             st = st_train.index_select(0, idx).contiguous()
             r = r_train.index_select(0, idx).contiguous()
@@ -224,12 +253,22 @@ def train(net: FsaiNet, st_train: torch.Tensor, r_train: torch.Tensor, e_train: 
             acts = net.forward(features(st))
             o = acts[-1]
             gst = assemble(st, o)
-            loss, dout = loss_and_grad(st, o, gst, r, e)
+            if kind is None:
+                loss, dout = loss_and_grad(st, o, gst, r, e)
+            else:
+                kb = kind.index_select(0, idx).float()
+                nh = kb.sum().clamp_min(1.0)
+                nl = (1 - kb).sum().clamp_min(1.0)
+                w = (kb / nh - (1 - kb) / nl).contiguous()
+                loss, dout = rq_loss_and_grad(st, o, gst, r, e, w)
             grad = net.backward(acts, dout)
             step += 1
+            state["step"] = step
             adam_step(net.params, grad, m1, m2, step, lr)
             tot += float(loss)
             cnt += 1
         hist.append(tot / max(cnt, 1))
-        log(f"epoch {ep}: mean pair loss {hist[-1]:.5f}")
+        log(f"pass {ep}: mean loss {hist[-1]:.5f}")
+        if on_epoch is not None:
+            on_epoch(ep, hist[-1])
     return hist

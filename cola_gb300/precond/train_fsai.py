@@ -3,14 +3,19 @@
     python -m cola_gb300.precond.train_fsai [--train 2048] [--epochs 8] [--out path]
 
 Training data: instances with seeds 1000.. (held apart from the validation seeds 4000.. and the
-benchmark's test seeds 5000..); for each instance a pair (r, e) with r ~ N(0, 1) and e = A^-1 r
-solved by this project's batched CG (Jacobi-PCG, FP64 refinement to 1e-7).  The network, loss,
-backward and Adam all run in libcolagb kernels.
+benchmark's test seeds 5000..); for each instance the error that closed-form-FSAI PCG has left after
+150 steps (the smooth, slowly converging bottom of the spectrum) and a white-noise error (the top),
+each with its residual.  Default loss: mean log Rayleigh quotient of P A on the white-noise errors
+minus that on the smooth errors, a scale-free proxy of log cond(P A).  The network, loss, backward
+and Adam all run in libcolagb kernels.  After every epoch the validation instances are
+solved with the current factor; the weights with the fewest mean PCG iterations are kept (the
+untrained network, which reproduces closed-form FSAI, is the first candidate).
 """
 from __future__ import annotations
 
 import argparse
 import json
+import math
 import time
 
 import torch
@@ -20,37 +25,42 @@ from ..workloads import diffusion_family_2d
 from . import learned_fsai as L
 
 
-def make_pairs(seeds, m, device, chunk=256, k_steps=150):
+def make_pairs(seeds, m, device, chunk=256, k_steps=150, white=True, net=None):
     """Residual / error pairs from this project's CG: x* solves A x = b (FP64-refined), x_k is the
-    closed-form-FSAI PCG iterate after k_steps; the pair is (r_k = b - A x_k, e_k = x* - x_k), the part
-    of the error that preconditioned CG has not removed yet."""
-    sts, rs, es = [], [], []
+    PCG iterate after k_steps with the factor of `net` (closed form when None); the pair is
+    (r_k = b - A x_k, e_k = x* - x_k), the part
+    of the error that preconditioned CG has not removed yet (kind 0, the bottom of the spectrum).
+    With `white`, also a white-noise error and its residual per instance (kind 1, the top)."""
+    sts, rs, es, kinds = [], [], [], []
     for c0 in range(0, len(seeds), chunk):
         fam, B, _, _ = diffusion_family_2d(seeds[c0: c0 + chunk], m=m, device=device)
-        pat, g0 = L.g_values(fam, None)
+        pat, g0 = L.g_values(fam, net)
         X, _ = solve_batched(fam, B, precond="fsai", fsai=(pat, g0), tol=1e-9)
         Xk, _ = solve_batched(fam, B, precond="fsai", fsai=(pat, g0), tol=1e-9, max_inner_iters=k_steps,
                               fallback=False)
         E = X - Xk
         R = B - fam.matvec(Xk)
-        # plus a white-noise error per instance, so that the loss also sees the high-frequency part of
-        # the spectrum (a factor tuned only on smooth errors could inflate the largest eigenvalues)
-        W = torch.randn_like(E)
-        RW = fam.matvec(W)
+        # optionally a white-noise error per instance as well (the high-frequency part of the
+        # spectrum; the row normalisation diag(G A G^T) = 1 already bounds the largest eigenvalues)
+        pairs = [(E, R)]
+        if white:
+            W = torch.randn_like(E)
+            pairs.append((W, fam.matvec(W)))
         st = L.stencil(fam, m)
-        for e_, r_ in ((E, R), (W, RW)):
+        for kd, (e_, r_) in enumerate(pairs):
             nrm = torch.sqrt((e_ * r_).sum(dim=1, keepdim=True)).clamp_min(1e-300)  # |e|_A
             sts.append(st)
             rs.append((r_ / nrm).float().view(-1, m, m))
             es.append((e_ / nrm).float().view(-1, m, m))
-        del fam, B, X, Xk, E, R, W, RW
-    return torch.cat(sts), torch.cat(rs), torch.cat(es)
+            kinds.append(torch.full((st.shape[0],), kd, dtype=torch.int64, device=device))
+        del fam, B, X, Xk, E, R, pairs
+    return torch.cat(sts), torch.cat(rs), torch.cat(es), torch.cat(kinds)
 
 
-def evaluate(net, seeds, m, device, inner_tol=1e-4):
+def evaluate(net, seeds, m, device, inner_tol=0.1, only=("plain", "jacobi", "fsai_closed_form", "learned")):
     fam, B, _, _ = diffusion_family_2d(seeds, m=m, device=device)
     out = {}
-    for name in ["plain", "jacobi", "fsai_closed_form", "learned"]:
+    for name in only:
         kw = dict(tol=1e-8, inner_tol=inner_tol)
         if name == "plain":
             kw["precond"] = "none"
@@ -71,6 +81,49 @@ def evaluate(net, seeds, m, device, inner_tol=1e-4):
     return out
 
 
+def set_constant_output(net, o1, o2):
+    """Network weights whose output is the constant (0, o1, o2) in every cell: zero last-layer
+    weights, biases o.  The factor is then closed-form FSAI with its N and W entries scaled by
+    (1 + tanh o1), (1 + tanh o2) and every row renormalised."""
+    W, b = net.layer(len(L.LAYERS) - 1)
+    W.zero_()
+    b.copy_(torch.tensor([0.0, o1, o2], device=b.device))
+
+
+def search(net, seeds, m, device, log=print):
+    """Direct search for the over-relaxation (w_N, w_W) = (tanh o1, tanh o2) of the FSAI off-diagonals
+    that minimises the mean PCG iteration count on the given training instances: a coarse grid, then
+    compass steps with halving.  Returns (w_N, w_W, mean iterations, evaluations)."""
+    fam, B, _, _ = diffusion_family_2d(seeds, m=m, device=device)
+    cache = {}
+
+    def cost(wn, wv):
+        key = (round(wn, 4), round(wv, 4))
+        if key not in cache:
+            set_constant_output(net, math.atanh(wn), math.atanh(wv))
+            pat, gv = L.g_values(fam, net)
+            _, info = solve_batched(fam, B, precond="fsai", fsai=(pat, gv), tol=1e-8, fallback=True)
+            ok = bool(((info["status"] == 1) | (info["status"] == 5)).all())
+            cache[key] = float(info["iterations"].double().mean()) if ok else float("inf")
+            log(f"search: w_N {wn:+.3f} w_W {wv:+.3f} -> {cache[key]:.1f} mean iterations")
+        return cache[key]
+
+    grid = [-0.25, 0.0, 0.25, 0.5, 0.75, 0.9]
+    best = min(((cost(a, b), a, b) for a in grid for b in grid))
+    step = 0.125
+    while step >= 0.015:
+        moved = False
+        for da, db in ((step, 0), (-step, 0), (0, step), (0, -step)):
+            a, b = best[1] + da, best[2] + db
+            if -0.95 < a < 0.97 and -0.95 < b < 0.97:
+                c = cost(a, b)
+                if c < best[0]:
+                    best, moved = (c, a, b), True
+        if not moved:
+            step /= 2
+    return best[1], best[2], best[0], len(cache)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--train", type=int, default=2048)
@@ -78,25 +131,77 @@ def main():
     ap.add_argument("--m", type=int, default=512)
     ap.add_argument("--epochs", type=int, default=8)
     ap.add_argument("--batch", type=int, default=16)
-    ap.add_argument("--lr", type=float, default=3e-3)
+    ap.add_argument("--lr", type=float, default=1e-4)
     ap.add_argument("--out", default=str(L.WEIGHTS))
     ap.add_argument("--report", default="")
+    ap.add_argument("--search", action="store_true",
+                    help="fit the off-diagonal over-relaxation by direct search on PCG iterations "
+                         "(instances 1000 .. 1000 + --search-systems) instead of gradient training")
+    ap.add_argument("--search-systems", type=int, default=64)
+    ap.add_argument("--refresh", type=int, default=1,
+                    help="regenerate the smooth errors with the current network every this many epochs "
+                         "(0: never); the slowest modes of the current factor are what the loss must see")
+    ap.add_argument("--loss", default="spectral", choices=["spectral", "pair"],
+                    help="spectral: log Rayleigh quotient on white-noise errors minus on smooth errors "
+                         "(a log-condition proxy); pair: |P r - e|_A^2 / |e|_A^2 on the smooth errors")
     args = ap.parse_args()
     dev = torch.device("cuda")
+    if args.search:
+        net = L.FsaiNet(dev, seed=0)
+        val_seeds = list(range(4000, 4000 + args.val))
+        before = evaluate(net, val_seeds, args.m, dev)
+        t0 = time.perf_counter()
+        wn, wv, it, nev = search(net, list(range(1000, 1000 + args.search_systems)), args.m, dev)
+        t_search = time.perf_counter() - t0
+        set_constant_output(net, math.atanh(wn), math.atanh(wv))
+        torch.save(net.state_dict(), args.out)
+        after = evaluate(net, val_seeds, args.m, dev)
+        rep = {"method": "direct search of the off-diagonal over-relaxation on PCG iterations",
+               "train_instances": args.search_systems, "w_N": wn, "w_W": wv, "train_mean_iters": it,
+               "evaluations": nev, "search_seconds": t_search, "validation_before": before,
+               "validation_after": after}
+        print(json.dumps(rep, indent=1))
+        if args.report:
+            with open(args.report, "w") as f:
+                json.dump(rep, f, indent=1)
+        return
     t0 = time.perf_counter()
-    st, r, e = make_pairs(list(range(1000, 1000 + args.train)), args.m, dev)
+    st, r, e, kind = make_pairs(list(range(1000, 1000 + args.train)), args.m, dev, white=args.loss == "spectral")
+    if args.lr <= 0:
+        raise SystemExit("--lr must be positive")
     t_data = time.perf_counter() - t0
     net = L.FsaiNet(dev, seed=0)
     val_seeds = list(range(4000, 4000 + args.val))
     before = evaluate(net, val_seeds, args.m, dev)
+    best = {"epoch": -1, "mean_iters": before["learned"]["mean_iters"], "params": net.params.clone()}
+    epochs_log = []
+
+    def on_epoch(ep, loss):
+        it = evaluate(net, val_seeds, args.m, dev, only=("learned",))["learned"]["mean_iters"]
+        epochs_log.append({"epoch": ep, "loss": loss, "val_mean_iters": it})
+        print(f"epoch {ep}: validation mean PCG iterations {it:.1f} (best {best['mean_iters']:.1f})", flush=True)
+        if it < best["mean_iters"]:
+            best.update(epoch=ep, mean_iters=it, params=net.params.clone())
+
     t1 = time.perf_counter()
-    hist = L.train(net, st, r, e, epochs=args.epochs, batch=args.batch, lr=args.lr)
+    state, hist = {}, []
+    train_seeds = list(range(1000, 1000 + args.train))
+    for ep in range(args.epochs):
+        if ep > 0 and args.refresh and ep % args.refresh == 0:
+            del st, r, e, kind
+            st, r, e, kind = make_pairs(train_seeds, args.m, dev, white=args.loss == "spectral", net=net)
+        hist += L.train(net, st, r, e, epochs=1, batch=args.batch, lr=args.lr, seed=ep,
+                        on_epoch=lambda _, loss: on_epoch(ep, loss), kind=kind if args.loss == "spectral" else None,
+                        state=state)
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t1
+    net.params.copy_(best["params"])
     torch.save(net.state_dict(), args.out)
     after = evaluate(net, val_seeds, args.m, dev)
-    rep = {"train_instances": args.train, "epochs": args.epochs, "loss_history": hist, "data_seconds": t_data,
-           "train_seconds": t_train, "validation_before": before, "validation_after": after}
+    rep = {"train_instances": args.train, "epochs": args.epochs, "loss": args.loss, "lr": args.lr,
+           "loss_history": hist, "data_seconds": t_data,
+           "train_seconds": t_train, "epochs_log": epochs_log, "kept_epoch": best["epoch"],
+           "validation_before": before, "validation_after": after}
     print(json.dumps(rep, indent=1))
     if args.report:
         with open(args.report, "w") as f:

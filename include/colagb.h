@@ -315,6 +315,13 @@ int colagb_conv3x3_backward(const float* grad_out, const float* act, const float
 int colagb_fsai_loss_grad(const float* stencil, const float* net_out, const float* g_stencil, const float* r,
                           const float* e, int64_t m, int64_t S, float* grad_out, double* loss_terms, float* scratch,
                           size_t scratch_bytes, void* stream);
+/* Spectral training loss: for each pair (r = A e, e) the Rayleigh quotient R_s = |G r|^2 / e^T r of
+ * P A (P = G^T G) in the A inner product; loss = sum_s weights[s] log R_s (weights: +1/#white-noise
+ * pairs, -1/#smooth pairs -- a scale-free proxy of log cond(P A)).  loss_terms (device, 2 S doubles):
+ * e^T r, |G r|^2.  grad_out (S, 3, m, m) as for colagb_fsai_loss_grad; scratch >= S m^2 floats. */
+int colagb_fsai_rq_loss_grad(const float* stencil, const float* net_out, const float* g_stencil, const float* r,
+                             const float* e, const float* weights, int64_t m, int64_t S, float* grad_out,
+                             double* loss_terms, float* scratch, size_t scratch_bytes, void* stream);
 /* Adam update of count parameters (bias-corrected, step >= 1) */
 int colagb_adam_step(float* param, const float* grad, float* m1, float* m2, int64_t count, float lr, float beta1,
                      float beta2, float eps, int32_t step, void* stream);

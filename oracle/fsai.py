@@ -3,7 +3,8 @@ INFRASTRUCTURE ONLY (the gradient oracle for the hand-written training kernels).
 
 Uses torch CPU autograd for the derivatives; the forward follows the same equations as
 cola_gb300/csrc/fsai.cu (stencil [N, W, C, E, S] on an m x m grid, features, three 3x3 conv
-layers with ReLU, closed-form FSAI scaled by the network output, loss
+layers with ReLU, closed-form FSAI reshaped by the network output and renormalised to
+diag(G A G^T) = 1, loss
 ||G^T G r - e||_A^2 / ||e||_A^2 averaged over systems).
 """
 from __future__ import annotations
@@ -63,9 +64,21 @@ def closed_form(st):
 
 
 def assemble(st, o):
+    """H = (fN (1 + tanh o1), fW (1 + tanh o2), fC), each row renormalised so that (G A G^T)_pp = 1."""
     fN, fW, fC = closed_form(st)
-    e0 = torch.exp(o[:, 0])
-    return e0 * (1 + o[:, 1]) * fN, e0 * (1 + o[:, 2]) * fW, e0 * fC
+    hN, hW, hC = (1 + torch.tanh(o[:, 1])) * fN, (1 + torch.tanh(o[:, 2])) * fW, fC
+    C = st[:, 2]
+    dN = torch.zeros_like(C)
+    dW = torch.zeros_like(C)
+    aN = torch.zeros_like(C)
+    aW = torch.zeros_like(C)
+    dN[:, 1:, :] = C[:, :-1, :]
+    dW[:, :, 1:] = C[:, :, :-1]
+    aN[:, 1:, :] = st[:, 0, 1:, :]
+    aW[:, :, 1:] = st[:, 1, :, 1:]
+    s = hC * hC * C + hN * hN * dN + hW * hW * dW + 2 * hC * (hN * aN + hW * aW)
+    inv = 1.0 / torch.sqrt(s)
+    return hN * inv, hW * inv, hC * inv
 
 
 def apply_G(gN, gW, gC, x):
@@ -106,5 +119,24 @@ def loss_and_grads(params, st, r, e):
     o = net_forward(params, features(st))
     o.retain_grad()
     loss = pair_loss(st, o, r, e)
+    loss.backward()
+    return float(loss), params.grad.clone(), o.grad.clone(), o.detach()
+
+
+def rq_loss(st, o, r, e, w):
+    """Spectral loss sum_s w_s log(|G r_s|^2 / e_s^T r_s)."""
+    gN, gW, gC = assemble(st, o)
+    t = apply_G(gN, gW, gC, r)
+    R = (t * t).sum((1, 2)) / (e * r).sum((1, 2))
+    return (w * torch.log(R)).sum()
+
+
+def rq_loss_and_grads(params, st, r, e, w):
+    """Spectral loss, d/d(params) and d/d(o) in float64 on the CPU."""
+    params = params.detach().double().clone().requires_grad_(True)
+    st, r, e, w = st.double(), r.double(), e.double(), w.double()
+    o = net_forward(params, features(st))
+    o.retain_grad()
+    loss = rq_loss(st, o, r, e, w)
     loss.backward()
     return float(loss), params.grad.clone(), o.grad.clone(), o.detach()

@@ -101,6 +101,29 @@ def test_gradients_match_cpu_oracle(small_family):
         assert rel(grad[off: off + ln], grad_o[off: off + ln]) < 5e-3, li
 
 
+def test_spectral_loss_gradients_match_cpu_oracle(small_family):
+    """The Rayleigh-quotient (log-condition proxy) loss: value, d/d(o) and d/d(params) against float64
+    autograd, with one pair of each kind (white-noise error weighted +1, smooth error -1)."""
+    fam, _ = small_family
+    m, n, S = 16, 256, fam.num_systems
+    net = L.FsaiNet(DEV, seed=7)
+    net.params.add_(0.05 * torch.randn(net.params.shape, generator=torch.Generator().manual_seed(2)).to(DEV))
+    st = L.stencil(fam)
+    e = torch.randn((S, m, m), device=DEV)
+    e[1] = torch.linspace(0, 1, m, device=DEV)[:, None] * torch.linspace(0, 1, m, device=DEV)[None, :]  # smooth
+    r = torch.stack([OF.apply_A(st[s: s + 1].double(), e[s: s + 1].double())[0] for s in range(S)]).float()
+    w = torch.tensor([0.5, -1.0, 0.5], device=DEV)
+    acts = net.forward(L.features(st))
+    o = acts[-1]
+    gst = L.assemble(st, o)
+    loss, dout = L.rq_loss_and_grad(st, o, gst, r, e, w)
+    grad = net.backward(acts, dout)
+    loss_o, grad_o, dout_o, _ = OF.rq_loss_and_grads(net.params.cpu(), st.cpu(), r.cpu(), e.cpu(), w.cpu())
+    assert abs(float(loss) - loss_o) < 1e-4 * abs(loss_o) + 1e-5
+    assert rel(dout, dout_o) < 2e-3
+    assert rel(grad, grad_o) < 2e-3
+
+
 def test_adam_step():
     p = torch.randn(1000, device=DEV)
     g = torch.randn(1000, device=DEV)
@@ -137,8 +160,8 @@ def test_training_reduces_loss_and_preconditioner_converges():
 
 @pytest.mark.skipif(not L.WEIGHTS.exists(), reason="trained weights not present")
 def test_trained_network_beats_jacobi_on_held_out_512():
-    """What the trained network gains over the method without it (Jacobi-PCG), measured in CG
-    iterations on held-out 512 x 512 instances (seeds never used in training)."""
+    """What the shipped factor gains over Jacobi-PCG and over closed-form FSAI, measured in CG
+    iterations on held-out 512 x 512 instances (seeds never used in fitting)."""
     fam, B, _, _ = diffusion_family_2d(list(range(4100, 4108)), m=512, device=DEV)
     net = L.FsaiNet.load(device=DEV)
     _, ij = solve_batched(fam, B, precond="jacobi", tol=1e-8)
@@ -147,3 +170,7 @@ def test_trained_network_beats_jacobi_on_held_out_512():
     it_j = float(ij["iterations"].double().mean())
     it_l = float(il["iterations"].double().mean())
     assert it_l < 0.8 * it_j, (it_l, it_j)
+    # and over closed-form FSAI on the same pattern (the fitted over-relaxation of its off-diagonals)
+    _, ic = solve_batched(fam, B, precond="fsai", fsai=L.g_values(fam, None), tol=1e-8)
+    it_c = float(ic["iterations"].double().mean())
+    assert it_l < it_c, (it_l, it_c)
