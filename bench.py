@@ -180,6 +180,11 @@ def make_preconditioner(method, fam, coeff, dev):
 
 
 PRECOND = {"plain": "none", "jacobi": "jacobi", "learned": "fsai", "fsai": "fsai"}
+# DRAM bytes (read + write) of one on-chip solve launch per system, from one ncu capture of
+# k_onchip_pcg on 7 systems of this workload (FSAI, ~1030 steps each): 362.2 MB + 197.1 MB.  DRAM
+# traffic is per system (reading its CSR values and right-hand side, writing its diagonals and x):
+# the diagonals of the systems in flight are re-read from L2 at every step.
+ONCHIP_DRAM_BYTES_PER_SYSTEM = 559.2e6 / 7
 KERNEL_OF = {"onchip": "k_onchip_pcg", "cluster8": "k_cluster_pcg", "cluster16": "k_cluster_pcg",
              "grid": "k_batched_ir"}
 
@@ -288,7 +293,11 @@ def run_ours(args, world, rank, local):
                     "max_fp64_replacements": max(sweeps)},
         "e2e": e2e,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                     "frac": achieved / peak,
+                     "traffic": ONCHIP_DRAM_BYTES_PER_SYSTEM * args.systems if sched_ran == "onchip" else None,
+                     "traffic_note": "ncu DRAM bytes of a 7-system capture scaled by systems" if sched_ran == "onchip"
+                                     else None,
+                     "peak_kind": peak_kind,
                      "kernel": KERNEL_OF.get(sched_ran, "k_cluster_pcg"), "schedule": sched_ran,
                      "alg_bytes_per_launch": alg_bytes_step},
         "gpu_launches": args.steps * launches_per_solve(sched_ran, method, args.systems),
