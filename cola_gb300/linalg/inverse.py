@@ -40,7 +40,21 @@ class IterativeOperatorWInfo(O.LinearOperator):
 
 def cg(A: O.LinearOperator, rhs: torch.Tensor, x0=None, P=None, tol=1e-6, max_iters=5000, pbar=False,
        check_every: int = 16, allow_fused: bool = True):
-    """Solve A X = B by CG (cg.py:39-69).  Returns (solution, info)."""
+    """Solve A X = B by CG (cg.py:39-69).  Returns (solution, info).
+
+    Differentiable in ``rhs`` and in the operator's tensors with the reference's rule (cg_bwd,
+    cg.py:72-86): the adjoint is one more CG solve with the same tolerance, iterations and P."""
+    from .autodiff import cg_with_grad, wants_grad
+    if wants_grad(A, rhs):
+        def solve(b, first=[True]):
+            use_x0 = x0 if first[0] else None
+            first[0] = False
+            return _cg_device(A, b.detach(), use_x0, P, tol, max_iters, check_every, allow_fused)
+        return cg_with_grad(A, rhs, solve)
+    return _cg_device(A, rhs, x0, P, tol, max_iters, check_every, allow_fused)
+
+
+def _cg_device(A, rhs, x0, P, tol, max_iters, check_every, allow_fused):
     low = lower(A)
     dev = operator_device(A, low)
     _capi.require_cuda(rhs)

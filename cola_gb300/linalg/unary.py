@@ -264,18 +264,29 @@ def stochastic_lanczos_quad(A: O.LinearOperator, fun: Callable, max_iters: int =
                             pbar: bool = False, key=None, probes: torch.Tensor | None = None):
     """tr f(A) ~ n * mean_b sum_j tau_bj^2 f(lambda_bj) over Gaussian probes (tbd/slq.py:37-75).
 
-    ``probes`` (n, num_samples) may be passed to reuse identical probe vectors."""
+    ``probes`` (n, num_samples) may be passed to reuse identical probe vectors.  Differentiable in
+    the operator's tensors with the reference's backward rule (that of f = log)."""
     num_samples = max(int(1 / vtol**2), 1)
     n = A.shape[0]
     if probes is None:
         key = PRNGKey(0) if key is None else key
         probes = randn(n, num_samples, dtype=A.dtype, key=key)
     probes = probes.to(A.device)
-    res = run_lanczos(A, probes, min(int(max_iters), n), tol)
-    alpha, beta, _ = res.alpha_beta_q()
-    evals, first, _ = tridiag_eigh(beta, alpha, want_vectors=False)
-    eps = torch.finfo(A.dtype).eps
-    const = 10 * eps * evals.max(dim=1, keepdim=True).values
-    fv = torch.where(evals.abs() > const, fun(evals), torch.zeros_like(evals))
-    approx = (first**2 * fv).sum(-1)
-    return (n * approx).mean()
+
+    def forward():
+        res = run_lanczos(A, probes, min(int(max_iters), n), tol)
+        alpha, beta, _ = res.alpha_beta_q()
+        evals, first, _ = tridiag_eigh(beta, alpha, want_vectors=False)
+        eps = torch.finfo(A.dtype).eps
+        const = 10 * eps * evals.max(dim=1, keepdim=True).values
+        fv = torch.where(evals.abs() > const, fun(evals), torch.zeros_like(evals))
+        approx = (first**2 * fv).sum(-1)
+        return (n * approx).mean()
+
+    from .autodiff import slq_with_grad, wants_grad
+    if wants_grad(A):
+        # backward of the reference (slq_bwd, tbd/slq.py:10-31): the rule of f = log, A^-1 z_i by CG
+        # with tol 1e-6 and 100 iterations on the forward's own probes
+        from .inverse import cg
+        return slq_with_grad(A, probes, forward, lambda Z: cg(A, Z, tol=1e-6, max_iters=100)[0])
+    return forward()
