@@ -18,6 +18,8 @@
 //     evaluated on the device and the host polls it every `check_every` steps (the reference
 //     syncs twice per step, torch_tqdm.py:42 and cg.py:136).
 // Column sums are reduced in a fixed order so every CTA derives bit-identical alpha / beta.
+#include <cooperative_groups.h>
+
 #include <cmath>
 #include <mutex>
 #include <type_traits>
@@ -62,11 +64,15 @@ __device__ __forceinline__ void block_col_partials(int64_t row_base, int64_t row
     }
     smem[t] = acc;
     __syncthreads();
-    if (t < kc) {
-      T s = T(0);
-      for (int q = 0; q < rpp; ++q) s += smem[q * kc + t];
-      partials_out[c0 + t] = s;
+    // tree over the rpp row slots of each column (a serial sum by one thread per column costs
+    // ~rpp dependent shared-memory round trips, 256 of them for a single right-hand side)
+    for (int w = rpp; w > 1;) {
+      const int h = (w + 1) >> 1;
+      if (my_r < w - h) smem[t] += smem[t + h * kc];
+      __syncthreads();
+      w = h;
     }
+    if (t < kc) partials_out[c0 + t] = smem[t];
     __syncthreads();
   }
 }
@@ -77,6 +83,32 @@ __device__ __forceinline__ T sum_partials(const T* partials, int nb, int64_t k, 
   T s = T(0);
   for (int b = 0; b < nb; ++b) s += ldcg(partials + (int64_t)b * k + c);
   return s;
+}
+
+// Sum of column c of the per-CTA partials, formed by the whole block (every thread gets it).
+template <class T>
+__device__ __forceinline__ T block_total(const T* partials, int nb, int64_t k, int64_t c, T* red) {
+  T v = T(0);
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) v += ldcg(partials + (int64_t)b * k + c);
+  return block_sum(v, red);
+}
+
+// Column totals of the per-CTA partials for the first kStage columns, block-parallel, into shared
+// memory (one thread summing nb partials from L2 in sequence costs nb dependent round trips);
+// total_at reads them, summing serially only for columns beyond kStage.
+constexpr int kStage = 64;
+template <class T>
+__device__ __forceinline__ void stage_totals(const T* partials, int nb, int64_t k, T* tot, T* red) {
+  const int64_t kk = k < kStage ? k : kStage;
+  for (int64_t c = 0; c < kk; ++c) {
+    const T v = block_total(partials, nb, k, c, red);
+    if (threadIdx.x == 0) tot[c] = v;
+  }
+  __syncthreads();
+}
+template <class T>
+__device__ __forceinline__ T total_at(const T* partials, int nb, int64_t k, int64_t c, const T* tot) {
+  return c < kStage ? tot[c] : sum_partials(partials, nb, k, c);
 }
 
 __device__ __forceinline__ bool is_last_block(unsigned int* counter) {
@@ -118,7 +150,9 @@ __global__ void __launch_bounds__(256) k_colnorm_b(const T* B, int64_t ldb, int6
                         [&](int64_t i, int64_t c) { const T v = B[i * ldb + c]; return v * v; },
                         s.pA + (int64_t)blockIdx.x * k, smem);
   if (is_last_block(s.counters + 0)) {
-    for (int64_t c = threadIdx.x; c < k; c += blockDim.x) s.mult[c] = sqrt(sum_partials(s.pA, gridDim.x, k, c));
+    __shared__ T totA[kStage], red[32];
+    stage_totals(s.pA, gridDim.x, k, totA, red);
+    for (int64_t c = threadIdx.x; c < k; c += blockDim.x) s.mult[c] = sqrt(total_at(s.pA, gridDim.x, k, c, totA));
     if (threadIdx.x == 0) s.counters[0] = 0;
   }
 }
@@ -151,11 +185,14 @@ __global__ void __launch_bounds__(256) k_init(const T* R, const T* Z, const T* d
   if (is_last_block(s.counters + 1)) {
     __shared__ int s_any;
     __shared__ T s_mean;
+    __shared__ T totB[kStage], totC[kStage], red[32];
+    stage_totals(s.pB, gridDim.x, k, totB, red);
+    stage_totals(s.pC, gridDim.x, k, totC, red);
     if (threadIdx.x == 0) { s_any = 0; s_mean = T(0); }
     __syncthreads();
     for (int64_t c = threadIdx.x; c < k; c += blockDim.x) {
-      const T g = sum_partials(s.pB, gridDim.x, k, c);
-      const T rn = sqrt(sum_partials(s.pC, gridDim.x, k, c));
+      const T g = total_at(s.pB, gridDim.x, k, c, totB);
+      const T rn = sqrt(total_at(s.pC, gridDim.x, k, c, totC));
       s.gamma[c] = g;
       s.rnorm[c] = rn;
       s.alpha[c] = T(0);
@@ -185,10 +222,12 @@ __global__ void __launch_bounds__(256) k_alpha(const T* P, const T* AP, int64_t 
                         [&](int64_t i, int64_t c) { return P[i * k + c] * AP[i * k + c]; },
                         s.pA + (int64_t)blockIdx.x * k, smem);
   if (is_last_block(s.counters + 2)) {
+    __shared__ T totA[kStage], red[32];
+    stage_totals(s.pA, gridDim.x, k, totA, red);
     for (int64_t c = threadIdx.x; c < k; c += blockDim.x) {
       const int cv = s.rnorm[c] < SmallValue<T>::v;
       s.conv[c] = cv;
-      const T a = safe_div(s.gamma[c], sum_partials(s.pA, gridDim.x, k, c));
+      const T a = safe_div(s.gamma[c], total_at(s.pA, gridDim.x, k, c, totA));
       s.alpha[c] = cv ? T(0) : a;
     }
     if (threadIdx.x == 0) s.counters[2] = 0;
@@ -220,21 +259,26 @@ __global__ void __launch_bounds__(256) k_update(T* X, int64_t ldx, T* R, const T
                           s.pB + (int64_t)blockIdx.x * k, smem);
   if (PK == 2) {
     if (is_last_block(s.counters + 3)) {
-      for (int64_t c = threadIdx.x; c < k; c += blockDim.x) s.rnorm[c] = sqrt(sum_partials(s.pC, gridDim.x, k, c));
+      __shared__ T totC2[kStage], red2[32];
+      stage_totals(s.pC, gridDim.x, k, totC2, red2);
+      for (int64_t c = threadIdx.x; c < k; c += blockDim.x) s.rnorm[c] = sqrt(total_at(s.pC, gridDim.x, k, c, totC2));
       if (threadIdx.x == 0) s.counters[3] = 0;
     }
     return;
   }
   if (is_last_block(s.counters + 3)) {
     __shared__ int s_any;
+    __shared__ T totB[kStage], totC[kStage], red[32];
+    stage_totals(s.pB, gridDim.x, k, totB, red);
+    stage_totals(s.pC, gridDim.x, k, totC, red);
     if (threadIdx.x == 0) s_any = 0;
     __syncthreads();
     for (int64_t c = threadIdx.x; c < k; c += blockDim.x) {
-      const T g1 = sum_partials(s.pB, gridDim.x, k, c);
+      const T g1 = total_at(s.pB, gridDim.x, k, c, totB);
       const T b = safe_div(g1, s.gamma[c]);
       s.beta[c] = s.conv[c] ? T(0) : b;
       s.gamma[c] = g1;
-      const T rn = sqrt(sum_partials(s.pC, gridDim.x, k, c));
+      const T rn = sqrt(total_at(s.pC, gridDim.x, k, c, totC));
       s.rnorm[c] = rn;
       if (rn > s.tol_eff[c]) atomicOr(&s_any, 1);
     }
@@ -264,10 +308,12 @@ __global__ void __launch_bounds__(256) k_gamma(const T* R, const T* Z, int64_t n
                         s.pB + (int64_t)blockIdx.x * k, smem);
   if (is_last_block(s.counters + 2)) {
     __shared__ int s_any;
+    __shared__ T totB[kStage], red[32];
+    stage_totals(s.pB, gridDim.x, k, totB, red);
     if (threadIdx.x == 0) s_any = 0;
     __syncthreads();
     for (int64_t c = threadIdx.x; c < k; c += blockDim.x) {
-      const T g1 = sum_partials(s.pB, gridDim.x, k, c);
+      const T g1 = total_at(s.pB, gridDim.x, k, c, totB);
       const T b = safe_div(g1, s.gamma[c]);
       s.beta[c] = s.conv[c] ? T(0) : b;
       s.gamma[c] = g1;
@@ -355,7 +401,42 @@ __device__ __forceinline__ void own_matvec(const FusedArgs<T, S>& a, const T* V,
     }
   } else {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int64_t i = r0 + warp; i < r1; i += nw) {
+    int64_t i_rest = r0;
+    if constexpr (std::is_same<S, float>::value && std::is_same<T, float>::value) {
+      if (a.vec4 && k == 1) {
+        // four rows per warp at a time: one vector load feeds four matrix-row loads, so each lane
+        // keeps ~20 128-bit loads in flight (the row-at-a-time loop left the SM latency-bound);
+        // each row's sum runs in the same order as the one-row loop below
+        const float4* v4 = reinterpret_cast<const float4*>(V);
+        const int64_t n4 = n / 4, l4 = a.lda / 4;
+        const int64_t nfull = r0 + (r1 - r0) / 4 * 4;
+        for (int64_t i = r0 + 4 * warp; i < nfull; i += 4 * nw) {
+          const float4* ra = reinterpret_cast<const float4*>(a.vals + i * a.lda);
+          float c0 = 0.f, c1 = 0.f, c2 = 0.f, c3 = 0.f;
+#pragma unroll 4
+          for (int64_t j = lane; j < n4; j += 32) {
+            const float4 vv = v4[j];
+            const float4 q0 = ra[j], q1 = ra[l4 + j], q2 = ra[2 * l4 + j], q3 = ra[3 * l4 + j];
+            c0 += q0.x * vv.x + q0.y * vv.y + q0.z * vv.z + q0.w * vv.w;
+            c1 += q1.x * vv.x + q1.y * vv.y + q1.z * vv.z + q1.w * vv.w;
+            c2 += q2.x * vv.x + q2.y * vv.y + q2.z * vv.z + q2.w * vv.w;
+            c3 += q3.x * vv.x + q3.y * vv.y + q3.z * vv.z + q3.w * vv.w;
+          }
+          c0 = warp_sum(c0);
+          c1 = warp_sum(c1);
+          c2 = warp_sum(c2);
+          c3 = warp_sum(c3);
+          if (lane == 0) {
+            OUT[i] = c0 + a.shift * V[i];
+            OUT[i + 1] = c1 + a.shift * V[i + 1];
+            OUT[i + 2] = c2 + a.shift * V[i + 2];
+            OUT[i + 3] = c3 + a.shift * V[i + 3];
+          }
+        }
+        i_rest = nfull;
+      }
+    }
+    for (int64_t i = i_rest + warp; i < r1; i += nw) {
       const S* row = a.vals + i * a.lda;
       for (int64_t c = 0; c < k; ++c) {
         T acc = T(0);
@@ -383,16 +464,33 @@ __device__ __forceinline__ void own_matvec(const FusedArgs<T, S>& a, const T* V,
 
 // Every CTA computes the column totals itself from the per-CTA partials (same order everywhere).
 template <class T>
-__device__ __forceinline__ void all_totals(const T* partials, int nb, int64_t k, T* out_smem) {
-  for (int64_t c = threadIdx.x; c < k; c += blockDim.x) out_smem[c] = sum_partials(partials, nb, k, c);
+__device__ __forceinline__ void all_totals(const T* partials, int nb, int64_t k, T* out_smem, T* red) {
+  // block-parallel per column (k <= 64 on the fused path): every CTA forms the same totals
+  for (int64_t c = 0; c < k; ++c) {
+    const T v = block_total(partials, nb, k, c, red);
+    if (threadIdx.x == 0) out_smem[c] = v;
+  }
   __syncthreads();
 }
 
-template <class T, class S, int PK>
-__global__ void __launch_bounds__(256) k_cg_fused(FusedArgs<T, S> a) {
+// Barrier between the phases of the fused kernel: the cooperative grid's bounded software barrier,
+// or -- when the whole grid is one thread-block cluster -- the hardware cluster barrier
+// (release/acquire at cluster scope, global memory included).
+template <bool CLUSTER>
+__device__ __forceinline__ bool phase_sync(const GridBarrier& gb) {
+  if constexpr (CLUSTER) {
+    cooperative_groups::this_cluster().sync();
+    return true;
+  } else {
+    return grid_sync(gb);
+  }
+}
+
+template <class T, class S, int PK, bool CLUSTER>
+__global__ void __launch_bounds__(CLUSTER ? 512 : 256) k_cg_fused(FusedArgs<T, S> a) {
   extern __shared__ unsigned char smem_raw[];
-  T* red = reinterpret_cast<T*>(smem_raw);           // 256 reduction slots
-  T* tot1 = red + 256;                                // k column totals
+  T* red = reinterpret_cast<T*>(smem_raw);           // blockDim.x reduction slots
+  T* tot1 = red + blockDim.x;                         // k column totals
   T* tot2 = tot1 + a.k;                               // k column totals
   T* alpha = tot2 + a.k;                              // k
   T* beta = alpha + a.k;                              // k
@@ -418,20 +516,20 @@ __global__ void __launch_bounds__(256) k_cg_fused(FusedArgs<T, S> a) {
 
   // ---- init: mult = |b| ----
   own_partials([&](int64_t i, int64_t c) { const T v = a.B[i * a.ldb + c]; return v * v; }, pA);
-  if (!grid_sync(a.gb)) return;
-  all_totals(a.s.pA, nb, k, tot1);
+  if (!phase_sync<CLUSTER>(a.gb)) return;
+  all_totals(a.s.pA, nb, k, tot1, red);
   for (int64_t c = threadIdx.x; c < k; c += blockDim.x) mult[c] = sqrt(tot1[c]);
   __syncthreads();
   // r = b / mult - A x0 (x0 gathered through P as scratch: P <- x0 first)
   for (int64_t i = r0; i < r1; ++i)
     for (int64_t c = threadIdx.x; c < k; c += blockDim.x) a.P[i * k + c] = a.X[i * a.ldx + c];
-  if (!grid_sync(a.gb)) return;
+  if (!phase_sync<CLUSTER>(a.gb)) return;
   own_matvec(a, a.P, a.AP, r0, r1);
   for (int64_t u = threadIdx.x; u < (r1 - r0) * k; u += blockDim.x) {
     const int64_t i = r0 + u / k, c = u % k;
     a.R[i * k + c] = safe_div(a.B[i * a.ldb + c], mult[c]) - a.AP[i * k + c];
   }
-  if (!grid_sync(a.gb)) return;  // everyone done reading x0 out of P
+  if (!phase_sync<CLUSTER>(a.gb)) return;  // everyone done reading x0 out of P
   own_partials([&](int64_t i, int64_t c) {
     const T r = a.R[i * k + c];
     const T z = PK == 0 ? r : a.dinv[i] * r;
@@ -439,9 +537,9 @@ __global__ void __launch_bounds__(256) k_cg_fused(FusedArgs<T, S> a) {
     return r * z;
   }, pB);
   own_partials([&](int64_t i, int64_t c) { const T r = a.R[i * k + c]; return r * r; }, pC);
-  if (!grid_sync(a.gb)) return;
-  all_totals(a.s.pB, nb, k, tot1);
-  all_totals(a.s.pC, nb, k, tot2);
+  if (!phase_sync<CLUSTER>(a.gb)) return;
+  all_totals(a.s.pB, nb, k, tot1, red);
+  all_totals(a.s.pC, nb, k, tot2, red);
   if (threadIdx.x == 0) s_any = 0;
   __syncthreads();
   for (int64_t c = threadIdx.x; c < k; c += blockDim.x) {
@@ -466,8 +564,8 @@ __global__ void __launch_bounds__(256) k_cg_fused(FusedArgs<T, S> a) {
     // ---- phase A: Ap = A p, <p, Ap> ----
     own_matvec(a, a.P, a.AP, r0, r1);
     own_partials([&](int64_t i, int64_t c) { return a.P[i * k + c] * a.AP[i * k + c]; }, pA);
-    if (!grid_sync(a.gb)) return;
-    all_totals(a.s.pA, nb, k, tot1);
+    if (!phase_sync<CLUSTER>(a.gb)) return;
+    all_totals(a.s.pA, nb, k, tot1, red);
     for (int64_t c = threadIdx.x; c < k; c += blockDim.x) alpha[c] = conv[c] ? T(0) : safe_div(gamma[c], tot1[c]);
     __syncthreads();
     // ---- phase B: x, r updates, <r, z>, |r|^2 ----
@@ -482,9 +580,9 @@ __global__ void __launch_bounds__(256) k_cg_fused(FusedArgs<T, S> a) {
       const T r = a.R[i * k + c];
       return r * (PK == 0 ? r : a.dinv[i] * r);
     }, pB);
-    if (!grid_sync(a.gb)) return;
-    all_totals(a.s.pB, nb, k, tot1);
-    all_totals(a.s.pC, nb, k, tot2);
+    if (!phase_sync<CLUSTER>(a.gb)) return;
+    all_totals(a.s.pB, nb, k, tot1, red);
+    all_totals(a.s.pC, nb, k, tot2, red);
     if (threadIdx.x == 0) s_any = 0;
     __syncthreads();
     for (int64_t c = threadIdx.x; c < k; c += blockDim.x) {
@@ -513,7 +611,7 @@ __global__ void __launch_bounds__(256) k_cg_fused(FusedArgs<T, S> a) {
       const T z = PK == 0 ? r : a.dinv[i] * r;
       a.P[i * k + c] = z + beta[c] * a.P[i * k + c];
     }
-    if (!grid_sync(a.gb)) return;
+    if (!phase_sync<CLUSTER>(a.gb)) return;
   }
   // ---- x *= mult ----
   for (int64_t u = threadIdx.x; u < (r1 - r0) * k; u += blockDim.x) {
@@ -565,7 +663,7 @@ template <class T, class S, int PK>
 static int fused_blocks_for() {
   int occ = 0;
   const size_t smem = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cg_fused<T, S, PK>, 256, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cg_fused<T, S, PK, false>, 256, smem);
   if (occ < 1) occ = 1;
   return num_sms() * (occ < 2 ? occ : 2);
 }
@@ -688,6 +786,20 @@ static int run_generic(const colagb_op* A, const colagb_op* P, const CgPlan& pl,
   return COLAGB_OK;
 }
 
+// Step count and barrier status of a finished fused solve.
+template <class T>
+static int finish_fused(const CgScalars<T>& s, colagb_cg_result* res, cudaStream_t st) {
+  int h[2] = {0, 0};
+  COLAGB_CUDA(cudaMemcpyAsync(&h[0], s.iters, sizeof(int), cudaMemcpyDeviceToHost, st));
+  COLAGB_CUDA(cudaMemcpyAsync(&h[1], s.counters + 6, sizeof(int), cudaMemcpyDeviceToHost, st));
+  COLAGB_CUDA(cudaStreamSynchronize(st));
+  res->iterations = h[0];
+  res->fused = 1;
+  res->status = h[1];
+  if (h[1] != 0) return fail(COLAGB_ERR_TIMEOUT, "fused CG: a grid barrier timed out");
+  return COLAGB_OK;
+}
+
 template <class T, class S, int PK>
 static int run_fused(const CgPlan& pl, const T* B, int64_t ldb, T* X, int64_t ldx, const colagb_cg_params& prm, T* hist,
                      CgScalars<T> s, T* R, T* Pv, T* AP, colagb_cg_result* res, cudaStream_t st) {
@@ -720,24 +832,53 @@ static int run_fused(const CgPlan& pl, const T* B, int64_t ldb, T* X, int64_t ld
   a.gb.err = reinterpret_cast<int*>(s.counters + 6);
   a.gb.spin_limit = prm.spin_limit > 0 ? prm.spin_limit : kDefaultSpinLimit;
   const size_t smem = 256 * sizeof(T) + 7 * (size_t)pl.k * sizeof(T) + (size_t)pl.k * sizeof(int);
+  const size_t smem512 = smem + 256 * sizeof(T);  // the cluster variant runs 512 threads per CTA
+  // An operator of at most ~32 MB is streamed from L2 by one 16-CTA cluster faster than the whole
+  // grid can pass three software grid barriers per step (measured: 2048 x 2048 FP32, ~24 us per step
+  // on 64 CTAs); larger operators use the cooperative grid (HBM-bound).
+  const double abytes0 = leaf->kind == COLAGB_OP_DENSE ? (double)leaf->rows * (double)leaf->cols * sizeof(S)
+                                                       : (double)leaf->nnz * (double)(sizeof(S) + 4);
+  if (abytes0 <= 32.0 * 1024 * 1024 && pl.fused_blocks >= 16) {
+    a.gb.nblocks = 16;
+    COLAGB_CUDA(cudaFuncSetAttribute(k_cg_fused<T, S, PK, true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 16;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cfg.gridDim = dim3(16);
+    cfg.blockDim = dim3(512);
+    cfg.dynamicSmemBytes = smem512;
+    cfg.stream = st;
+    int ncl = 0;
+    if (cudaOccupancyMaxActiveClusters(&ncl, k_cg_fused<T, S, PK, true>, &cfg) == cudaSuccess && ncl >= 1) {
+      COLAGB_CUDA(cudaMemsetAsync(s.counters, 0, 8 * sizeof(unsigned int), st));
+      COLAGB_CUDA(cudaLaunchKernelEx(&cfg, k_cg_fused<T, S, PK, true>, a));
+      return finish_fused(s, res, st);
+    }
+    cudaGetLastError();
+  }
   int occ = 0;
-  COLAGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cg_fused<T, S, PK>, 256, smem));
+  COLAGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cg_fused<T, S, PK, false>, 256, smem));
   if (occ < 1) return fail(COLAGB_ERR_UNSUPPORTED, "fused CG kernel cannot be resident");
-  const int nb = num_sms() * (occ < 2 ? occ : 2);
+  // Grid sized to the operator: ~256 KB of matrix per CTA (at least 16 CTAs).  Every step ends in
+  // three grid barriers whose arrivals are atomics on one word, so a CTA with only a few rows of a
+  // small matrix costs more in barrier time than it saves in streaming time (n = 2048 dense: 64
+  // CTAs instead of two per SM).
+  const int nb_max = num_sms() * (occ < 2 ? occ : 2);
+  const double abytes = leaf->kind == COLAGB_OP_DENSE ? (double)leaf->rows * (double)leaf->cols * sizeof(S)
+                                                      : (double)leaf->nnz * (double)(sizeof(S) + 4);
+  const double want = abytes / (256.0 * 1024.0);
+  const int nb = (int)(want < 16.0 ? 16.0 : (want > (double)nb_max ? (double)nb_max : want + 0.999));
   if (nb > pl.fused_blocks) return fail(COLAGB_ERR_WORKSPACE, "fused CG block count exceeds planned partials");
   a.gb.nblocks = (unsigned)nb;
   COLAGB_CUDA(cudaMemsetAsync(s.counters, 0, 8 * sizeof(unsigned int), st));
   void* args[] = {&a};
-  COLAGB_CUDA(cudaLaunchCooperativeKernel((const void*)k_cg_fused<T, S, PK>, dim3(nb), dim3(256), args, smem, st));
-  int h[3] = {0, 0, 0};
-  COLAGB_CUDA(cudaMemcpyAsync(&h[0], s.iters, sizeof(int), cudaMemcpyDeviceToHost, st));
-  COLAGB_CUDA(cudaMemcpyAsync(&h[1], s.counters + 6, sizeof(int), cudaMemcpyDeviceToHost, st));
-  COLAGB_CUDA(cudaStreamSynchronize(st));
-  res->iterations = h[0];
-  res->fused = 1;
-  res->status = h[1];
-  if (h[1] != 0) return fail(COLAGB_ERR_TIMEOUT, "fused CG: a grid barrier timed out");
-  return COLAGB_OK;
+  COLAGB_CUDA(cudaLaunchCooperativeKernel((const void*)k_cg_fused<T, S, PK, false>, dim3(nb), dim3(256), args, smem, st));
+  return finish_fused(s, res, st);
 }
 
 template <class T>
