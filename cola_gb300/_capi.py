@@ -103,6 +103,8 @@ SIGNATURES = {
     "colagb_cg_dense_batched_solve": (C.c_int, [_i64, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _d, _i32, _vp, _vp, _vp,
                                                 _sz, _vp]),
     "colagb_lanczos_workspace_bytes": (C.c_int, [_vp, _i64, _i32, _P(_sz)]),
+    "colagb_arnoldi_workspace_bytes": (C.c_int, [_vp, _i64, _i32, _P(_sz)]),
+    "colagb_arnoldi": (C.c_int, [_vp, _vp, _i64, _i64, _P(LanczosParams), _vp, _vp, _P(_i32), _vp, _sz, _vp]),
     "colagb_lanczos": (C.c_int, [_vp, _vp, _i64, _i64, _P(LanczosParams), _vp, _vp, _vp, _P(_i32), _vp, _sz,
                                  _vp]),
     "colagb_basis_combine": (C.c_int, [_vp, _i64, _i64, _i32, _vp, _i64, _vp, _i32, _vp]),

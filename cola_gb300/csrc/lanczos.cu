@@ -457,6 +457,116 @@ static int lanczos_t(const colagb_op* A, const T* V0, int64_t ldv0, int64_t bs, 
   return COLAGB_OK;
 }
 
+
+// ---- Arnoldi (arnoldi.py:303-334) on the same basis slots: Q[j] lives in slot j + 1 ----------
+// H is (bs, max_iters + 1, max_iters) row-major; column idx = step - 1 collects the projection
+// coefficients of both Gram-Schmidt passes and, below them, |w|.
+template <class T>
+__global__ void k_ar_accum_h(T* H, int64_t bs, int max_iters, int first_pass, LzState<T> s) {
+  if (*s.done) return;
+  const int i = *s.step;  // slots 1..i were projected out: rows 0..i-1 of column i-1
+  const int idx = i - 1;
+  const int64_t total = (int64_t)i * bs;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < total; u += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = u / bs, b = u % bs;
+    T* h = H + (b * (max_iters + 1) + j) * max_iters + idx;
+    const T c = s.hbuf[(j + 1) * bs + b];
+    *h = first_pass ? c : *h + c;
+  }
+}
+
+// w /= max(|w|, tol / 2)  (the new basis vector; |w| from k_lz_norm)
+template <class T>
+__global__ void k_ar_scale_clip(T* w, int64_t n, int64_t bs, double tol, LzState<T> s) {
+  if (*s.done) return;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n * bs; u += (int64_t)gridDim.x * blockDim.x) {
+    const T nv = s.nrm[u % bs];
+    w[u] = w[u] / (nv > (T)(tol / 2) ? nv : (T)(tol / 2));
+  }
+}
+
+// H[b][idx + 1][idx] = |w| ; idx += 1 ; stop test of arnoldi_fact.cond_fun:
+// continue while idx < max_iters and (any |w| > tol * H[b][1][0] or idx <= 0)
+template <class T>
+__global__ void k_ar_finish(T* H, int64_t bs, int max_iters, double tol, LzState<T> s) {
+  if (*s.done) return;
+  __shared__ int s_any;
+  const int i = *s.step;
+  const int idx = i - 1;
+  if (threadIdx.x == 0) s_any = 0;
+  __syncthreads();
+  for (int64_t b = threadIdx.x; b < bs; b += blockDim.x) {
+    const T nv = s.nrm[b];
+    H[(b * (max_iters + 1) + idx + 1) * max_iters + idx] = nv;
+    const T h10 = H[(b * (max_iters + 1) + 1) * max_iters + 0];
+    if (nv > (T)tol * h10) atomicOr(&s_any, 1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int nidx = idx + 1;
+    *s.step = nidx + 1;
+    *s.done = !(nidx < max_iters && (s_any || nidx <= 0));
+  }
+}
+
+template <class T>
+static int arnoldi_t(const colagb_op* A, const T* V0, int64_t ldv0, int64_t bs, const colagb_lanczos_params& prm,
+                     T* basis, T* H, int32_t* steps, void* workspace, size_t ws_bytes, cudaStream_t st) {
+  const int64_t n = A->nodes[A->root].rows;
+  const int m = prm.max_iters;
+  const int64_t slots = (int64_t)m + 2;
+  const int nb = lz_blocks(n, bs);
+  Bump ws(workspace, ws_bytes);
+  LzState<T> s = lz_carve<T>(ws, bs, m, nb);
+  size_t opb = 0;
+  COLAGB_TRY(colagb_matmat_workspace_bytes(A, bs, &opb));
+  void* opws = ws.take<char>(opb > 0 ? opb : 1);
+  if (workspace == nullptr || ws.overflow())
+    return fail(COLAGB_ERR_WORKSPACE, "colagb_arnoldi: workspace too small (need " + std::to_string(ws.peak) + ")");
+  const int eg = (int)std::min<int64_t>(std::max<int64_t>(ceil_div(n * bs, 256), 1), (int64_t)num_sms() * 8);
+  const size_t blk = (size_t)n * bs;
+  COLAGB_CUDA(cudaMemsetAsync(basis, 0, sizeof(T) * blk * slots, st));
+  COLAGB_CUDA(cudaMemsetAsync(H, 0, sizeof(T) * bs * (m + 1) * (m > 0 ? m : 1), st));
+  COLAGB_CUDA(cudaMemsetAsync(s.counters, 0, 8 * sizeof(unsigned int), st));
+  k_lz_set_state<T><<<1, 32, 0, st>>>(s, m);
+  T* q0 = basis + blk;  // Q[0] = V0 / |V0|
+  k_lz_init_copy<T><<<eg, 256, 0, st>>>(V0, ldv0, q0, n, bs);
+  k_lz_norm<T><<<nb, 256, 0, st>>>(q0, n, bs, s);
+  k_lz_scale<T><<<eg, 256, 0, st>>>(q0, n, bs, s);
+  COLAGB_CUDA(cudaGetLastError());
+  const int every = prm.check_every > 0 ? prm.check_every : 8;
+  int host_step = 1;  // slot of Q[idx] for the next step (idx = host_step - 1)
+  int hdone = 0;
+  while (true) {
+    for (int q = 0; q < every && host_step <= m; ++q, ++host_step) {
+      const int i = host_step;
+      T* qi = basis + (size_t)i * blk;
+      T* w = basis + (size_t)(i + 1) * blk;
+      Bump ow(opws, opb > 0 ? opb : 1);
+      COLAGB_TRY(op_apply<T>(A, A->root, qi, bs, 0, w, bs, 0, bs, 1, T(1), T(0), ow, s.done, st));
+      for (int pass = 0; pass < 2; ++pass) {  // classical Gram-Schmidt, twice
+        k_lz_project<T><<<nb, 256, 0, st>>>(basis, w, n, bs, slots, s);
+        k_lz_reduce_h<T><<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div((int64_t)(i + 1) * bs, 256), 4096)),
+                           256, 0, st>>>(nb, bs, slots, s);
+        k_ar_accum_h<T><<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div((int64_t)i * bs, 256), 4096)), 256,
+                          0, st>>>(H, bs, m, pass == 0, s);
+        k_lz_subtract<T><<<eg, 256, 0, st>>>(basis, w, n, bs, s);
+      }
+      k_lz_norm<T><<<nb, 256, 0, st>>>(w, n, bs, s);
+      k_ar_scale_clip<T><<<eg, 256, 0, st>>>(w, n, bs, prm.tol, s);
+      k_ar_finish<T><<<1, 256, 0, st>>>(H, bs, m, prm.tol, s);
+      COLAGB_CUDA(cudaGetLastError());
+    }
+    COLAGB_CUDA(cudaMemcpyAsync(&hdone, s.done, sizeof(int), cudaMemcpyDeviceToHost, st));
+    COLAGB_CUDA(cudaStreamSynchronize(st));
+    if (hdone || host_step > m) break;
+  }
+  int dstep = 0;
+  COLAGB_CUDA(cudaMemcpyAsync(&dstep, s.step, sizeof(int), cudaMemcpyDeviceToHost, st));
+  COLAGB_CUDA(cudaStreamSynchronize(st));
+  *steps = dstep - 1;  // Arnoldi steps taken (idx)
+  return COLAGB_OK;
+}
 }  // namespace colagb
 
 using namespace colagb;
@@ -525,4 +635,24 @@ extern "C" int colagb_tridiag_eig_f64(const double* a, const double* b, int64_t 
   k_tridiag_ql<<<(unsigned)batch, 128, smem, st>>>(a, b, m, evals, first_row, evecs, status);
   COLAGB_CUDA(cudaGetLastError());
   return COLAGB_OK;
+}
+
+extern "C" int colagb_arnoldi_workspace_bytes(const colagb_op* A, int64_t bs, int32_t max_iters, size_t* bytes) {
+  return colagb_lanczos_workspace_bytes(A, bs, max_iters, bytes);
+}
+
+extern "C" int colagb_arnoldi(const colagb_op* A, const void* V0, int64_t ldv0, int64_t bs,
+                              const colagb_lanczos_params* params, void* basis, void* H, int32_t* steps, void* workspace,
+                              size_t workspace_bytes, void* stream) {
+  if (!A || !params || !V0 || !basis || !H || !steps) return fail(COLAGB_ERR_INVALID, "colagb_arnoldi: null argument");
+  const colagb_op_node& r = A->nodes[A->root];
+  if (r.rows != r.cols) return fail(COLAGB_ERR_INVALID, "colagb_arnoldi: operator must be square");
+  if (bs < 1 || ldv0 < bs || params->max_iters < 1)
+    return fail(COLAGB_ERR_INVALID, "colagb_arnoldi: bad bs / ldv0 / max_iters");
+  cudaStream_t st = as_stream(stream);
+  if (A->compute_dtype == COLAGB_F64)
+    return arnoldi_t<double>(A, static_cast<const double*>(V0), ldv0, bs, *params, static_cast<double*>(basis),
+                             static_cast<double*>(H), steps, workspace, workspace_bytes, st);
+  return arnoldi_t<float>(A, static_cast<const float*>(V0), ldv0, bs, *params, static_cast<float*>(basis),
+                          static_cast<float*>(H), steps, workspace, workspace_bytes, st);
 }

@@ -1,5 +1,6 @@
 """cola.linalg equivalents on the GPU Krylov path."""
-from .algorithms import (LU, Algorithm, Auto, CG, Cholesky, Eigh, Exact, Hutch, Lanczos, get_slice)
+from .algorithms import (LU, Algorithm, Arnoldi, Auto, CG, Cholesky, Eigh, Exact, GMRES, Hutch, Lanczos, get_slice)
+from .arnoldi import arnoldi, gmres
 from .batched import BatchedCSR, solve_batched
 from .inverse import IterativeOperatorWInfo, cg, inv, solve
 from .lanczos import eig, eigmax, eigmin, lanczos, lanczos_eigs, run_lanczos, tridiag_eigh
@@ -9,7 +10,7 @@ from .unary import (LanczosUnary, apply_unary, diag, exact_diag, exp, hutchinson
                     slogdet, sqrt, stochastic_lanczos_quad, trace)
 
 __all__ = [
-    "Algorithm", "Auto", "CG", "Lanczos", "Exact", "Hutch", "Cholesky", "LU", "Eigh", "get_slice",
+    "Algorithm", "Auto", "CG", "GMRES", "Arnoldi", "arnoldi", "gmres", "Lanczos", "Exact", "Hutch", "Cholesky", "LU", "Eigh", "get_slice",
     "IterativeOperatorWInfo", "cg", "inv", "solve", "eig", "eigmax", "eigmin", "lanczos", "lanczos_eigs",
     "run_lanczos", "tridiag_eigh", "PRNGKey", "next_key", "randn", "sha_hash", "LanczosUnary", "apply_unary",
     "diag", "exact_diag", "hutchinson_diag_estimate", "log", "logdet", "slogdet", "stochastic_lanczos_quad",

@@ -49,6 +49,34 @@ class CG(Algorithm):
 
 
 @dataclass
+class GMRES(Algorithm):
+    """Generalised minimal residual for square (non-symmetric) A (gmres.py:11-36)."""
+    tol: float = 1e-6
+    max_iters: int = 1000
+    pbar: bool = False
+    x0: Any = None
+    P: Optional[LinearOperator] = None
+
+    def __call__(self, A, b):
+        from .arnoldi import gmres
+        return gmres(A, b, **self.__dict__)
+
+
+@dataclass
+class Arnoldi(Algorithm):
+    """Arnoldi decomposition A Q = Q H (decompositions.py:147-174)."""
+    start_vector: Any = None
+    max_iters: int = 1_000
+    tol: float = 1e-6
+    pbar: bool = False
+    key: Optional[PRNGKey] = None
+
+    def __call__(self, A: LinearOperator):
+        from .arnoldi import arnoldi
+        return arnoldi(A, **self.__dict__)
+
+
+@dataclass
 class Lanczos(Algorithm):
     """Lanczos decomposition Q^T A Q = T for self-adjoint A (decompositions.py:118-144)."""
     start_vector: Any = None

@@ -17,7 +17,7 @@ from .. import _capi
 from .. import ops as O
 from ..annotations import PSD, Unitary
 from ..lowering import lower, operator_device
-from .algorithms import CG, LU, Algorithm, Auto, Cholesky
+from .algorithms import CG, GMRES, LU, Algorithm, Auto, Cholesky
 
 
 class IterativeOperatorWInfo(O.LinearOperator):
@@ -143,6 +143,8 @@ def inv(A: O.LinearOperator, alg: Algorithm = Auto()):
         return O.BlockDiag(*[inv(M, alg) for M in A.Ms], multiplicities=A.multiplicities)
     if isinstance(A, O.Kronecker):
         return O.Kronecker(*[inv(M, alg) for M in A.Ms])
+    if isinstance(alg, GMRES):
+        return IterativeOperatorWInfo(A, alg)
     if isinstance(alg, CG):
         assert A.isa(PSD), "CG only valid for PSD matrices, wrap in cola.PSD if desired"
         return IterativeOperatorWInfo(A, alg)
@@ -152,7 +154,7 @@ def inv(A: O.LinearOperator, alg: Algorithm = Auto()):
             return inv(A, Cholesky() if small else CG(**alg.__dict__))
         if small:
             return inv(A, LU())
-        raise NotImplementedError("GMRES (non-PSD large operators) is not on the accelerated path")
+        return inv(A, GMRES(**alg.__dict__))
     if isinstance(alg, Cholesky):
         assert A.isa(PSD), "Cholesky only valid for PSD matrices, wrap in cola.PSD if desired"
         return _dense_cholesky_inv(A)

@@ -263,6 +263,21 @@ int colagb_lanczos(const colagb_op* A, const void* V0, int64_t ldv0, int64_t bs,
 
 /* Ritz combination: out (n x bs) = for each probe b: sum_j basis[j+1][:, b] * coef[b][j], j < m.
  * Forms Q @ w for the LanczosUnary quadrature (unary.py:58-59) and Ritz vectors. */
+/* ------------------------------------------------------------------------ *
+ *  Arnoldi decomposition of a square (non-symmetric) operator              *
+ *  (cola/linalg/decompositions/arnoldi.py:166-201, 303-334): Q[0] = V0 /   *
+ *  |V0|, each step w = A Q[idx] orthogonalised against Q[0..idx] (two      *
+ *  classical Gram-Schmidt passes; the reference does one modified pass),   *
+ *  H[:, idx] = the coefficients, H[idx+1, idx] = |w|, Q[idx+1] = w /       *
+ *  max(|w|, tol/2); stops when idx = max_iters or every column's |w| <=    *
+ *  tol * H[1, 0].  basis: (max_iters + 2) x n x bs slots, Q[j] in slot     *
+ *  j + 1; H: bs x (max_iters + 1) x max_iters row-major; steps = idx.      *
+ *  Workspace as for colagb_lanczos.                                        *
+ * ------------------------------------------------------------------------ */
+int colagb_arnoldi_workspace_bytes(const colagb_op* A, int64_t bs, int32_t max_iters, size_t* bytes);
+int colagb_arnoldi(const colagb_op* A, const void* V0, int64_t ldv0, int64_t bs, const colagb_lanczos_params* params,
+                   void* basis, void* H, int32_t* steps, void* workspace, size_t workspace_bytes, void* stream);
+
 int colagb_basis_combine(const void* basis, int64_t n, int64_t bs, int32_t m, const void* coef, int64_t ldc,
                          void* out, int32_t dtype, void* stream);
 

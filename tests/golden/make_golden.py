@@ -222,7 +222,32 @@ def case_ops():
     save("ops_sum_product", D=D, d=d, X=Xs, Ysum=SumOp @ torch.from_numpy(Xs), Yprod=ProdOp @ torch.from_numpy(Xs))
 
 
+def case_arnoldi_gmres():
+    """Non-symmetric operators: Arnoldi (arnoldi.py:166-201, 303-334) and GMRES (gmres.py:39-117)."""
+    from cola.linalg.decompositions.arnoldi import arnoldi
+    from cola.linalg.inverse.gmres import gmres
+    rng = np.random.default_rng(7)
+    n = 40
+    A = 3 * np.eye(n) + 0.5 * rng.standard_normal((n, n)) / np.sqrt(n)
+    b = rng.standard_normal(n)
+    At, bt = torch.from_numpy(A), torch.from_numpy(b)
+    Q, H, info = arnoldi(cola.ops.Dense(At), start_vector=bt, max_iters=12, tol=1e-12)
+    save("arnoldi_dense", A=A, v0=b, max_iters=12, tol=1e-12, Q=Q.to_dense(), H=H.to_dense(),
+         iterations=info["iterations"])
+    for tag, m in (("full", 30), ("short", 8)):
+        x, info = gmres(cola.ops.Dense(At), bt, max_iters=m, tol=1e-10)
+        save(f"gmres_dense_{tag}", A=A, b=b, max_iters=m, tol=1e-10, x=x, iterations=info["iterations"])
+    # two right-hand sides at once, float32
+    B = rng.standard_normal((n, 2)).astype(np.float32)
+    X, info = gmres(cola.ops.Dense(At.float()), torch.from_numpy(B), max_iters=25, tol=1e-6)
+    save("gmres_dense_multi_f32", A=A.astype(np.float32), B=B, max_iters=25, tol=1e-6, x=X, iterations=info["iterations"])
+
+
 if __name__ == "__main__":
-    for fn in [case_cg_dense, case_cg_multi_jacobi_x0, case_cg_sparse, case_cg_repeated_eig, case_lanczos, case_eig,
-               case_lanczos_unary, case_logdet_slq, case_kron_slq, case_slq_tbd, case_ops]:
-        fn()
+    import os
+    cases = [case_cg_dense, case_cg_multi_jacobi_x0, case_cg_sparse, case_cg_repeated_eig, case_lanczos, case_eig,
+             case_lanczos_unary, case_logdet_slq, case_kron_slq, case_slq_tbd, case_ops, case_arnoldi_gmres]
+    only = [x for x in os.environ.get("GOLDEN_ONLY", "").split(",") if x]
+    for fn in cases:
+        if not only or fn.__name__ in only:
+            fn()
