@@ -15,6 +15,8 @@
 #include <cmath>
 #include <string>
 
+#include <type_traits>
+
 #include "common.cuh"
 #include "ops.cuh"
 
@@ -55,13 +57,38 @@ __device__ __forceinline__ void lz_partials(int64_t n, int64_t bs, F f, T* out, 
       for (int64_t r = (int64_t)blockIdx.x * rpp + my_r; r < n; r += (int64_t)rpp * gridDim.x) acc += f(r, b0 + my_b);
     smem[t] = acc;
     __syncthreads();
-    if (t < bc) {
-      T s = T(0);
-      for (int q = 0; q < rpp; ++q) s += smem[q * bc + t];
-      out[b0 + t] = s;
+    // tree over the rpp row slots (a serial sum by one thread per column is rpp dependent
+    // shared-memory round trips)
+    for (int w = rpp; w > 1;) {
+      const int h = (w + 1) >> 1;
+      if (my_r < w - h) smem[t] += smem[t + h * bc];
+      __syncthreads();
+      w = h;
     }
+    if (t < bc) out[b0 + t] = smem[t];
     __syncthreads();
   }
+}
+
+// Sum over the nb per-CTA partials of column b, formed by the whole block (all threads get it).
+template <class T>
+__device__ __forceinline__ T lz_block_total(const T* part, int nb, int64_t bs, int64_t b, T* red) {
+  T v = T(0);
+  for (int q = threadIdx.x; q < nb; q += blockDim.x) v += __ldcg(part + (int64_t)q * bs + b);
+  return block_sum(v, red);
+}
+
+// Totals of the first kLzStage columns into shared memory, block-parallel; lz_total reads them
+// (serial sum only beyond kLzStage columns).
+constexpr int kLzStage = 64;
+template <class T>
+__device__ __forceinline__ void lz_stage(const T* part, int nb, int64_t bs, T* tot, T* red) {
+  const int64_t kk = bs < kLzStage ? bs : kLzStage;
+  for (int64_t b = 0; b < kk; ++b) {
+    const T v = lz_block_total(part, nb, bs, b, red);
+    if (threadIdx.x == 0) tot[b] = v;
+  }
+  __syncthreads();
 }
 
 template <class T>
@@ -69,6 +96,11 @@ __device__ __forceinline__ T lz_sum(const T* part, int nb, int64_t bs, int64_t b
   T s = T(0);
   for (int q = 0; q < nb; ++q) s += __ldcg(part + (int64_t)q * bs + b);
   return s;
+}
+
+template <class T>
+__device__ __forceinline__ T lz_total(const T* part, int nb, int64_t bs, int64_t b, const T* tot) {
+  return b < kLzStage ? tot[b] : lz_sum(part, nb, bs, b);
 }
 
 // V[i] /= |V[i]|   (norm pass; the division is k_lz_scale)
@@ -79,7 +111,9 @@ __global__ void __launch_bounds__(256) k_lz_norm(const T* v, int64_t n, int64_t 
   lz_partials<T>(n, bs, [&](int64_t r, int64_t b) { const T x = v[r * bs + b]; return x * x; },
                  s.npart + (int64_t)blockIdx.x * bs, smem);
   if (lz_last_block(s.counters + 0)) {
-    for (int64_t b = threadIdx.x; b < bs; b += blockDim.x) s.nrm[b] = sqrt(lz_sum(s.npart, gridDim.x, bs, b));
+    __shared__ T tot[kLzStage], red[32];
+    lz_stage(s.npart, gridDim.x, bs, tot, red);
+    for (int64_t b = threadIdx.x; b < bs; b += blockDim.x) s.nrm[b] = sqrt(lz_total(s.npart, gridDim.x, bs, b, tot));
     if (threadIdx.x == 0) s.counters[0] = 0;
   }
 }
@@ -100,9 +134,11 @@ __global__ void __launch_bounds__(256) k_lz_alpha(const T* w, const T* vi, int64
   lz_partials<T>(n, bs, [&](int64_t r, int64_t b) { return w[r * bs + b] * vi[r * bs + b]; },
                  s.npart + (int64_t)blockIdx.x * bs, smem);
   if (lz_last_block(s.counters + 1)) {
+    __shared__ T tot[kLzStage], red[32];
+    lz_stage(s.npart, gridDim.x, bs, tot, red);
     const int i = *s.step;
     for (int64_t b = threadIdx.x; b < bs; b += blockDim.x)
-      diag[b * max_iters + (i - 1)] = lz_sum(s.npart, gridDim.x, bs, b);
+      diag[b * max_iters + (i - 1)] = lz_total(s.npart, gridDim.x, bs, b, tot);
     if (threadIdx.x == 0) s.counters[1] = 0;
   }
 }
@@ -120,58 +156,107 @@ __global__ void k_lz_three_term(T* w, const T* vi, const T* vim1, int64_t n, int
 }
 
 // Projection partials: hpart[blk][j][b] = sum over the block's rows of V[j][r][b] * w[r][b], j = 1..i.
-// Each block owns a contiguous row range (staged w rows reused across all j).
+// Each block owns a contiguous row range.  Four basis slots per pass: w is read once for the four,
+// and the four partial sums share one tree reduction (one pass per slot re-read w and waited on a
+// reduction per slot -- this kernel is most of an SLQ run's time).
 template <class T>
 __global__ void __launch_bounds__(256) k_lz_project(const T* basis, const T* w, int64_t n, int64_t bs,
                                                     int64_t slots, LzState<T> s) {
   if (*s.done) return;
-  __shared__ T smem[256];
+  constexpr int JB = 4;
+  __shared__ T smem[JB * 256];
   const int i = *s.step;
   const int64_t rows_per_block = ceil_div(n, gridDim.x);
   const int64_t r0 = (int64_t)blockIdx.x * rows_per_block;
   const int64_t r1 = r0 + rows_per_block < n ? r0 + rows_per_block : n;
   T* out = s.hpart + (int64_t)blockIdx.x * slots * bs;
   const int t = threadIdx.x;
+  const int64_t slot = n * bs;
   for (int64_t b0 = 0; b0 < bs; b0 += blockDim.x) {
     const int bc = (int)((bs - b0) < (int64_t)blockDim.x ? (bs - b0) : (int64_t)blockDim.x);
     const int rpp = blockDim.x / bc;
     const int my_b = t % bc, my_r = t / bc;
-    for (int j = 1; j <= i; ++j) {
-      const T* vj = basis + (int64_t)j * n * bs;
-      T acc = T(0);
-      if (my_r < rpp)
-        for (int64_t r = r0 + my_r; r < r1; r += rpp) acc += vj[r * bs + b0 + my_b] * w[r * bs + b0 + my_b];
-      smem[t] = acc;
+    for (int j0 = 1; j0 <= i; j0 += JB) {
+      const int nj = (i - j0 + 1) < JB ? (i - j0 + 1) : JB;
+      T acc[JB] = {T(0), T(0), T(0), T(0)};
+      if (my_r < rpp) {
+        const T* v0 = basis + (int64_t)j0 * slot + b0 + my_b;
+        for (int64_t r = r0 + my_r; r < r1; r += rpp) {
+          const T wv = w[r * bs + b0 + my_b];
+#pragma unroll
+          for (int q = 0; q < JB; ++q)
+            if (q < nj) acc[q] += v0[(int64_t)q * slot + r * bs] * wv;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < JB; ++q) smem[q * 256 + t] = acc[q];
       __syncthreads();
+      for (int wd = rpp; wd > 1;) {  // tree over the row slots, all JB sums at once
+        const int h = (wd + 1) >> 1;
+        if (my_r < wd - h) {
+#pragma unroll
+          for (int q = 0; q < JB; ++q) smem[q * 256 + t] += smem[q * 256 + t + h * bc];
+        }
+        __syncthreads();
+        wd = h;
+      }
       if (t < bc) {
-        T sum = T(0);
-        for (int q = 0; q < rpp; ++q) sum += smem[q * bc + t];
-        out[(int64_t)j * bs + b0 + t] = sum;
+        for (int q = 0; q < nj; ++q) out[(int64_t)(j0 + q) * bs + b0 + t] = smem[q * 256 + t];
       }
       __syncthreads();
     }
   }
 }
 
-// h[j][b] = sum over blocks of hpart  (thread per (j, b))
+// h[j][b] = sum over blocks of hpart  (one warp per (j, b): lanes take strided blocks, then a
+// shuffle tree; a thread per (j, b) would wait on nblk dependent loads)
 template <class T>
 __global__ void k_lz_reduce_h(int nblk, int64_t bs, int64_t slots, LzState<T> s) {
   if (*s.done) return;
   const int i = *s.step;
   const int64_t total = (int64_t)(i + 1) * bs;
-  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < total; u += (int64_t)gridDim.x * blockDim.x) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t u = warp0; u < total; u += nwarps) {
     T acc = T(0);
     if (u >= bs)  // slot 0 is the zero vector
-      for (int q = 0; q < nblk; ++q) acc += s.hpart[(int64_t)q * slots * bs + u];
-    s.hbuf[u] = acc;
+      for (int q = lane; q < nblk; q += 32) acc += s.hpart[(int64_t)q * slots * bs + u];
+    acc = warp_sum(acc);
+    if (lane == 0) s.hbuf[u] = acc;
   }
 }
 
-// w -= sum_j V[j] h[j]
+// w -= sum_j V[j] h[j]  (128-bit accesses for FP32 when bs is a multiple of 4)
 template <class T>
 __global__ void k_lz_subtract(const T* basis, T* w, int64_t n, int64_t bs, LzState<T> s) {
   if (*s.done) return;
   const int i = *s.step;
+  if constexpr (std::is_same<T, float>::value) {
+    if (bs % 4 == 0) {
+      const int64_t n4 = n * bs / 4;
+      float4* w4 = reinterpret_cast<float4*>(w);
+      for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n4; u += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t b = (4 * u) % bs;
+        float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int j = 1; j <= i; ++j) {
+          const float4 v = reinterpret_cast<const float4*>(basis + (int64_t)j * n * bs)[u];
+          const float* h = s.hbuf + (int64_t)j * bs + b;
+          acc.x += v.x * h[0];
+          acc.y += v.y * h[1];
+          acc.z += v.z * h[2];
+          acc.w += v.w * h[3];
+        }
+        float4 wv = w4[u];
+        wv.x -= acc.x;
+        wv.y -= acc.y;
+        wv.z -= acc.z;
+        wv.w -= acc.w;
+        w4[u] = wv;
+      }
+      return;
+    }
+  }
   for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n * bs; u += (int64_t)gridDim.x * blockDim.x) {
     const int64_t b = u % bs;
     T acc = T(0);
@@ -190,11 +275,13 @@ __global__ void __launch_bounds__(256) k_lz_finish(const T* w, int64_t n, int64_
                  s.npart + (int64_t)blockIdx.x * bs, smem);
   if (lz_last_block(s.counters + 2)) {
     __shared__ int s_any;
+    __shared__ T tot[kLzStage], red[32];
+    lz_stage(s.npart, gridDim.x, bs, tot, red);
     const int i = *s.step;
     if (threadIdx.x == 0) s_any = 0;
     __syncthreads();
     for (int64_t b = threadIdx.x; b < bs; b += blockDim.x) {
-      const T nv = sqrt(lz_sum(s.npart, gridDim.x, bs, b));
+      const T nv = sqrt(lz_total(s.npart, gridDim.x, bs, b, tot));
       subdiag[b * (max_iters + 1) + i] = nv;
       const T first = subdiag[b * (max_iters + 1) + 1];
       if (nv > (T)tol * first) atomicOr(&s_any, 1);
@@ -439,7 +526,7 @@ static int lanczos_t(const colagb_op* A, const T* V0, int64_t ldv0, int64_t bs, 
       k_lz_three_term<T><<<eg, 256, 0, st>>>(w, vi, vim1, n, bs, diag, subdiag, m, s);
       for (int pass = 0; pass < 2; ++pass) {
         k_lz_project<T><<<nb, 256, 0, st>>>(basis, w, n, bs, slots, s);
-        k_lz_reduce_h<T><<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div((int64_t)(i + 1) * bs, 256), 4096)),
+        k_lz_reduce_h<T><<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div((int64_t)(i + 1) * bs, 8), 4096)),
                            256, 0, st>>>(nb, bs, slots, s);
         k_lz_subtract<T><<<eg, 256, 0, st>>>(basis, w, n, bs, s);
       }
@@ -546,7 +633,7 @@ static int arnoldi_t(const colagb_op* A, const T* V0, int64_t ldv0, int64_t bs, 
       COLAGB_TRY(op_apply<T>(A, A->root, qi, bs, 0, w, bs, 0, bs, 1, T(1), T(0), ow, s.done, st));
       for (int pass = 0; pass < 2; ++pass) {  // classical Gram-Schmidt, twice
         k_lz_project<T><<<nb, 256, 0, st>>>(basis, w, n, bs, slots, s);
-        k_lz_reduce_h<T><<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div((int64_t)(i + 1) * bs, 256), 4096)),
+        k_lz_reduce_h<T><<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div((int64_t)(i + 1) * bs, 8), 4096)),
                            256, 0, st>>>(nb, bs, slots, s);
         k_ar_accum_h<T><<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div((int64_t)i * bs, 256), 4096)), 256,
                           0, st>>>(H, bs, m, pass == 0, s);
