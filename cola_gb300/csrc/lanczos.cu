@@ -14,6 +14,7 @@
 // reductions, 1 dot, and 2 x (V^T w then w -= V h) passes over the filled slots.
 #include <cmath>
 #include <string>
+#include <vector>
 
 #include <type_traits>
 
@@ -329,8 +330,12 @@ __global__ void k_basis_combine(const T* basis, int64_t n, int64_t bs, int m, co
 // Thread 0 runs the scalar recurrence; each QL sweep's Givens rotations are recorded in shared
 // memory and then applied by all threads to their own rows of the eigenvector matrix (rows are
 // independent under column rotations).  Row 0 alone (Gauss weights) is tracked by thread 0.
+// `rec` (optional, with evecs == nullptr): every Givens rotation (c, s) on columns (i, i+1) is
+// appended in generation order to rec[sys * cap ...] / rec_i, the count to rec_n[sys] (-1 when cap
+// was exceeded), and the sorting permutation to rec_perm[sys * m ...]; k_tridiag_apply replays them.
 __global__ void k_tridiag_ql(const double* A, const double* Bv, int64_t m, double* evals, double* first_row,
-                             double* evecs, int32_t* status) {
+                             double* evecs, int32_t* status, double2* rec = nullptr, int32_t* rec_i = nullptr,
+                             int32_t* rec_n = nullptr, int32_t* rec_perm = nullptr, int64_t cap = 0) {
   extern __shared__ double sm[];
   double* d = sm;              // m
   double* e = d + m;           // m
@@ -353,6 +358,9 @@ __global__ void k_tridiag_ql(const double* A, const double* Bv, int64_t m, doubl
   if (threadIdx.x == 0) s_fail = 0;
   __syncthreads();
   int l = 0, iter = 0;
+  int64_t nrec = 0;
+  double2* my_rec = rec ? rec + sys * cap : nullptr;
+  int32_t* my_rec_i = rec ? rec_i + sys * cap : nullptr;
   while (true) {
     // thread 0: one QL sweep (or decide to move on)
     if (threadIdx.x == 0) {
@@ -390,6 +398,13 @@ __global__ void k_tridiag_ql(const double* A, const double* Bv, int64_t m, doubl
           g = c * r - bb;
           rc[i] = c;
           rs[i] = s;
+          if (my_rec) {
+            if (nrec < cap) {
+              my_rec[nrec] = make_double2(c, s);
+              my_rec_i[nrec] = i;
+            }
+            ++nrec;
+          }
           const double zf = z0[i + 1];
           z0[i + 1] = s * z0[i] + c * zf;
           z0[i] = c * z0[i] - s * zf;
@@ -444,7 +459,9 @@ __global__ void k_tridiag_ql(const double* A, const double* Bv, int64_t m, doubl
   for (int64_t j = threadIdx.x; j < m; j += blockDim.x) {
     evals[sys * m + j] = d[perm[j]];
     if (first_row) first_row[sys * m + j] = Z ? Z[perm[j]] : z0[perm[j]];
+    if (rec_perm) rec_perm[sys * m + j] = perm[j];
   }
+  if (rec && threadIdx.x == 0) rec_n[sys] = nrec <= cap ? (int32_t)nrec : -1;
   __syncthreads();
   if (Z) {
     double* tmp = rc;  // reuse as a row buffer
@@ -456,6 +473,36 @@ __global__ void k_tridiag_ql(const double* A, const double* Bv, int64_t m, doubl
     }
   }
   if (threadIdx.x == 0 && status) status[sys] = s_fail;
+}
+
+// Replays the recorded rotations on the eigenvector matrix: Z starts as the identity, each thread
+// owns one row (rows are independent), held in shared memory as zs[col][lane] (conflict-free);
+// every rotation acts on columns (i, i+1).  Output columns follow the sorted eigenvalues.
+constexpr int kRotRows = 32;
+__global__ void __launch_bounds__(kRotRows) k_tridiag_apply(const double2* rec, const int32_t* rec_i,
+                                                            const int32_t* rec_n, const int32_t* rec_perm, int64_t m,
+                                                            int64_t cap, double* evecs) {
+  extern __shared__ double zs[];  // m x kRotRows
+  const int64_t sys = blockIdx.y;
+  const int t = threadIdx.x;
+  const int64_t row = (int64_t)blockIdx.x * kRotRows + t;
+  const int32_t nr = rec_n[sys];
+  if (nr < 0) return;  // the recording overflowed: the in-kernel path produced Z
+  for (int64_t i = 0; i < m; ++i) zs[i * kRotRows + t] = (row == i) ? 1.0 : 0.0;
+  const double2* r = rec + sys * cap;
+  const int32_t* ri = rec_i + sys * cap;
+  for (int32_t q = 0; q < nr; ++q) {
+    const double2 cs = r[q];
+    const int i = ri[q];
+    const double zi = zs[i * kRotRows + t], f = zs[(i + 1) * kRotRows + t];
+    zs[(i + 1) * kRotRows + t] = cs.y * zi + cs.x * f;
+    zs[i * kRotRows + t] = cs.x * zi - cs.y * f;
+  }
+  if (row < m) {
+    double* out = evecs + sys * m * m + row * m;
+    const int32_t* perm = rec_perm + sys * m;
+    for (int64_t j = 0; j < m; ++j) out[j] = zs[perm[j] * kRotRows + t];
+  }
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -719,6 +766,37 @@ extern "C" int colagb_tridiag_eig_f64(const double* a, const double* b, int64_t 
   if (smem > 48 * 1024)
     COLAGB_CUDA(cudaFuncSetAttribute(k_tridiag_ql, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   cudaStream_t st = as_stream(stream);
+  const size_t smem_rot = (size_t)m * kRotRows * sizeof(double);
+  if (evecs && smem_rot <= 200 * 1024) {
+    // eigenvectors: QL records its rotations (one thread generates them serially), then many CTAs
+    // replay them on the rows of Z in shared memory; applying them to Z in global memory from the
+    // same CTA, row per thread, cost ~95 % of the solve
+    const int64_t cap = 6 * m * m + 64;
+    void* buf = nullptr;
+    const size_t bytes = (size_t)batch * cap * (sizeof(double2) + sizeof(int32_t)) +
+                         (size_t)batch * (m + 1) * sizeof(int32_t);
+    COLAGB_CUDA(cudaMallocAsync(&buf, bytes, st));
+    double2* rec = static_cast<double2*>(buf);
+    int32_t* rec_i = reinterpret_cast<int32_t*>(rec + batch * cap);
+    int32_t* rec_n = rec_i + batch * cap;
+    int32_t* rec_perm = rec_n + batch;
+    k_tridiag_ql<<<(unsigned)batch, 128, smem, st>>>(a, b, m, evals, first_row, nullptr, status, rec, rec_i, rec_n,
+                                                     rec_perm, cap);
+    COLAGB_CUDA(cudaGetLastError());
+    if (smem_rot > 48 * 1024)
+      COLAGB_CUDA(cudaFuncSetAttribute(k_tridiag_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_rot));
+    k_tridiag_apply<<<dim3((unsigned)ceil_div(m, (int64_t)kRotRows), (unsigned)batch), kRotRows, smem_rot, st>>>(
+        rec, rec_i, rec_n, rec_perm, m, cap, evecs);
+    COLAGB_CUDA(cudaGetLastError());
+    std::vector<int32_t> hn(batch);
+    COLAGB_CUDA(cudaMemcpyAsync(hn.data(), rec_n, batch * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    COLAGB_CUDA(cudaStreamSynchronize(st));
+    bool overflow = false;
+    for (int64_t q = 0; q < batch; ++q) overflow |= hn[q] < 0;
+    COLAGB_CUDA(cudaFreeAsync(buf, st));
+    if (!overflow) return COLAGB_OK;
+    // rare: more rotations than recorded -- recompute with Z updated inside the QL kernel
+  }
   k_tridiag_ql<<<(unsigned)batch, 128, smem, st>>>(a, b, m, evals, first_row, evecs, status);
   COLAGB_CUDA(cudaGetLastError());
   return COLAGB_OK;

@@ -424,6 +424,8 @@ int op_apply(const colagb_op* op, int node, const T* X, int64_t ldx, int64_t bsx
       }
       const size_t mark = ws.used;
       T* buf[2] = {ws.take<T>((size_t)maxsz * k), ws.take<T>((size_t)maxsz * k)};
+      // scratch for the axis-swapped form of a factor with few columns per block (below)
+      T* sw[2] = {ws.take<T>((size_t)maxsz * k), ws.take<T>((size_t)maxsz * k)};
       for (int64_t b = 0; b < batch && !measuring; ++b) {
         const T* in = X + b * bsx;
         int which = 0;  // next scratch buffer to write
@@ -439,8 +441,19 @@ int op_apply(const colagb_op* op, int node, const T* X, int64_t ldx, int64_t bsx
           const bool last = (i == m - 1);
           const bool direct = last && ldy == k;
           T* out = direct ? (Y + b * bsy) : buf[which];
-          COLAGB_TRY(op_apply<T>(op, ch[i], in, post * k, c[i] * post * k, out, post * k, r[i] * post * k, post * k,
-                                 pre, direct ? alpha : T(1), direct ? beta : T(0), ws, skip, st));
+          const int64_t q = post * k;
+          if (q <= 8 && pre >= 16 && pre <= 65535 && c[i] <= 65535) {
+            // `pre` products of M_i with (c_i x q) blocks re-read M_i `pre` times; with the first two
+            // axes swapped they are one product M_i @ (c_i x pre*q), then swapped back
+            COLAGB_TRY(launch_axpby_b<T>(in, c[i] * q, q, sw[0], q, pre * q, pre, q, c[i], T(1), T(0), skip, st));
+            COLAGB_TRY(op_apply<T>(op, ch[i], sw[0], pre * q, 0, sw[1], pre * q, 0, pre * q, 1, T(1), T(0), ws, skip,
+                                   st));
+            COLAGB_TRY(launch_axpby_b<T>(sw[1], pre * q, q, out, q, r[i] * q, r[i], q, pre, direct ? alpha : T(1),
+                                         direct ? beta : T(0), skip, st));
+          } else {
+            COLAGB_TRY(op_apply<T>(op, ch[i], in, post * k, c[i] * post * k, out, post * k, r[i] * post * k,
+                                   post * k, pre, direct ? alpha : T(1), direct ? beta : T(0), ws, skip, st));
+          }
           if (last && !direct)
             COLAGB_TRY(launch_axpby_b<T>(out, k, 0, Y + b * bsy, ldy, 0, nd.rows, k, 1, alpha, beta, skip, st));
           in = out;
