@@ -402,7 +402,9 @@ def main():
     ap.add_argument("--config", default="c4", choices=["c1", "c2", "c3a", "c3b", "c4", "c5"],
                     help="c4 (default): the headline family; the others print one measurement line each")
     ap.add_argument("--method", default="learned", choices=["learned", "fsai", "jacobi", "plain"])
-    ap.add_argument("--compare", default="plain,jacobi")
+    ap.add_argument("--compare", default="plain,jacobi,fsai",
+                    help="methods timed once each beside the headline (same schedule): plain CG, Jacobi PCG, "
+                         "closed-form FSAI PCG")
     ap.add_argument("--systems", type=int, default=SYSTEMS)
     ap.add_argument("--m", type=int, default=M)
     ap.add_argument("--inner-tol", type=float, default=None)

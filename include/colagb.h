@@ -291,6 +291,10 @@ int colagb_basis_combine(const void* basis, int64_t n, int64_t bs, int32_t m, co
  *  evecs: batch x m x m (row-major, column j = eigenvector j), may be NULL. *
  *  status: batch ints, 0 = converged, 1 = iteration limit hit.            *
  * ======================================================================== */
+/* With evecs, the rotations of the QL sweeps are recorded and replayed on the rows of the eigenvector
+ * matrix by a second kernel; the record lives in a stream-ordered temporary (cudaMallocAsync /
+ * cudaFreeAsync on `stream`) of batch * (6 m^2 + 64) * 20 bytes -- the one entry point that allocates
+ * device memory itself. */
 int colagb_tridiag_eig_f64(const double* a, const double* b, int64_t m, int64_t batch, double* evals,
                            double* first_row, double* evecs, int32_t* status, void* stream);
 
