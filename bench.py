@@ -258,14 +258,19 @@ def run_ours(args, world, rank, local):
     X_h = torch.empty_like(B_h).pin_memory()
     e2e_steps = max(1, min(args.steps, 2))
     from cola_gb300.linalg.batched import BatchedCSR
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(st)
-    for _ in range(e2e_steps):
+
+    def e2e_step():
         vals_d = vals_h.to(dev, non_blocking=True)
         B_d = B_h.to(dev, non_blocking=True)
         Xd, _ = solve_batched(BatchedCSR(fam.indptr, fam.indices, vals_d), B_d, **kw)
         X_h.copy_(Xd, non_blocking=True)
+
+    e2e_step()  # untimed: the device buffers of this path come from the allocator's cache afterwards
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(e2e_steps):
+        e2e_step()
     e1.record(st)
     torch.cuda.synchronize()
     t_e2e = max_over_ranks(e0.elapsed_time(e1) / 1e3, world)
