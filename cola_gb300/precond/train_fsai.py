@@ -90,6 +90,63 @@ def set_constant_output(net, o1, o2):
     b.copy_(torch.tensor([0.0, o1, o2], device=b.device))
 
 
+def set_feature_map(net, theta):
+    """Network weights computing, per cell, o1 = theta[0] + sum_k theta[1+k] h_k and
+    o2 = theta[13] + sum_k theta[14+k] h_k over h = (ReLU(f), ReLU(-f)) of the six local features f:
+    layer 1 splits each feature into its two signs (center taps +-1), layer 2 passes the 12
+    channels through, layer 3 combines them.  A piecewise-linear map of each cell's coefficients to
+    the over-relaxation of its two off-diagonals."""
+    net.params.zero_()
+    W1, _ = net.layer(0)
+    W2, _ = net.layer(1)
+    W3, b3 = net.layer(2)
+    for k in range(6):
+        W1[k, k, 1, 1] = 1.0
+        W1[6 + k, k, 1, 1] = -1.0
+    for c in range(12):
+        W2[c, c, 1, 1] = 1.0
+    th = torch.as_tensor(theta, dtype=torch.float32, device=net.params.device)
+    b3[1], b3[2] = th[0], th[13]
+    W3[1, :12, 1, 1] = th[1:13]
+    W3[2, :12, 1, 1] = th[14:26]
+
+
+def search_features(net, seeds, m, device, wn, wv, sweeps=3, log=print):
+    """Coordinate search of the 26 parameters of set_feature_map on the mean PCG iteration count of
+    the given instances, from the global over-relaxation (wn, wv); a move is kept when it saves more
+    than 0.2 % of the iterations.  Returns (theta, mean iterations, evaluations)."""
+    fam, B, _, _ = diffusion_family_2d(seeds, m=m, device=device)
+    evals = [0]
+
+    def cost(th):
+        set_feature_map(net, th)
+        pat, gv = L.g_values(fam, net)
+        _, info = solve_batched(fam, B, precond="fsai", fsai=(pat, gv), tol=1e-8, fallback=True)
+        evals[0] += 1
+        ok = bool(((info["status"] == 1) | (info["status"] == 5)).all())
+        return float(info["iterations"].double().mean()) if ok else float("inf")
+
+    theta = [0.0] * 26
+    theta[0], theta[13] = math.atanh(wn), math.atanh(wv)
+    best = cost(theta)
+    log(f"features search: start {best:.1f}")
+    steps = [0.5] + [0.5] * 4 + [0.5] * 4 + [0.2] * 4  # bias, |ratio| features, log-contrast features
+    for sw in range(sweeps):
+        for d0 in (0, 13):
+            for j in range(13):
+                q = d0 + j
+                step = steps[j] / (2 ** sw)
+                for sgn in (1, -1):
+                    trial = list(theta)
+                    trial[q] += sgn * step
+                    c = cost(trial)
+                    if c < best * 0.998:
+                        theta, best = trial, c
+                        log(f"features search: sweep {sw} param {q} -> {theta[q]:+.3f}: {best:.1f}")
+                        break
+    return theta, best, evals[0]
+
+
 def search(net, seeds, m, device, log=print):
     """Direct search for the over-relaxation (w_N, w_W) = (tanh o1, tanh o2) of the FSAI off-diagonals
     that minimises the mean PCG iteration count on the given training instances: a coarse grid, then
@@ -138,6 +195,9 @@ def main():
                     help="fit the off-diagonal over-relaxation by direct search on PCG iterations "
                          "(instances 1000 .. 1000 + --search-systems) instead of gradient training")
     ap.add_argument("--search-systems", type=int, default=64)
+    ap.add_argument("--features", action="store_true",
+                    help="after the global search, fit a per-cell over-relaxation, piecewise linear in the "
+                         "local coefficient features (coordinate search on PCG iterations)")
     ap.add_argument("--refresh", type=int, default=1,
                     help="regenerate the smooth errors with the current network every this many epochs "
                          "(0: never); the slowest modes of the current factor are what the loss must see")
@@ -151,15 +211,29 @@ def main():
         val_seeds = list(range(4000, 4000 + args.val))
         before = evaluate(net, val_seeds, args.m, dev)
         t0 = time.perf_counter()
-        wn, wv, it, nev = search(net, list(range(1000, 1000 + args.search_systems)), args.m, dev)
-        t_search = time.perf_counter() - t0
+        seeds = list(range(1000, 1000 + args.search_systems))
+        wn, wv, it, nev = search(net, seeds, args.m, dev)
         set_constant_output(net, math.atanh(wn), math.atanh(wv))
-        torch.save(net.state_dict(), args.out)
-        after = evaluate(net, val_seeds, args.m, dev)
         rep = {"method": "direct search of the off-diagonal over-relaxation on PCG iterations",
                "train_instances": args.search_systems, "w_N": wn, "w_W": wv, "train_mean_iters": it,
-               "evaluations": nev, "search_seconds": t_search, "validation_before": before,
-               "validation_after": after}
+               "evaluations": nev}
+        if args.features:
+            glob = evaluate(net, val_seeds, args.m, dev, only=("learned",))["learned"]["mean_iters"]
+            theta, it2, nev2 = search_features(net, seeds, args.m, dev, wn, wv)
+            set_feature_map(net, theta)
+            feat = evaluate(net, val_seeds, args.m, dev, only=("learned",))["learned"]["mean_iters"]
+            rep.update(method="direct search: global over-relaxation, then a per-cell map of local features",
+                       theta=theta, train_mean_iters_features=it2, evaluations_features=nev2,
+                       validation_global_mean_iters=glob, validation_features_mean_iters=feat)
+            if feat >= glob:  # the per-cell map did not generalise: keep the global fit
+                set_constant_output(net, math.atanh(wn), math.atanh(wv))
+                rep["kept"] = "global"
+            else:
+                rep["kept"] = "features"
+        t_search = time.perf_counter() - t0
+        torch.save(net.state_dict(), args.out)
+        after = evaluate(net, val_seeds, args.m, dev)
+        rep.update(search_seconds=t_search, validation_before=before, validation_after=after)
         print(json.dumps(rep, indent=1))
         if args.report:
             with open(args.report, "w") as f:
