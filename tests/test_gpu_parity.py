@@ -533,3 +533,28 @@ def test_gmres_multi_rhs_f32_and_dispatch(golden):
     x = cola.linalg.inv(S, cola.linalg.Auto(max_iters=60, tol=1e-7)) @ b
     r = b - S @ x
     assert float(r.norm() / b.norm()) < 1e-5
+
+
+def test_onchip_limits_restart_nan_and_geometry():
+    from cola_gb300.linalg.batched import onchip_schedule_info
+    from cola_gb300.workloads import diffusion_family_2d
+    fam, B, _, _ = diffusion_family_2d(range(60, 63), m=32, device=DEV)
+    # restart mode (classic refinement) on the on-chip schedule
+    X, info = cola.linalg.solve_batched(fam, B, precond="jacobi", tol=1e-8, mode="restart", schedule="onchip")
+    assert info["schedule"] == "onchip" and torch.all(info["status"] == 1)
+    R = B - fam.matvec(X)
+    assert float((R.norm(dim=1) / B.norm(dim=1)).max()) <= 1.01e-8
+    # the step cap: MAX_ITERS (2) with the FP64-refined iterate returned
+    X2, i2 = cola.linalg.solve_batched(fam, B, precond="none", tol=1e-12, max_inner_iters=20, schedule="onchip")
+    assert torch.all(i2["status"] == 2) and torch.all(i2["iterations"] == 20) and bool(torch.isfinite(X2).all())
+    assert float(i2["relres"].max()) < 1.0
+    # a NaN right-hand side is reported for that system only
+    B3 = B.clone()
+    B3[1, 5] = float("nan")
+    X3, i3 = cola.linalg.solve_batched(fam, B3, precond="jacobi", tol=1e-8, schedule="onchip")
+    assert i3["status"].tolist() == [1, 4, 1]
+    assert rel(X3[0], X[0]) < 1e-6 and rel(X3[2], X[2]) < 1e-6
+    # geometry of the schedule for the 512 x 512 family
+    g = onchip_schedule_info(512 * 512, 512)
+    assert g["cluster_size"] == 16 and g["rows_per_cta"] == 16384 and g["clusters_in_flight"] >= 1
+    assert onchip_schedule_info(2 ** 22, 4)["cluster_size"] == 0  # too large to hold on chip
