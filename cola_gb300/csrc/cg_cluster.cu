@@ -7,8 +7,9 @@
 //     starts a new system's cluster as soon as one finishes (dynamic load balance, no grid-wide sync);
 //   * each CTA owns a fixed contiguous row range of its system for the whole solve;
 //   * phase boundaries are hardware cluster barriers (barrier.cluster arrive/wait via
-//     cooperative_groups), reductions are block sums exchanged through distributed shared memory
-//     and summed in rank order, so every CTA of a cluster derives bit-identical alpha / beta;
+//     cooperative_groups); the per-step dot products are FP32 block sums exchanged through
+//     distributed shared memory and combined by the same butterfly in every CTA, so every CTA of a
+//     cluster derives bit-identical alpha / beta (|b| and the FP64 true residual stay FP64);
 //   * with ~10-19 systems in flight their vectors and values (~10 MB per 512^2 system) largely stay
 //     in the 126 MB L2 across iterations.
 #include <cooperative_groups.h>
@@ -69,8 +70,11 @@ __global__ void __launch_bounds__(kCT, 1) k_cluster_pcg(const __grid_constant__ 
   __shared__ double slots[2][8];
   __shared__ double red[32];
   __shared__ double bcast[8];
-  int buf = 0;
+  __shared__ float fslots[2][4];
+  __shared__ float wpart[2 * 32];
+  int buf = 0, fbuf = 0;
   auto next_slot = [&]() { double* p = slots[buf]; buf ^= 1; return p; };
+  auto next_fslot = [&]() { float* p = fslots[fbuf]; fbuf ^= 1; return p; };
 
   const int64_t n = a.n;
   const int64_t rows = ((n + CL - 1) / CL + 3) / 4 * 4;
@@ -138,8 +142,8 @@ __global__ void __launch_bounds__(kCT, 1) k_cluster_pcg(const __grid_constant__ 
     }
   };
   // z = M r, <r, z>
-  auto apply_z = [&](double (&q)[1]) {
-    float qf = 0.f;  // per-thread partials in FP32, block / cluster sums in FP64
+  auto apply_z = [&](float (&q)[1]) {
+    float qf = 0.f;
     for (int64_t i = i0 + tid; i < i1; i += kCT) {
       float zv;
       if (prec == COLAGB_PREC_FSAI) {
@@ -152,7 +156,7 @@ __global__ void __launch_bounds__(kCT, 1) k_cluster_pcg(const __grid_constant__ 
       z[i] = zv;
       qf += r[i] * zv;
     }
-    q[0] = (double)qf;
+    q[0] = qf;
   };
 
   cl.sync();  // x, d zero and bnorm known everywhere before the residual reads x
@@ -166,10 +170,10 @@ __global__ void __launch_bounds__(kCT, 1) k_cluster_pcg(const __grid_constant__ 
     fsai_t();
     cl.sync();
   }
-  double q1[1];
+  float q1[1];
   apply_z(q1);
-  cluster_sum<1, CL>(cl, q1, next_slot(), red, bcast);
-  double gamma = q1[0];
+  cluster_sum_f<1, CL>(cl, q1, wpart, next_fslot());
+  float gamma = q1[0];
   if (status == COLAGB_SYS_RUNNING && rn <= (float)a.tol) status = COLAGB_SYS_CONVERGED;
   for (int64_t i = i0 + tid; i < i1; i += kCT) p[i] = z[i];
   cl.sync();
@@ -191,14 +195,14 @@ __global__ void __launch_bounds__(kCT, 1) k_cluster_pcg(const __grid_constant__ 
       }
       qaf += acc;
     }
-    double qa[1] = {(double)qaf};
-    cluster_sum<1, CL>(cl, qa, next_slot(), red, bcast);
-    const double pap = qa[0];
-    if (!(pap > 0.0)) {  // not SPD in FP32 (or NaN)
+    float qa[1] = {qaf};
+    cluster_sum_f<1, CL>(cl, qa, wpart, next_fslot());
+    const float pap = qa[0];
+    if (!(pap > 0.f)) {  // not SPD in FP32 (or NaN)
       status = (pap == pap) ? COLAGB_SYS_BREAKDOWN : COLAGB_SYS_NAN;
       break;
     }
-    const float alpha = (float)(gamma / pap);
+    const float alpha = gamma / pap;
     // B: d += alpha p ; r -= alpha Ap ; |r|^2 ; <r, M r>  (own rows, 128-bit)
     float qb0 = 0.f, qb1 = 0.f;
     for (int64_t i = v0; i < i1; i += vstep) {
@@ -226,11 +230,11 @@ __global__ void __launch_bounds__(kCT, 1) k_cluster_pcg(const __grid_constant__ 
         }
       }
     }
-    double qb[2] = {(double)qb0, (double)qb1};
-    cluster_sum<2, CL>(cl, qb, next_slot(), red, bcast);
+    float qb[2] = {qb0, qb1};
+    cluster_sum_f<2, CL>(cl, qb, wpart, next_fslot());
     ++it;
-    rn = (float)sqrt(qb[0]);
-    double gamma_new = qb[1];
+    rn = sqrtf(qb[0]);
+    float gamma_new = qb[1];
     bool restart = false;
     if (!(rn == rn)) {
       status = COLAGB_SYS_NAN;
@@ -261,7 +265,7 @@ __global__ void __launch_bounds__(kCT, 1) k_cluster_pcg(const __grid_constant__ 
       relres_prev = rr;
       rn = (float)rr;
       rmax = rn;
-      gamma_new = q2[1];
+      gamma_new = (float)q2[1];
     }
     if (prec == COLAGB_PREC_FSAI || restart) {
       if (prec == COLAGB_PREC_FSAI) {
@@ -269,10 +273,10 @@ __global__ void __launch_bounds__(kCT, 1) k_cluster_pcg(const __grid_constant__ 
         cl.sync();
       }
       apply_z(q1);
-      cluster_sum<1, CL>(cl, q1, next_slot(), red, bcast);
+      cluster_sum_f<1, CL>(cl, q1, wpart, next_fslot());
       gamma_new = q1[0];
     }
-    const float beta = restart || gamma == 0.0 ? 0.f : (float)(gamma_new / gamma);
+    const float beta = restart || gamma == 0.f ? 0.f : gamma_new / gamma;
     gamma = gamma_new;
     // C: p = z + beta p
     const bool zstored = prec == COLAGB_PREC_FSAI || restart;
