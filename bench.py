@@ -4,7 +4,10 @@ Workload (one step): the 256 held-out instances of the 2-D variable-coefficient 
 (5-point CSR, n = 262,144, Matern-3/2 log-coefficient fields, seeds 5000-5255, b ~ N(0,1)), all
 solved in one batched call to |b - A x| / |b| <= 1e-8 measured in FP64.  The headline method is
 FP32 preconditioned CG inside FP64 iterative refinement with the learned FSAI preconditioner
-(Jacobi fallback); plain CG and Jacobi-PCG run through the same kernel for comparison.
+(Jacobi fallback); plain CG and Jacobi-PCG run through the same kernel for comparison.  Every timed
+step includes the build of the step's preconditioner (the network's inference and the assembly of
+G for all 256 operators); the network's weights and the pattern of G, which depend only on the
+mesh, are loaded once before timing.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--method M]
 
@@ -169,14 +172,28 @@ def bytes_per_replacement(n, nnz):
     return nnz * 4 + 24 * n + 20 * n
 
 
-def make_preconditioner(method, fam, coeff, dev):
-    """(pattern, G values) of the FSAI factor: trained network ("learned") or closed form ("fsai")."""
+def preconditioner_builder(method, fam, dev):
+    """The per-family preconditioner build, run inside every timed step: `build(family)` returns the
+    (pattern, G values) of the FSAI factor from the trained network ("learned": stencil extraction,
+    features, three convolutions, assembly) or in closed form ("fsai": stencil, assembly), None for
+    the other methods.  What depends only on the mesh -- the network's weights and the pattern of G --
+    is loaded / analysed once, here."""
+    from cola_gb300.linalg.batched import FsaiPattern
     from cola_gb300.precond import learned_fsai
+    if method not in ("learned", "fsai"):
+        return lambda f: None
+    net = None
     if method == "learned":
-        return learned_fsai.preconditioner_for(fam, coeff)
-    if method == "fsai":
-        return learned_fsai.g_values(fam, None)
-    return None
+        if not learned_fsai.WEIGHTS.exists():
+            raise FileNotFoundError(f"trained weights {learned_fsai.WEIGHTS} not found")
+        net = learned_fsai.FsaiNet.load(learned_fsai.WEIGHTS, device=dev)
+    pat = FsaiPattern(fam.indptr, fam.indices)
+    return lambda f: learned_fsai.g_values(f, net, pat)
+
+
+# this library's kernels per batch of 64 systems in a preconditioner build (learned_fsai.g_values):
+# the stencil extraction and the fused build (network + assembly, or the closed form)
+BUILD_LAUNCHES_PER_64 = {"learned": 2, "fsai": 2}
 
 
 PRECOND = {"plain": "none", "jacobi": "jacobi", "learned": "fsai", "fsai": "fsai"}
@@ -190,13 +207,14 @@ KERNEL_OF = {"onchip": "k_onchip_pcg", "cluster8": "k_cluster_pcg", "cluster16":
 
 
 def launches_per_solve(schedule, method, systems):
-    """This library's kernels per solve call: per chunk of <= 1024 systems the on-chip schedule runs
-    the pattern analysis (bitmap + collect, for A and, with FSAI, for G) and the solve kernel; the
-    other schedules one solve kernel."""
+    """This library's kernels per timed step: the preconditioner build, then per chunk of <= 1024
+    systems the on-chip schedule runs the pattern analysis (bitmap + collect, for A and, with FSAI,
+    for G) and the solve kernel; the other schedules one solve kernel."""
     chunks = (systems + 1023) // 1024
+    build = BUILD_LAUNCHES_PER_64.get(method, 0) * ((systems + 63) // 64)
     if schedule == "onchip":
-        return chunks * (1 + 2 * (2 if PRECOND[method] == "fsai" else 1))
-    return chunks
+        return build + chunks * (1 + 2 * (2 if PRECOND[method] == "fsai" else 1))
+    return build + chunks
 
 
 def run_ours(args, world, rank, local):
@@ -211,25 +229,28 @@ def run_ours(args, world, rank, local):
     fam, B, coeff, _ = diffusion_family_2d(shard_seeds(rank, args.systems), m=args.m, device=dev)
     n, nnz = fam.n, fam.indices.numel()
     method = args.method
-    fsai = None
-    if method in ("learned", "fsai"):
-        try:
-            fsai = make_preconditioner(method, fam, coeff, dev)
-        except FileNotFoundError as e:  # trained weights missing: say so and time Jacobi-PCG
-            print(f"# learned preconditioner unavailable ({e}); timing jacobi", file=sys.stderr)
-            method = "jacobi"
+    try:
+        build = preconditioner_builder(method, fam, dev)
+    except FileNotFoundError as e:  # trained weights missing: say so and time Jacobi-PCG
+        print(f"# learned preconditioner unavailable ({e}); timing jacobi", file=sys.stderr)
+        method = "jacobi"
+        build = preconditioner_builder(method, fam, dev)
     prec = PRECOND[method]
-    kw = dict(precond=prec, tol=1e-8, inner_tol=args.inner_tol, fsai=fsai, mode=args.mode, schedule=args.schedule)
+    kw = dict(precond=prec, tol=1e-8, inner_tol=args.inner_tol, mode=args.mode, schedule=args.schedule)
     st = torch.cuda.current_stream(dev)
 
-    def step():
-        return solve_batched(fam, B, **kw)
+    def step(mid=None):
+        # the preconditioner of this family is built inside the step, then every system is solved
+        fs = build(fam)
+        if mid is not None:
+            mid.record(st)
+        return solve_batched(fam, B, fsai=fs, **kw)
 
     for _ in range(args.warmup):
         X, info = step()
     torch.cuda.synchronize()
     barrier(world)
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    ev = [tuple(torch.cuda.Event(enable_timing=True) for _ in range(3)) for _ in range(args.steps)]
     iters_total = 0
     sweeps = []
     with Clocks(local) as clk:
@@ -237,45 +258,76 @@ def run_ours(args, world, rank, local):
         t0 = time.perf_counter()
         for i in range(args.steps):
             ev[i][0].record(st)
-            X, info = step()
+            X, info = step(ev[i][2])
             ev[i][1].record(st)
             iters_total += int(info["iterations"].sum().item())
             sweeps.append(info["sweeps"])
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
     barrier(world)
-    ms = [a.elapsed_time(b) for a, b in ev]
+    ms = [a.elapsed_time(b) for a, b, _ in ev]
     t_dev = sum(ms) / 1e3
+    t_solve = sum(m.elapsed_time(b) for _, b, m in ev) / 1e3   # the solve call alone (build excluded)
     t_max = max_over_ranks(t_dev, world)
     relres_max = float(info["relres"].max().item())
     status_ok = bool(torch.all((info["status"] == 1) | (info["status"] == 5)).item())
     value = world * args.systems * args.steps / t_max
 
-    # end to end through the public API from pinned host buffers: H2D of the family values and the
-    # right-hand sides, the solve, D2H of the solutions
+    # end to end through the public API from pinned host buffers: every step copies its family's
+    # values and right-hand sides in (H2D), builds the preconditioner, solves and copies the solutions
+    # out (D2H).  The copies run on two copy streams and overlap the neighbouring steps' solves
+    # (double-buffered device inputs), the way a stream of families would be fed.
     vals_h = fam.values.cpu().pin_memory()
     B_h = B.cpu().pin_memory()
-    X_h = torch.empty_like(B_h).pin_memory()
-    e2e_steps = max(1, min(args.steps, 2))
+    X_h = [torch.empty_like(B_h).pin_memory() for _ in range(2)]
+    e2e_steps = max(1, args.steps)
     from cola_gb300.linalg.batched import BatchedCSR
+    h2d_s, d2h_s = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+    vals_buf = [torch.empty_like(fam.values) for _ in range(2)]
+    B_buf = [torch.empty_like(B) for _ in range(2)]
+    free = [torch.cuda.Event() for _ in range(2)]   # input buffer k no longer read by its solve
+    for k in range(2):
+        free[k].record(st)
 
-    def e2e_step():
-        vals_d = vals_h.to(dev, non_blocking=True)
-        B_d = B_h.to(dev, non_blocking=True)
-        Xd, _ = solve_batched(BatchedCSR(fam.indptr, fam.indices, vals_d), B_d, **kw)
-        X_h.copy_(Xd, non_blocking=True)
+    def e2e_run(nsteps, marks=None):
+        for i in range(nsteps):
+            k = i % 2
+            with torch.cuda.stream(h2d_s):
+                h2d_s.wait_event(free[k])
+                vals_buf[k].copy_(vals_h, non_blocking=True)
+                B_buf[k].copy_(B_h, non_blocking=True)
+                arrived = torch.cuda.Event()
+                arrived.record(h2d_s)
+            st.wait_event(arrived)
+            if marks:
+                marks[i][0].record(st)
+            fam_d = BatchedCSR(fam.indptr, fam.indices, vals_buf[k])
+            Xd, _ = solve_batched(fam_d, B_buf[k], fsai=build(fam_d), wait=False, **kw)
+            free[k].record(st)
+            if marks:
+                marks[i][1].record(st)
+            with torch.cuda.stream(d2h_s):
+                d2h_s.wait_event(free[k])
+                X_h[k].copy_(Xd, non_blocking=True)
+            Xd.record_stream(d2h_s)
+        st.wait_stream(d2h_s)
 
-    e2e_step()  # untimed: the device buffers of this path come from the allocator's cache afterwards
+    e2e_run(1)  # untimed: the device buffers of this path come from the allocator's cache afterwards
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    marks = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(e2e_steps)]
     e0.record(st)
-    for _ in range(e2e_steps):
-        e2e_step()
+    e2e_run(e2e_steps, marks)
     e1.record(st)
     torch.cuda.synchronize()
     t_e2e = max_over_ranks(e0.elapsed_time(e1) / 1e3, world)
+    solve_ms = sum(m[0].elapsed_time(m[1]) for m in marks)
     e2e = {"value": world * args.systems * e2e_steps / t_e2e, "unit": UNIT,
-           "h2d_bytes_per_step": vals_h.numel() * 4 + B_h.numel() * 8, "d2h_bytes_per_step": X_h.numel() * 8}
+           "h2d_bytes_per_step": vals_h.numel() * 4 + B_h.numel() * 8, "d2h_bytes_per_step": X_h[0].numel() * 8,
+           "ms_per_step": 1e3 * t_e2e / e2e_steps, "steps": e2e_steps,
+           "copies": "H2D and D2H on two copy streams, overlapping the neighbouring steps' solves",
+           "split_ms": {"first_h2d": e0.elapsed_time(marks[0][0]), "build_and_solve_per_step": solve_ms / e2e_steps,
+                        "last_d2h": marks[-1][1].elapsed_time(e1)}}
 
     peak, peak_kind = peaks()
     # CG steps only: the FP64 residual replacements (about 1 % of the traffic) are left out, so the
@@ -283,7 +335,8 @@ def run_ours(args, world, rank, local):
     sched_ran = info.get("schedule", args.schedule)
     nd, nm = diagonal_counts(fam)
     alg_bytes_step = (iters_total / args.steps) * bytes_per_system_iter(n, nnz, method, sched_ran, nd, nm)
-    achieved = alg_bytes_step / (t_dev / args.steps) / 1e9
+    # over the solve call (pattern analysis + k_onchip_pcg); the preconditioner build is timed apart
+    achieved = alg_bytes_step / (t_solve / args.steps) / 1e9
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -304,7 +357,9 @@ def run_ours(args, world, rank, local):
                                      else None,
                      "peak_kind": peak_kind,
                      "kernel": KERNEL_OF.get(sched_ran, "k_cluster_pcg"), "schedule": sched_ran,
-                     "alg_bytes_per_launch": alg_bytes_step},
+                     "alg_bytes_per_launch": alg_bytes_step,
+                     "solve_ms_per_step": 1e3 * t_solve / args.steps,
+                     "build_ms_per_step": 1e3 * (t_dev - t_solve) / args.steps},
         "gpu_launches": args.steps * launches_per_solve(sched_ran, method, args.systems),
         "wall_s_timed": wall,
     }
@@ -316,19 +371,17 @@ def run_ours(args, world, rank, local):
         for mth in args.compare.split(","):
             if mth == method:
                 continue
-            fsai2 = None
-            if mth in ("learned", "fsai"):
-                try:
-                    fsai2 = make_preconditioner(mth, fam, coeff, dev)
-                except FileNotFoundError:
-                    continue
-            kw2 = dict(precond=PRECOND[mth], tol=1e-8, inner_tol=args.inner_tol, fsai=fsai2, mode=args.mode,
+            try:
+                build2 = preconditioner_builder(mth, fam, dev)
+            except FileNotFoundError:
+                continue
+            kw2 = dict(precond=PRECOND[mth], tol=1e-8, inner_tol=args.inner_tol, mode=args.mode,
                        schedule=args.schedule)
-            solve_batched(fam, B, **kw2)
+            solve_batched(fam, B, fsai=build2(fam), **kw2)
             torch.cuda.synchronize()
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(st)
-            _, inf2 = solve_batched(fam, B, **kw2)
+            _, inf2 = solve_batched(fam, B, fsai=build2(fam), **kw2)
             b.record(st)
             torch.cuda.synchronize()
             t2 = a.elapsed_time(b) / 1e3

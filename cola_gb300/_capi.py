@@ -67,7 +67,7 @@ class BatchedCsr(C.Structure):
 class IrParams(C.Structure):
     _fields_ = [("tol", C.c_double), ("inner_tol", C.c_double), ("max_sweeps", C.c_int32),
                 ("max_inner_iters", C.c_int32), ("preconditioner", C.c_int32), ("fallback", C.c_int32),
-                ("spin_limit", C.c_int64), ("mode", C.c_int32), ("schedule", C.c_int32)]
+                ("spin_limit", C.c_int64), ("mode", C.c_int32), ("schedule", C.c_int32), ("no_wait", C.c_int32)]
 
 
 class IrResult(C.Structure):
@@ -113,6 +113,8 @@ SIGNATURES = {
     "colagb_fsai_features": (C.c_int, [_vp, _i64, _i64, _vp, _vp]),
     "colagb_fsai_assemble": (C.c_int, [_vp, _vp, _i64, _i64, _vp, _vp]),
     "colagb_fsai_compact": (C.c_int, [_vp, _vp, _i64, _i64, _i64, _vp, _vp]),
+    "colagb_fsai_net_build": (C.c_int, [_vp, _vp, _i64, _i64, _i64, _vp, _i64, _vp, _vp]),
+    "colagb_fsai_closed_build": (C.c_int, [_vp, _i64, _i64, _vp, _i64, _vp, _vp]),
     "colagb_conv3x3_forward": (C.c_int, [_vp, _i64, _i32, _i32, _i64, _i64, _vp, _vp, _i32, _vp, _vp]),
     "colagb_conv3x3_backward_scratch_bytes": (C.c_int, [_i32, _i32, _P(_sz)]),
     "colagb_conv3x3_backward": (C.c_int, [_vp, _vp, _vp, _i64, _i32, _i32, _i64, _i64, _vp, _vp, _vp, _vp, _sz,

@@ -770,6 +770,10 @@ extern "C" int colagb_cg_batched_csr_solve(const colagb_batched_csr* A, const do
                                      per_system_status ? per_system_status + s0 : nullptr,
                                      relres ? relres + s0 : nullptr, w.r, w.p, w.ap, w.d, w.z, w.t, w.dinv, w.nrep,
                                      csize, st));
+      if (params->no_wait) {
+        result->sweeps = -1;
+        continue;
+      }
       int mx[2] = {0, 0};
       std::vector<int> hrep(S);
       COLAGB_CUDA(cudaMemcpyAsync(hrep.data(), w.nrep, S * sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -191,6 +191,200 @@ __global__ void __launch_bounds__(256) k_conv3_fwd(const float* __restrict__ in,
   }
 }
 
+// ---------------------------------------------------------------------------------------------
+// The preconditioner build of the trained network in one pass.  One CTA builds a 32 x 32 tile of
+// cells: features -> conv 6->16 (ReLU) -> conv 16->16 (ReLU) -> conv 16->3, of whose output only
+// channels 1 and 2 are evaluated (the assembly reads no other) -> normalised G row -> CSR values.
+// Each layer is evaluated on the tile plus the halo the layers after it read (38^2 feature cells,
+// then 36^2, 34^2, 32^2), all in shared memory.  Cells outside the grid hold 0 in every layer -- the
+// zero padding of the layer-by-layer evaluation -- and every output is the same chain of FMAs in
+// the same order as in k_fsai_features -> k_conv3_fwd x 3 -> k_fsai_assemble -> k_fsai_compact.
+//
+// Work split: item k of thread t covers cell lt + k * (512 / NG) of the layer's region and output
+// channels grp * CG .. grp * CG + CG - 1 (grp = t / (512 / NG)), so that the CG weights of one
+// (input channel, tap) -- one or two 128-bit shared loads, the same address for the whole warp --
+// serve every item of the thread.  Layer 1: 1296 cells x 16 channels as 3 items; layer 2: 1156
+// cells as 5 items of 8 channels; layer 3: 1024 cells x 2 channels as 2 items.
+constexpr int kNetTile = 32;
+constexpr int kNetThreads = 512;
+constexpr int kNetF = kNetTile + 6;               // side of the feature region
+constexpr int kNetBufA = 16 * (kNetTile + 2) * (kNetTile + 2);  // features (6 x 38^2), later h2 (16 x 34^2)
+constexpr int kNetBufB = 16 * (kNetTile + 4) * (kNetTile + 4);  // h1 (16 x 36^2)
+constexpr int kNetW1 = 6 * 9 * 16, kNetW2 = 16 * 9 * 16, kNetW3 = 16 * 9 * 2;
+constexpr int kNetParams = 16 * 6 * 9 + 16 + 16 * 16 * 9 + 16 + 3 * 16 * 9 + 3;  // FsaiNet's flat layout
+constexpr size_t kNetSmemBytes = (size_t)(kNetBufA + kNetBufB + kNetW1 + kNetW2 + kNetW3 + 16 + 16 + 4) * sizeof(float);
+static_assert(6 * kNetF * kNetF <= kNetBufA, "features fit in buffer A");
+static_assert(kNetBufA % 4 == 0 && kNetBufB % 4 == 0 && kNetW1 % 4 == 0, "weights 16-byte aligned");
+
+template <int CIN, int COUT, int NG, int RIN, int PPT>
+__device__ __forceinline__ void net_conv(const float* in, const float* w, const float* b,
+                                         float (&acc)[PPT][COUT / NG], int& grp, int& lt) {
+  constexpr int CG = COUT / NG, TPG = kNetThreads / NG, ROUT = RIN - 2, NP = ROUT * ROUT, PIN = RIN * RIN;
+  static_assert(PPT * TPG >= NP && (PPT - 1) * TPG < NP, "items per thread");
+  static_assert(CG % 4 == 0 || CG == 2, "weight vector width");
+  grp = threadIdx.x / TPG;
+  lt = threadIdx.x % TPG;
+  int base[PPT];
+#pragma unroll
+  for (int k = 0; k < PPT; ++k) {
+    const int q = lt + k * TPG;
+    base[k] = q < NP ? (q / ROUT) * RIN + q % ROUT : 0;  // items past the region read cell 0, discarded
+  }
+  const float* wg = w + grp * CG;
+#pragma unroll
+  for (int k = 0; k < PPT; ++k)
+#pragma unroll
+    for (int c = 0; c < CG; ++c) acc[k][c] = b[grp * CG + c];
+#pragma unroll 1
+  for (int ci = 0; ci < CIN; ++ci) {
+    const float* src = in + ci * PIN;
+    const float* wc = wg + ci * 9 * COUT;
+#pragma unroll
+    for (int t = 0; t < 9; ++t) {
+      const int off = (t / 3) * RIN + t % 3;
+      float wv[CG];
+      if constexpr (CG % 4 == 0) {
+#pragma unroll
+        for (int c4 = 0; c4 < CG / 4; ++c4) {
+          const float4 x = *reinterpret_cast<const float4*>(wc + t * COUT + 4 * c4);
+          wv[4 * c4] = x.x; wv[4 * c4 + 1] = x.y; wv[4 * c4 + 2] = x.z; wv[4 * c4 + 3] = x.w;
+        }
+      } else {
+        const float2 x = *reinterpret_cast<const float2*>(wc + t * COUT);
+        wv[0] = x.x; wv[1] = x.y;
+      }
+#pragma unroll
+      for (int k = 0; k < PPT; ++k) {
+        const float v = src[base[k] + off];
+#pragma unroll
+        for (int c = 0; c < CG; ++c) acc[k][c] += wv[c] * v;
+      }
+    }
+  }
+}
+
+// ReLU'd layer output into its shared region (ROUT^2 cells from grid cell (oy, ox)); 0 off the grid
+template <int COUT, int NG, int ROUT, int PPT>
+__device__ __forceinline__ void net_store(const float (&acc)[PPT][COUT / NG], int grp, int lt, float* out, int oy, int ox,
+                                          int64_t m) {
+  constexpr int CG = COUT / NG, TPG = kNetThreads / NG, NP = ROUT * ROUT;
+#pragma unroll
+  for (int k = 0; k < PPT; ++k) {
+    const int q = lt + k * TPG;
+    if (q < NP) {
+      const int y = oy + q / ROUT, x = ox + q % ROUT;
+      const bool inside = y >= 0 && y < m && x >= 0 && x < m;
+#pragma unroll
+      for (int c = 0; c < CG; ++c) out[(grp * CG + c) * NP + q] = inside ? fmaxf(acc[k][c], 0.f) : 0.f;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kNetThreads, 1)
+    k_fsai_net_build(const float* __restrict__ st, const float* __restrict__ params, int64_t m, int64_t S,
+                     const int32_t* __restrict__ g_indptr, int64_t g_nnz, float* __restrict__ out) {
+  extern __shared__ __align__(16) float nsm[];
+  float* bufA = nsm;
+  float* bufB = bufA + kNetBufA;
+  float* w1 = bufB + kNetBufB;
+  float* w2 = w1 + kNetW1;
+  float* w3 = w2 + kNetW2;
+  float* b1 = w3 + kNetW3;
+  float* b2 = b1 + 16;
+  float* b3 = b2 + 16;
+  const int tid = threadIdx.x;
+  // weights W (cout, cin, 3, 3) then b (cout) per layer -> [(ci * 9 + tap) * cout + co]
+  for (int u = tid; u < 16 * 6 * 9; u += kNetThreads) w1[((u / 9) % 6 * 9 + u % 9) * 16 + u / 54] = params[u];
+  for (int u = tid; u < 16 * 16 * 9; u += kNetThreads) w2[((u / 9) % 16 * 9 + u % 9) * 16 + u / 144] = params[880 + u];
+  for (int u = tid; u < 2 * 16 * 9; u += kNetThreads) {
+    const int co = 1 + u / 144;  // output channels 1 and 2 of the last layer
+    w3[((u / 9) % 16 * 9 + u % 9) * 2 + co - 1] = params[3200 + co * 144 + u % 144];
+  }
+  if (tid < 16) {
+    b1[tid] = params[864 + tid];
+    b2[tid] = params[3184 + tid];
+  }
+  if (tid < 2) b3[tid] = params[3632 + 1 + tid];
+
+  const int64_t n = m * m;
+  const int64_t side = (m + kNetTile - 1) / kNetTile, per_sys = side * side;
+  for (int64_t tile = blockIdx.x; tile < per_sys * S; tile += gridDim.x) {
+    const int64_t s = tile / per_sys, r = tile % per_sys;
+    const int y0 = (int)(r / side) * kNetTile, x0 = (int)(r % side) * kNetTile;
+    const float* a = st + s * 5 * n;
+    __syncthreads();  // weights in; the previous tile's reads of buffer A done
+    // features (as k_fsai_features) on the 38^2 region from (y0 - 3, x0 - 3)
+    for (int q = tid; q < kNetF * kNetF; q += kNetThreads) {
+      const int y = y0 - 3 + q / kNetF, x = x0 - 3 + q % kNetF;
+      float f[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      if (y >= 0 && y < m && x >= 0 && x < m) {
+        const int64_t p = (int64_t)y * m + x;
+        const float d = at5(a, n, 2, p);
+        f[0] = -at5(a, n, 0, p) / d;
+        f[1] = -at5(a, n, 1, p) / d;
+        f[2] = -at5(a, n, 3, p) / d;
+        f[3] = -at5(a, n, 4, p) / d;
+        f[4] = y > 0 ? logf(d / at5(a, n, 2, p - m)) : 0.f;
+        f[5] = x > 0 ? logf(d / at5(a, n, 2, p - 1)) : 0.f;
+      }
+#pragma unroll
+      for (int c = 0; c < 6; ++c) bufA[c * kNetF * kNetF + q] = f[c];
+    }
+    __syncthreads();
+    {
+      float acc[3][16];
+      int grp, lt;
+      net_conv<6, 16, 1, kNetTile + 6, 3>(bufA, w1, b1, acc, grp, lt);
+      net_store<16, 1, kNetTile + 4, 3>(acc, grp, lt, bufB, y0 - 2, x0 - 2, m);
+    }
+    __syncthreads();
+    {
+      float acc[5][8];
+      int grp, lt;
+      net_conv<16, 16, 2, kNetTile + 4, 5>(bufB, w2, b2, acc, grp, lt);
+      net_store<16, 2, kNetTile + 2, 5>(acc, grp, lt, bufA, y0 - 1, x0 - 1, m);
+    }
+    __syncthreads();
+    {
+      float acc[2][2];
+      int grp, lt;
+      net_conv<16, 2, 1, kNetTile + 2, 2>(bufA, w3, b3, acc, grp, lt);
+      float* o = out + s * g_nnz;
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const int q = lt + k * kNetThreads;
+        const int y = y0 + q / kNetTile, x = x0 + q % kNetTile;
+        if (y < m && x < m) {
+          const int64_t p = (int64_t)y * m + x;
+          const FsaiRow row = fsai_row(a, n, m, p, acc[k][0], acc[k][1]);
+          const float is = rsqrtf(row.s);
+          int64_t e = g_indptr[p];
+          if (y > 0) o[e++] = row.hN * is;
+          if (x > 0) o[e++] = row.hW * is;
+          o[e] = row.hC * is;
+        }
+      }
+    }
+  }
+}
+
+// closed-form FSAI straight to CSR values (k_fsai_assemble with o = 0, then k_fsai_compact)
+__global__ void k_fsai_closed_build(const float* __restrict__ st, int64_t m, int64_t S,
+                                    const int32_t* __restrict__ g_indptr, int64_t g_nnz, float* __restrict__ out) {
+  const int64_t n = m * m;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < S * n; u += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s = u / n, p = u % n;
+    const int64_t i = p / m, j = p % m;
+    float fN, fW, fC;
+    fsai_closed_form(st + s * 5 * n, n, m, p, fN, fW, fC);
+    float* o = out + s * g_nnz;
+    int64_t e = g_indptr[p];
+    if (i > 0) o[e++] = fN;
+    if (j > 0) o[e++] = fW;
+    o[e] = fC;
+  }
+}
+
 // grad_in (B, CIN, H, W) from grad_out (B, cout, H, W); when `act` is given the forward output
 // was ReLU(act) and grad_out is masked by act > 0.
 template <int CIN>
@@ -532,6 +726,34 @@ extern "C" int colagb_fsai_compact(const float* g_stencil, const int32_t* g_indp
     return fail(COLAGB_ERR_INVALID, "colagb_fsai_compact: bad arguments");
   if (S == 0) return COLAGB_OK;
   k_fsai_compact<<<grid_for(S * m * m), 256, 0, as_stream(stream)>>>(g_stencil, g_indptr, m, S, g_nnz, g_values);
+  COLAGB_CUDA(cudaGetLastError());
+  return COLAGB_OK;
+}
+
+extern "C" int colagb_fsai_net_build(const float* stencil, const float* params, int64_t n_params, int64_t m, int64_t S,
+                                     const int32_t* g_indptr, int64_t g_nnz, float* g_values, void* stream) {
+  if (!stencil || !params || !g_indptr || !g_values || m < 1 || S < 0)
+    return fail(COLAGB_ERR_INVALID, "colagb_fsai_net_build: bad arguments");
+  if (n_params != kNetParams)
+    return fail(COLAGB_ERR_INVALID, "colagb_fsai_net_build: the network has " + std::to_string(kNetParams) +
+                                        " parameters (6->16->16->3 3x3 convolutions), got " + std::to_string(n_params));
+  if (S == 0) return COLAGB_OK;
+  COLAGB_CUDA(cudaFuncSetAttribute(k_fsai_net_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kNetSmemBytes));
+  const int64_t side = (m + kNetTile - 1) / kNetTile;
+  const int64_t tiles = side * side * S;
+  const int grid = (int)std::min<int64_t>(tiles, num_sms());
+  k_fsai_net_build<<<grid, kNetThreads, kNetSmemBytes, as_stream(stream)>>>(stencil, params, m, S, g_indptr, g_nnz,
+                                                                            g_values);
+  COLAGB_CUDA(cudaGetLastError());
+  return COLAGB_OK;
+}
+
+extern "C" int colagb_fsai_closed_build(const float* stencil, int64_t m, int64_t S, const int32_t* g_indptr,
+                                        int64_t g_nnz, float* g_values, void* stream) {
+  if (!stencil || !g_indptr || !g_values || m < 1 || S < 0)
+    return fail(COLAGB_ERR_INVALID, "colagb_fsai_closed_build: bad arguments");
+  if (S == 0) return COLAGB_OK;
+  k_fsai_closed_build<<<grid_for(S * m * m), 256, 0, as_stream(stream)>>>(stencil, m, S, g_indptr, g_nnz, g_values);
   COLAGB_CUDA(cudaGetLastError());
   return COLAGB_OK;
 }

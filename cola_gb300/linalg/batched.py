@@ -146,7 +146,7 @@ def onchip_schedule_info(n: int, halo: int) -> dict:
 def solve_batched(A: BatchedCSR, B: torch.Tensor, precond: str = "jacobi", tol: float = 1e-8,
                   inner_tol: float | None = None, max_sweeps: int = 200, max_inner_iters: int = 50000,
                   fsai: tuple | None = None, fallback: bool = True, mode: str = "reliable",
-                  schedule: str = "auto"):
+                  schedule: str = "auto", wait: bool = True):
     """Solve A_s x_s = b_s for every system s to |b_s - A_s x_s| / |b_s| <= tol (FP64 residual).
 
     Args:
@@ -162,6 +162,10 @@ def solve_batched(A: BatchedCSR, B: torch.Tensor, precond: str = "jacobi", tol: 
             constant-offset diagonals, n <= 262144); "cluster8" / "cluster16" -- one cluster per system
             on the CSR pattern, vectors in global memory; "grid" -- one cooperative grid that advances
             every system together; "auto" (default) -- "onchip" when it applies, else a cluster.
+        wait: False returns once the solve is enqueued on the current stream (the on-chip and cluster
+            schedules); X and the per-system tensors of info are then ready in stream order and
+            info["sweeps"] is None.  Later calls on other streams must not run before it completes
+            (the library's scratch buffer is shared).
     Returns (X (S, n) float64, info) with per-system iterations, status and FP64 relative residuals.
     """
     _capi.require_cuda(A.values, B)
@@ -198,7 +202,7 @@ def solve_batched(A: BatchedCSR, B: torch.Tensor, precond: str = "jacobi", tol: 
     prm = _capi.IrParams(tol=float(tol), inner_tol=float(inner_tol), max_sweeps=int(max_sweeps),
                          max_inner_iters=int(max_inner_iters), preconditioner=pk, fallback=1 if fallback else 0,
                          spin_limit=0, mode=_capi.IR_RELIABLE if mode == "reliable" else _capi.IR_RESTART,
-                         schedule=_SCHED[schedule])
+                         schedule=_SCHED[schedule], no_wait=0 if wait else 1)
     iters = torch.zeros(S, dtype=torch.int32, device=dev)
     status = torch.zeros(S, dtype=torch.int32, device=dev)
     relres = torch.zeros(S, dtype=torch.float64, device=dev)
@@ -209,7 +213,8 @@ def solve_batched(A: BatchedCSR, B: torch.Tensor, precond: str = "jacobi", tol: 
     _capi.check(lib.colagb_cg_batched_csr_solve(C.byref(desc), Bd.data_ptr(), X.data_ptr(), C.byref(prm),
                                                 iters.data_ptr(), status.data_ptr(), relres.data_ptr(), ws.data_ptr(),
                                                 nbytes.value, C.byref(res), _capi.stream_ptr(dev)), "batched cg")
-    info = {"iterations": iters, "status": status, "relres": relres, "replacements": int(res.sweeps),
-            "sweeps": int(res.sweeps), "max_iterations": int(res.total_inner_iters),
+    swp = int(res.sweeps) if res.sweeps >= 0 else None
+    info = {"iterations": iters, "status": status, "relres": relres, "replacements": swp,
+            "sweeps": swp, "max_iterations": int(res.total_inner_iters),
             "schedule": _SCHED_NAME.get(int(res.schedule), "auto")}
     return X, info

@@ -121,18 +121,28 @@ def grid_side(fam: BatchedCSR) -> int:
     return m
 
 
-def stencil(fam: BatchedCSR, m: int | None = None) -> torch.Tensor:
-    """(S, 5, m, m) [N, W, C, E, S] stencil of every operator of the family."""
+def stencil(fam: BatchedCSR, m: int | None = None, err: torch.Tensor | None = None) -> torch.Tensor:
+    """(S, 5, m, m) [N, W, C, E, S] stencil of every operator of the family.
+
+    With ``err`` (a device int32 flag) the pattern check is left to the caller, who reads the flag
+    once after several calls; without it the flag is read here."""
     m = m or grid_side(fam)
     S = fam.num_systems
     st = torch.empty((S, 5, m, m), dtype=torch.float32, device=fam.values.device)
-    err = torch.zeros(1, dtype=torch.int32, device=fam.values.device)
+    own = err is None
+    if own:
+        err = torch.zeros(1, dtype=torch.int32, device=fam.values.device)
     vals = fam.values.to(torch.float32).contiguous()
     _capi.check(_lib().colagb_grid5_stencil(fam.indptr.data_ptr(), fam.indices.data_ptr(), vals.data_ptr(),
                                             fam.indices.numel(), m, S, st.data_ptr(), err.data_ptr(), _sp(st)), "stencil")
+    if own:
+        check_stencil(err)
+    return st
+
+
+def check_stencil(err: torch.Tensor):
     if int(err.item()) != 0:
         raise ValueError("operator pattern is not the 5-point stencil of an m x m grid")
-    return st
 
 
 def features(st: torch.Tensor) -> torch.Tensor:
@@ -150,9 +160,11 @@ def assemble(st: torch.Tensor, o: torch.Tensor | None) -> torch.Tensor:
     return g
 
 
-def compact(gst: torch.Tensor, pat: FsaiPattern) -> torch.Tensor:
+def compact(gst: torch.Tensor, pat: FsaiPattern, out: torch.Tensor | None = None) -> torch.Tensor:
+    """G values on the CSR pattern of G, (S, g_nnz); ``out``: a contiguous tensor of that shape."""
     S, _, m, _ = gst.shape
-    out = torch.empty((S, pat.g_nnz), dtype=torch.float32, device=gst.device)
+    if out is None:
+        out = torch.empty((S, pat.g_nnz), dtype=torch.float32, device=gst.device)
     _capi.check(_lib().colagb_fsai_compact(gst.data_ptr(), pat.g_indptr.data_ptr(), m, S, pat.g_nnz, out.data_ptr(),
                                            _sp(gst)), "compact")
     return out
@@ -192,17 +204,44 @@ def rq_loss_and_grad(st, o, gst, r, e, w, want_grad=True):
 # ---------------------------------------------------------------------------------------------
 # inference and training
 
-def g_values(fam: BatchedCSR, net: FsaiNet | None, pat: FsaiPattern | None = None, batch: int = 32):
-    """Compact G values (S, g_nnz) for the batched solver; net=None gives closed-form FSAI."""
+def g_values(fam: BatchedCSR, net: FsaiNet | None, pat: FsaiPattern | None = None, batch: int = 64):
+    """Compact G values (S, g_nnz) for the batched solver; net=None gives closed-form FSAI.
+
+    Two kernels per batch of systems: the stencil extraction and the fused build
+    (colagb_fsai_net_build: features, the network and the assembly in shared memory, or
+    colagb_fsai_closed_build)."""
     m = grid_side(fam)
     pat = pat or FsaiPattern(fam.indptr, fam.indices)
-    out = []
+    out = torch.empty((fam.num_systems, pat.g_nnz), dtype=torch.float32, device=fam.values.device)
+    err = torch.zeros(1, dtype=torch.int32, device=fam.values.device)
+    lib = _lib()
+    for s0 in range(0, fam.num_systems, batch):
+        sub = BatchedCSR(fam.indptr, fam.indices, fam.values[s0: s0 + batch])
+        st = stencil(sub, m, err)
+        dst = out[s0: s0 + batch]
+        if net is not None:
+            _capi.check(lib.colagb_fsai_net_build(st.data_ptr(), net.params.data_ptr(), net.params.numel(), m,
+                                                  sub.num_systems, pat.g_indptr.data_ptr(), pat.g_nnz,
+                                                  dst.data_ptr(), _sp(st)), "net build")
+        else:
+            _capi.check(lib.colagb_fsai_closed_build(st.data_ptr(), m, sub.num_systems, pat.g_indptr.data_ptr(),
+                                                     pat.g_nnz, dst.data_ptr(), _sp(st)), "closed build")
+    check_stencil(err)  # one host read for all batches
+    return pat, out
+
+
+def g_values_layered(fam: BatchedCSR, net: FsaiNet | None, pat: FsaiPattern | None = None, batch: int = 32):
+    """The same values as ``g_values``, layer by layer (features, each convolution, assembly and
+    compaction as separate kernels with their fields in device memory) -- the path training runs."""
+    m = grid_side(fam)
+    pat = pat or FsaiPattern(fam.indptr, fam.indices)
+    out = torch.empty((fam.num_systems, pat.g_nnz), dtype=torch.float32, device=fam.values.device)
     for s0 in range(0, fam.num_systems, batch):
         sub = BatchedCSR(fam.indptr, fam.indices, fam.values[s0: s0 + batch])
         st = stencil(sub, m)
         o = net.forward(features(st))[-1] if net is not None else None
-        out.append(compact(assemble(st, o), pat))
-    return pat, torch.cat(out)
+        compact(assemble(st, o), pat, out[s0: s0 + batch])
+    return pat, out
 
 
 def preconditioner_for(fam: BatchedCSR, coeff=None, net: FsaiNet | None = None, weights=WEIGHTS):

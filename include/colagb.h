@@ -193,6 +193,10 @@ typedef struct colagb_ir_params {
   int64_t spin_limit;    /* grid-barrier spin bound (0 = default) */
   int32_t mode;          /* COLAGB_IR_RELIABLE or COLAGB_IR_RESTART */
   int32_t schedule;      /* COLAGB_SCHED_* */
+  int32_t no_wait;       /* 1: the on-chip and cluster schedules return once the solve is enqueued
+                            (per-system outputs valid when the stream gets there, result->sweeps
+                            = -1); 0: wait and report the largest replacement count.  The grid
+                            schedule always waits (it reads its barrier-timeout flag). */
 } colagb_ir_params;
 
 #define COLAGB_SCHED_AUTO 0     /* on-chip when the pattern allows it, else a cluster per system */
@@ -210,7 +214,7 @@ typedef struct colagb_ir_params {
 int colagb_onchip_schedule_info(int64_t n, int32_t halo, int32_t* info);
 
 typedef struct colagb_ir_result {
-  int32_t sweeps;
+  int32_t sweeps;              /* largest FP64 residual replacement count (-1 with no_wait) */
   int32_t total_inner_iters;   /* sum over sweeps of the max inner iterations */
   int32_t status;              /* COLAGB_OK or COLAGB_ERR_TIMEOUT */
   int32_t schedule;            /* the COLAGB_SCHED_* that ran (AUTO resolved) */
@@ -319,6 +323,16 @@ int colagb_fsai_assemble(const float* stencil, const float* net_out, int64_t m, 
 /* G stencil -> CSR values (S, g_nnz) in the lower pattern order (for colagb_batched_csr.g_values) */
 int colagb_fsai_compact(const float* g_stencil, const int32_t* g_indptr, int64_t m, int64_t S, int64_t g_nnz,
                         float* g_values, void* stream);
+/* The preconditioner build in one pass: the CSR values (S, g_nnz) of the normalised learned factor
+ * from the stencil and the network's parameters (n_params = 3635 floats in FsaiNet's flat layout:
+ * per layer W (cout, cin, 3, 3) then b (cout), layers 6->16 ReLU, 16->16 ReLU, 16->3).  The same
+ * values as colagb_fsai_features -> 3 x colagb_conv3x3_forward -> colagb_fsai_assemble ->
+ * colagb_fsai_compact, without the intermediate fields. */
+int colagb_fsai_net_build(const float* stencil, const float* params, int64_t n_params, int64_t m, int64_t S,
+                          const int32_t* g_indptr, int64_t g_nnz, float* g_values, void* stream);
+/* closed-form FSAI straight to CSR values (colagb_fsai_assemble with NULL, then colagb_fsai_compact) */
+int colagb_fsai_closed_build(const float* stencil, int64_t m, int64_t S, const int32_t* g_indptr, int64_t g_nnz,
+                             float* g_values, void* stream);
 /* 3x3 convolution (padding 1): out (B, cout, H, W) = bias + w * in (B, cin, H, W); cout in {16, 3} */
 int colagb_conv3x3_forward(const float* in, int64_t B, int32_t cin, int32_t cout, int64_t H, int64_t W,
                            const float* weight, const float* bias, int32_t relu, float* out, void* stream);

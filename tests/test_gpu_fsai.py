@@ -174,3 +174,34 @@ def test_trained_network_beats_jacobi_on_held_out_512():
     _, ic = solve_batched(fam, B, precond="fsai", fsai=L.g_values(fam, None), tol=1e-8)
     it_c = float(ic["iterations"].double().mean())
     assert it_l < it_c, (it_l, it_c)
+
+
+@pytest.mark.parametrize("m", [20, 45, 64])
+def test_fused_build_matches_layered_path(m):
+    """colagb_fsai_net_build (features, three convolutions and the assembly of a 32 x 32 tile in
+    shared memory) gives the values of the layer-by-layer kernels; every layer random, biases too,
+    grids whose side is not a multiple of the tile.  Both evaluate the same FMAs in the same order,
+    so the comparison is to 1 ulp-level (2e-6 relative)."""
+    fam, _, _, _ = diffusion_family_2d(list(range(700, 705)), m=m, device=DEV)
+    net = L.FsaiNet(DEV, seed=3)
+    g = torch.Generator().manual_seed(11)
+    net.params.copy_((0.3 * torch.randn(net.params.shape, generator=g)).to(DEV))
+    pat = FsaiPattern(fam.indptr, fam.indices)
+    _, fused = L.g_values(fam, net, pat, batch=3)
+    _, layered = L.g_values_layered(fam, net, pat, batch=3)
+    assert torch.isfinite(fused).all()
+    assert (fused - layered).abs().max().item() <= 2e-6 * layered.abs().max().item()
+    _, cf = L.g_values(fam, None, pat)
+    _, cl = L.g_values_layered(fam, None, pat)
+    assert torch.equal(cf, cl)
+
+
+def test_fused_build_rejects_other_network_shapes():
+    fam, _, _, _ = diffusion_family_2d([1], m=16, device=DEV)
+    pat = FsaiPattern(fam.indptr, fam.indices)
+    st = L.stencil(fam, 16)
+    out = torch.empty((1, pat.g_nnz), dtype=torch.float32, device=DEV)
+    bad = torch.zeros(100, dtype=torch.float32, device=DEV)
+    rc = _capi.load().colagb_fsai_net_build(st.data_ptr(), bad.data_ptr(), bad.numel(), 16, 1, pat.g_indptr.data_ptr(),
+                                            pat.g_nnz, out.data_ptr(), _capi.stream_ptr(DEV))
+    assert rc != 0
