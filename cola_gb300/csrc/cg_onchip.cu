@@ -120,9 +120,11 @@ __device__ __forceinline__ void fill_halo(cg::cluster_group& cl, const OnchipCta
 
 // zq[j] = sum_k D[k][rows of group j] * v[rows + off[k]], k ascending (the CSR column order); returns
 // this thread's part of <v, D v>.  One diagonal at a time over all of the thread's groups (G4 128-bit
-// loads in flight per thread, ~64 KB per SM).  Measured on GB300: each diagonal costs about one L2
-// round trip plus its transfer (~1.9k cycles for 64 KB per SM); deeper software pipelining needs more
-// registers than the 128 a thread has here next to the G4 result registers.  `pending`: a
+// loads per thread, ~64 KB per SM), pipelined by halves: once the first half of diagonal k has been
+// used, its registers load the first half of diagonal k + 1 while the second half of k is still
+// arriving.  (Waiting for a whole diagonal before issuing the next cost one L2 round trip plus the
+// transfer per diagonal, ~1.9k cycles for 64 KB per SM; double-buffering whole diagonals needs more
+// registers than the 128 a thread has here next to the G4 result registers.)  `pending`: a
 // cluster_arrive() publishing v's own rows is outstanding; the first diagonal's loads are issued
 // before waiting on it (the matrix does not depend on it), then v's halo is filled.
 template <int CL, int G4>
@@ -140,12 +142,9 @@ __device__ __forceinline__ float diag_product(cg::cluster_group& cl, const Onchi
 #pragma unroll
   for (int j = 0; j < G4; ++j) zq[j] = make_float4(0.f, 0.f, 0.f, 0.f);
   for (int k = 0; k < nk; ++k) {
-    if (k > 0) {
-      const float* Dk = D + k * c.np + c.i0;
-#pragma unroll
-      for (int j = 0; j < G4; ++j) a4[j] = ld4(Dk + 4 * (c.tid + j * kOT));
-    }
     const int o = off[k];
+    const bool more = k + 1 < nk;  // the same for every thread
+    const float* Dn = D + (k + 1) * c.np + c.i0;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       // the shared-memory operands in two halves, so at most half of them are held at once
@@ -159,6 +158,16 @@ __device__ __forceinline__ float diag_product(cg::cluster_group& cl, const Onchi
         zq[j].y = fmaf(a4[j].y, pv[jj].y, zq[j].y);
         zq[j].z = fmaf(a4[j].z, pv[jj].z, zq[j].z);
         zq[j].w = fmaf(a4[j].w, pv[jj].w, zq[j].w);
+      }
+      // this half's registers are free: they take the same half of the next diagonal, so the other
+      // half's loads are still in flight when these are issued (the stream never drains between
+      // diagonals, and no register is added)
+      if (more) {
+#pragma unroll
+        for (int jj = 0; jj < G4 / 2; ++jj) {
+          const int j = h * (G4 / 2) + jj;
+          a4[j] = ld4(Dn + 4 * (c.tid + j * kOT));
+        }
       }
     }
   }
