@@ -70,7 +70,7 @@ __global__ void __launch_bounds__(kCT, 1) k_cluster_pcg(const __grid_constant__ 
   __shared__ double slots[2][8];
   __shared__ double red[32];
   __shared__ double bcast[8];
-  __shared__ float fslots[2][4];
+  __shared__ float fslots[2][2 * CL];  // cluster_sum_f slots: NQ <= 2 sums x CL ranks
   __shared__ float wpart[2 * 32];
   int buf = 0, fbuf = 0;
   auto next_slot = [&]() { double* p = slots[buf]; buf ^= 1; return p; };

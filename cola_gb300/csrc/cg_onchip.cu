@@ -118,6 +118,30 @@ __device__ __forceinline__ void fill_halo(cg::cluster_group& cl, const OnchipCta
   }
 }
 
+// Group `l` (4 rows from local row l) of a vector v whose own rows sit at v[0, R), just computed by
+// this thread: rows within H of either edge are also stored into the neighbouring CTA's halo of the
+// same vector (its rows [R, R + H) for our first H rows, its rows [-H, 0) for our last H rows).  The
+// cluster barrier that follows (arrive.release, then wait.acquire in the reader) makes them visible,
+// so the reader's halo is complete when its wait returns, with no load on its critical path.  The
+// halos at the two ends of the cluster are never written (zero from the system's setup).  A writer
+// only pushes after the cluster barrier that ends the neighbour's last read of that halo.
+template <int CL>
+__device__ __forceinline__ void push_halo(cg::cluster_group& cl, const OnchipCta& c, float* v, int l, float4 x) {
+  if (l < c.H && c.rank > 0) st4(cl.map_shared_rank(v + c.R + l, c.rank - 1), x);
+  if (l >= c.R - c.H && c.rank + 1 < CL) st4(cl.map_shared_rank(v + (l - c.R), c.rank + 1), x);
+}
+
+// push_halo for every edge group of this thread, re-read from its own just-written rows (the same
+// thread wrote them, so no barrier is needed; a pass of its own keeps the phase loops' registers).
+template <int CL, int G4>
+__device__ __forceinline__ void push_halos(cg::cluster_group& cl, const OnchipCta& c, float* v) {
+#pragma unroll 1
+  for (int j = 0; j < G4; ++j) {
+    const int l = 4 * (c.tid + j * kOT);
+    if (l < c.H || l >= c.R - c.H) push_halo<CL>(cl, c, v, l, ld4(v + l));
+  }
+}
+
 // zq[j] = sum_k D[k][rows of group j] * v[rows + off[k]], k ascending (the CSR column order); returns
 // this thread's part of <v, D v>.  One diagonal at a time over all of the thread's groups (G4 128-bit
 // loads per thread, ~64 KB per SM), pipelined by halves: once the first half of diagonal k has been
@@ -125,8 +149,9 @@ __device__ __forceinline__ void fill_halo(cg::cluster_group& cl, const OnchipCta
 // arriving.  (Waiting for a whole diagonal before issuing the next cost one L2 round trip plus the
 // transfer per diagonal, ~1.9k cycles for 64 KB per SM; double-buffering whole diagonals needs more
 // registers than the 128 a thread has here next to the G4 result registers.)  `pending`: a
-// cluster_arrive() publishing v's own rows is outstanding; the first diagonal's loads are issued
-// before waiting on it (the matrix does not depend on it), then v's halo is filled.
+// cluster_arrive() publishing v's own rows and the halos pushed into the neighbours (push_halo) is
+// outstanding; the first diagonal's loads are issued before waiting on it (the matrix does not
+// depend on it).
 template <int CL, int G4>
 __device__ __forceinline__ float diag_product(cg::cluster_group& cl, const OnchipCta& c, float4 (&zq)[G4],
                                               const float* D, const int* off, int nk, float* v, bool pending) {
@@ -134,11 +159,7 @@ __device__ __forceinline__ float diag_product(cg::cluster_group& cl, const Onchi
   const float* D0 = D + c.i0;
 #pragma unroll
   for (int j = 0; j < G4; ++j) a4[j] = ld4(D0 + 4 * (c.tid + j * kOT));
-  if (pending) {
-    cluster_wait();
-    fill_halo<CL>(cl, c, v);
-    __syncthreads();
-  }
+  if (pending) cluster_wait();  // v's own rows and both halos complete
 #pragma unroll
   for (int j = 0; j < G4; ++j) zq[j] = make_float4(0.f, 0.f, 0.f, 0.f);
   for (int k = 0; k < nk; ++k) {
@@ -214,7 +235,7 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
   __shared__ double slots[2][8];
   __shared__ double red[32];
   __shared__ double bcast[8];
-  __shared__ float fslots[2][4];
+  __shared__ float fslots[2][2 * CL];  // cluster_sum_f slots: NQ <= 2 sums x CL ranks
   __shared__ float wpart[2 * 32];
   __shared__ unsigned int s_sys;
   int buf = 0, fbuf = 0;
@@ -267,6 +288,12 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
       ps[l] = 0.f;
       rs[l] = 0.f;
       ds[l] = 0.f;
+      if (l < H) {  // halos (those at the ends of the cluster stay zero)
+        ps[l - H] = 0.f;
+        ps[R + l] = 0.f;
+        rs[l - H] = 0.f;
+        rs[R + l] = 0.f;
+      }
       if (live) {
         const double bv = B[i];
         v1[0] += bv * bv;
@@ -328,8 +355,9 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
     if (status == COLAGB_SYS_RUNNING && rn <= (float)a.tol) status = COLAGB_SYS_CONVERGED;
 #pragma unroll
     for (int j = 0; j < G4; ++j) st4(ps + 4 * (tid + j * kOT), zq[j]);
+    push_halos<CL, G4>(cl, ctx, ps);
     __syncthreads();
-    cluster_arrive();  // p published; waited for inside the first step
+    cluster_arrive();  // p and its halos published; waited for inside the first step
     bool arrived = true;
 
     int it = 0, nrep = 0, it_rep = 0;
@@ -383,6 +411,7 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
       }
       float qb[2] = {rrf, rzf};
       if (prec == COLAGB_PREC_FSAI) {
+        push_halos<CL, G4>(cl, ctx, rs);  // M r reads r's halo
         __syncthreads();
         cluster_arrive();
         qb[1] = apply_z<CL, G4>(cl, ctx, zq, prec, a, M, Dv, rs, true);
@@ -455,8 +484,9 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
                                                       dd[jj].z + alpha * po[jj].z, dd[jj].w + alpha * po[jj].w));
         }
       }
+      push_halos<CL, G4>(cl, ctx, ps);
       __syncthreads();
-      cluster_arrive();  // p published; waited for at the start of the next step
+      cluster_arrive();  // p and its halos published; waited for at the start of the next step
       arrived = true;
     }
     // every break leaves the loop with no arrive outstanding; a system that needs no step (zero or

@@ -39,11 +39,14 @@ __device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster
 __device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory"); }
 
 // FP32 cluster-wide sums for the per-iteration inner products, built for latency: a butterfly in
-// each warp, one block barrier, one cluster barrier, then every warp reads the CL per-CTA partials
-// through distributed shared memory and combines them with the same butterfly.  Every thread of
-// every CTA ends with bit-identical sums (fixed combination order; a + b == b + a in IEEE
-// arithmetic).  `wpart` holds NQ x 32 floats; `slot` NQ floats and must alternate between two
-// buffers across consecutive calls (the same rule as cluster_sum).
+// each warp, one block barrier, then warp 0 of every CTA stores the CTA's totals straight into every
+// peer's `slot` (distributed shared memory, entry [q][rank]), one cluster barrier publishes them,
+// and every warp reads the CL partials from its own shared memory and combines them with the same
+// butterfly.  Every thread of every CTA ends with bit-identical sums (the same values in the same
+// lanes, fixed combination order; a + b == b + a in IEEE arithmetic).  `wpart` holds NQ x 32
+// floats; `slot` NQ x CL floats and must alternate between two buffers across consecutive calls: a
+// CTA writes a peer's buffer again only two calls later, after the intervening cluster barrier that
+// the peer reaches once it has read that buffer.
 template <int NQ, int CL>
 __device__ __forceinline__ void cluster_sum_f(cooperative_groups::cluster_group& cl, float (&v)[NQ], float* wpart,
                                               float* slot) {
@@ -57,15 +60,16 @@ __device__ __forceinline__ void cluster_sum_f(cooperative_groups::cluster_group&
   }
   __syncthreads();
   if (warp == 0) {
+    const int rank = (int)cl.block_rank();
 #pragma unroll
     for (int q = 0; q < NQ; ++q) {
-      const float x = warp_sum(lane < nw ? wpart[q * 32 + lane] : 0.f);
-      if (lane == 0) slot[q] = x;
+      const float x = warp_sum(lane < nw ? wpart[q * 32 + lane] : 0.f);  // every lane holds the total
+      if (lane < CL) *cl.map_shared_rank(slot + q * CL + rank, lane) = x;
     }
   }
   cl.sync();
 #pragma unroll
-  for (int q = 0; q < NQ; ++q) v[q] = warp_sum(lane < CL ? *cl.map_shared_rank(slot + q, lane) : 0.f);
+  for (int q = 0; q < NQ; ++q) v[q] = warp_sum(lane < CL ? slot[q * CL + lane] : 0.f);
 }
 
 }  // namespace colagb
