@@ -32,6 +32,7 @@ namespace cg = cooperative_groups;
 namespace colagb {
 
 constexpr int kOT = 512;         // threads per CTA
+constexpr int kRowBatch = 8;     // rows per thread whose loads are issued together in the FP64 passes
 constexpr int kMaxDiagA = 9;     // diagonals of A
 constexpr int kMaxDiagG = 5;     // diagonals of the FSAI factor G
 constexpr int kMaxDiagM = 17;    // diagonals of M = G^T G
@@ -71,13 +72,45 @@ struct OnchipArgs {
   int max_sweeps, max_inner, prec_kind, fallback, mode;
 };
 
-// One CSR row as a dense value on diagonal `o` (entries with the same column are summed).
+// One CSR row as dense values on diagonal `o` (entries with the same column are summed).
 __device__ __forceinline__ float csr_diag_value(const int32_t* indptr, const int32_t* indices, const float* vals,
                                                 int64_t i, int o) {
   float v = 0.f;
   for (int32_t e = indptr[i]; e < indptr[i + 1]; ++e)
     if ((int64_t)indices[e] - i == o) v += vals[e];
   return v;
+}
+
+// Row i of a CSR matrix into diagonal storage: out[k * stride] = the sum, in CSR order, of the
+// row's entries in column i + off[k], for k < nk (0 for a row past n).  A row of at most eight
+// entries is loaded once, all loads in flight together, and matched against every diagonal from
+// registers; a longer row is scanned once per diagonal.
+__device__ __forceinline__ void csr_row_to_diagonals(const int32_t* indptr, const int32_t* indices, const float* vals,
+                                                     int64_t i, bool live, const int* off, int nk, float* out,
+                                                     int64_t stride) {
+  const int32_t b = live ? indptr[i] : 0, e = live ? indptr[i + 1] : 0;
+  if (e - b <= 8) {
+    int32_t col[8];
+    float v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const bool ok = b + u < e;
+      col[u] = ok ? indices[b + u] : 0;
+      v[u] = ok ? vals[b + u] : 0.f;
+    }
+#pragma unroll 1
+    for (int k = 0; k < nk; ++k) {
+      const int64_t c = i + off[k];
+      float acc = 0.f;
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (b + u < e && col[u] == c) acc += v[u];
+      out[k * stride] = acc;
+    }
+  } else {
+#pragma unroll 1
+    for (int k = 0; k < nk; ++k) out[k * stride] = csr_diag_value(indptr, indices, vals, i, off[k]);
+  }
 }
 
 // Per-CTA geometry of the on-chip schedule.
@@ -274,17 +307,9 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
     for (int l = tid; l < R; l += kOT) {
       const int64_t i = i0 + l;
       const bool live = i < n;
-      for (int k = 0; k < a.nd; ++k) {
-        const float v = live ? csr_diag_value(a.indptr, a.indices, vals, i, a.off[k]) : 0.f;
-        A[k * np + i] = v;
-        if (k == a.center) Dv[i] = v != 0.f ? 1.f / v : 1.f;
-      }
-      if (a.center < 0) Dv[i] = 1.f;
-      if (Gd) {
-        const float* gv = a.g_vals + s * a.g_nnz;
-        for (int k = 0; k < a.ng; ++k)
-          Gd[k * np + i] = live ? csr_diag_value(a.g_indptr, a.g_indices, gv, i, a.goff[k]) : 0.f;
-      }
+      csr_row_to_diagonals(a.indptr, a.indices, vals, i, live, a.off, a.nd, A + i, np);
+      Dv[i] = a.center >= 0 && A[a.center * np + i] != 0.f ? 1.f / A[a.center * np + i] : 1.f;
+      if (Gd) csr_row_to_diagonals(a.g_indptr, a.g_indices, a.g_vals + s * a.g_nnz, i, live, a.goff, a.ng, Gd + i, np);
       ps[l] = 0.f;
       rs[l] = 0.f;
       ds[l] = 0.f;
@@ -303,16 +328,26 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
     cluster_sum<1, CL>(cl, v1, next_slot(), red, bcast);  // also publishes G's diagonals and x = 0
     if (M) {  // M = G^T G on this CTA's rows, from G's diagonals (rows k >= i may belong to the next CTA)
 #pragma unroll 1
-      for (int l = tid; l < R; l += kOT) {
-        const int64_t i = i0 + l;
+      for (int l0 = tid; l0 < R; l0 += kRowBatch * kOT) {  // eight rows' loads in flight per product
+#pragma unroll 1
         for (int m = 0; m < a.nm; ++m) {
-          float v = 0.f;
-          if (i < n)
-            for (int q = a.pstart[m]; q < a.pstart[m + 1]; ++q) {
-              const int64_t k = i - a.goff[a.pa[q]];
-              if (k < n) v += Gd[a.pa[q] * np + k] * Gd[a.pb[q] * np + k];
+          float v[kRowBatch];
+#pragma unroll
+          for (int u = 0; u < kRowBatch; ++u) v[u] = 0.f;
+#pragma unroll 1
+          for (int q = a.pstart[m]; q < a.pstart[m + 1]; ++q) {
+            const float* ga = Gd + a.pa[q] * np;
+            const float* gb = Gd + a.pb[q] * np;
+            const int go = a.goff[a.pa[q]];
+#pragma unroll
+            for (int u = 0; u < kRowBatch; ++u) {
+              const int64_t i = i0 + l0 + u * kOT;
+              const int64_t k = i - go;  // go <= 0: k >= i
+              if (i < n && k < n) v[u] += ga[k] * gb[k];
             }
-          M[m * np + i] = v;
+          }
+#pragma unroll
+          for (int u = 0; u < kRowBatch; ++u) M[m * np + i0 + l0 + u * kOT] = v[u];
         }
       }
     }
@@ -324,20 +359,38 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
 
     // r = b/|b| - A x in FP64 (x gathered from global memory), |r|^2
     float4 zq[G4];  // per-row register values: A p in phase A, z in phases B/C
+    // Eight rows per thread per pass, diagonal by diagonal: the eight rows' loads of one diagonal are
+    // in flight together (a row at a time paid one L2 round trip per term).  Terms are added in
+    // diagonal order, as in the CSR row.
     auto residual = [&](double& rr) {
       rr = 0.0;
 #pragma unroll 1
-      for (int l = tid; l < R; l += kOT) {
-        const int64_t i = i0 + l;
-        if (i < n) {
-          double ax = 0.0;
-          for (int k = 0; k < a.nd; ++k) {
-            const int64_t c = i + a.off[k];
-            if (c >= 0 && c < n) ax += (double)A[k * np + i] * X[c];
+      for (int l0 = tid; l0 < R; l0 += kRowBatch * kOT) {  // R is a multiple of kRowBatch * kOT
+        double ax[kRowBatch];
+#pragma unroll
+        for (int u = 0; u < kRowBatch; ++u) ax[u] = 0.0;
+#pragma unroll 1
+        for (int k = 0; k < a.nd; ++k) {
+          const float* Ak = A + k * np + i0;
+          const int o = a.off[k];
+#pragma unroll
+          for (int u = 0; u < kRowBatch; ++u) {
+            const int l = l0 + u * kOT;
+            const int64_t c = i0 + l + o;
+            const float av = Ak[l];  // 0 where row i0 + l has no entry on this diagonal (and past n)
+            const double xv = c >= 0 && c < n ? X[c] : 0.0;
+            ax[u] += (double)av * xv;
           }
-          const double rv = B[i] * binv - ax;
-          rs[l] = (float)rv;
-          rr += rv * rv;
+        }
+#pragma unroll
+        for (int u = 0; u < kRowBatch; ++u) {
+          const int l = l0 + u * kOT;
+          const int64_t i = i0 + l;
+          if (i < n) {
+            const double rv = B[i] * binv - ax[u];
+            rs[l] = (float)rv;
+            rr += rv * rv;
+          }
         }
       }
     };
@@ -429,13 +482,23 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
       }
       if (rn <= delta * rmax || rn <= (float)a.tol || it >= a.max_inner ||
           (a.fallback && prec == COLAGB_PREC_FSAI && it - it_rep >= kJudgeSteps)) {
-        // FP64 replacement: x += d + alpha p, d = 0 ; r = b/|b| - A x
+        // FP64 replacement: x += d + alpha p, d = 0 ; r = b/|b| - A x  (eight rows' x loads in flight)
 #pragma unroll 1
-        for (int l = tid; l < R; l += kOT) {
-          const int64_t i = i0 + l;
-          const float dn = ds[l] + alpha * ps[l];
-          if (i < n) X[i] += (double)dn;
-          ds[l] = 0.f;
+        for (int l0 = tid; l0 < R; l0 += kRowBatch * kOT) {
+          double xv[kRowBatch];
+#pragma unroll
+          for (int u = 0; u < kRowBatch; ++u) {
+            const int64_t i = i0 + l0 + u * kOT;
+            xv[u] = i < n ? X[i] : 0.0;
+          }
+#pragma unroll
+          for (int u = 0; u < kRowBatch; ++u) {
+            const int l = l0 + u * kOT;
+            const int64_t i = i0 + l;
+            const float dn = ds[l] + alpha * ps[l];
+            if (i < n) X[i] = xv[u] + (double)dn;
+            ds[l] = 0.f;
+          }
         }
         dpend = false;
         it_rep = it;
@@ -494,9 +557,19 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
     if (arrived) cluster_wait();
     // finish: x += d, scale by |b|
 #pragma unroll 1
-    for (int l = tid; l < R; l += kOT) {
-      const int64_t i = i0 + l;
-      if (i < n) X[i] = (X[i] + (double)ds[l]) * (bnorm > 0.0 ? bnorm : 1.0);
+    for (int l0 = tid; l0 < R; l0 += kRowBatch * kOT) {
+      double xv[kRowBatch];
+#pragma unroll
+      for (int u = 0; u < kRowBatch; ++u) {
+        const int64_t i = i0 + l0 + u * kOT;
+        xv[u] = i < n ? X[i] : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < kRowBatch; ++u) {
+        const int l = l0 + u * kOT;
+        const int64_t i = i0 + l;
+        if (i < n) X[i] = (xv[u] + (double)ds[l]) * (bnorm > 0.0 ? bnorm : 1.0);
+      }
     }
     if (rank == 0 && tid == 0) {
       int st = status == COLAGB_SYS_RUNNING ? COLAGB_SYS_MAX_ITERS : status;
