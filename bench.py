@@ -147,8 +147,8 @@ def bytes_per_system_iter(n, nnz, method, schedule="cluster8", nd=5, nm=7):
     """Algorithmic memory bytes of one FP32 PCG step of one system.
 
     On-chip schedule: the Krylov vectors stay in the cluster's shared memory, so a step moves only
-    the matrix diagonals (nd n 4 bytes; Jacobi adds 1/diag, n 4; FSAI adds the nm diagonals of
-    M = G^T G).  Other schedules: the CSR values (the batch shares one pattern, read from L2) + 6
+    the matrix diagonals (nd n 4 bytes; Jacobi adds 1/diag, n 4; FSAI adds the nm bfloat16
+    diagonals of M = G^T G, nm n 2).  Other schedules: the CSR values (the batch shares one pattern, read from L2) + 6
     vector streams (p read, x r/w, r r/w, p write) + the preconditioner (Jacobi: the diagonal; FSAI:
     G and G^T values and the intermediate t written and read)."""
     if schedule == "onchip":
@@ -156,7 +156,7 @@ def bytes_per_system_iter(n, nnz, method, schedule="cluster8", nd=5, nm=7):
         if method == "jacobi":
             b += n * 4
         elif method in ("learned", "fsai"):
-            b += nm * n * 4
+            b += nm * n * 2  # M = G^T G in bfloat16
         return b
     b = nnz * 4 + 6 * n * 4
     if method == "jacobi":

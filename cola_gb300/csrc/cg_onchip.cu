@@ -18,6 +18,7 @@
 //     system's CSR values into its own diagonal slot, solves it and moves on.
 // Results are per system and independent of the scheduling order.
 #include <cooperative_groups.h>
+#include <cuda_bf16.h>
 
 #include <algorithm>
 #include <string>
@@ -38,6 +39,13 @@ constexpr int kMaxDiagG = 5;     // diagonals of the FSAI factor G
 constexpr int kMaxDiagM = 17;    // diagonals of M = G^T G
 constexpr int kMaxPairs = 32;    // (G diagonal, G diagonal) products that make up M
 constexpr size_t kOnchipSmemMax = 227 * 1024 - 1024;
+// The FSAI operator M = G^T G is stored in bfloat16 (round to nearest: each entry off by at most
+// 2^-8 of itself) with every main-diagonal entry raised by kMBoost = 2^-7 times its row's absolute
+// sum.  The change to M is then diagonally dominant with a non-negative diagonal, so the stored M'
+// satisfies M' >= M > 0 (Gershgorin): still SPD and symmetric, a preconditioner within ~1 % of M,
+// at half the bytes per step.  A stays FP32 (CG's operator), and the FP64 true residual still judges
+// convergence.
+constexpr float kMBoost = 1.f / 128.f;
 
 struct OnchipArgs {
   int64_t n, S, np;  // rows, systems, rows padded to the cluster (CL * R)
@@ -59,7 +67,7 @@ struct OnchipArgs {
   int64_t g_nnz;
   float* adia;  // [slot][nd][np]
   float* gdia;  // [slot][ng][np]
-  float* mdia;  // [slot][nm][np]
+  float* mdia;  // [slot][nm][np] floats of space, holding bfloat16 diagonals [slot][nm][np]
   float* dinv;  // [slot][np]: 1 / A(i, i) (1 where the diagonal is absent or zero)
   unsigned int* next;
   const double* B;
@@ -185,20 +193,41 @@ __device__ __forceinline__ void push_halos(cg::cluster_group& cl, const OnchipCt
 // cluster_arrive() publishing v's own rows and the halos pushed into the neighbours (push_halo) is
 // outstanding; the first diagonal's loads are issued before waiting on it (the matrix does not
 // depend on it).
-template <int CL, int G4>
+// Four consecutive diagonal values as they sit in registers between load and use: FP32 (A) or
+// bfloat16 (M, 8 bytes per 4 rows, widened to FP32 when used).
+template <typename T>
+struct Diag4;
+template <>
+struct Diag4<float> {
+  using Reg = float4;
+  static __device__ __forceinline__ Reg load(const float* p) { return ld4(p); }
+  static __device__ __forceinline__ float4 wide(Reg r) { return r; }
+};
+template <>
+struct Diag4<__nv_bfloat16> {
+  using Reg = uint2;
+  static __device__ __forceinline__ Reg load(const __nv_bfloat16* p) { return *reinterpret_cast<const uint2*>(p); }
+  static __device__ __forceinline__ float4 wide(Reg r) {  // bfloat16 = the high half of an FP32 word
+    return make_float4(__uint_as_float(r.x << 16), __uint_as_float(r.x & 0xffff0000u), __uint_as_float(r.y << 16),
+                       __uint_as_float(r.y & 0xffff0000u));
+  }
+};
+
+template <int CL, int G4, typename T>
 __device__ __forceinline__ float diag_product(cg::cluster_group& cl, const OnchipCta& c, float4 (&zq)[G4],
-                                              const float* D, const int* off, int nk, float* v, bool pending) {
-  float4 a4[G4];
-  const float* D0 = D + c.i0;
+                                              const T* D, const int* off, int nk, float* v, bool pending) {
+  using DL = Diag4<T>;
+  typename DL::Reg a4[G4];
+  const T* D0 = D + c.i0;
 #pragma unroll
-  for (int j = 0; j < G4; ++j) a4[j] = ld4(D0 + 4 * (c.tid + j * kOT));
+  for (int j = 0; j < G4; ++j) a4[j] = DL::load(D0 + 4 * (c.tid + j * kOT));
   if (pending) cluster_wait();  // v's own rows and both halos complete
 #pragma unroll
   for (int j = 0; j < G4; ++j) zq[j] = make_float4(0.f, 0.f, 0.f, 0.f);
   for (int k = 0; k < nk; ++k) {
     const int o = off[k];
     const bool more = k + 1 < nk;  // the same for every thread
-    const float* Dn = D + (k + 1) * c.np + c.i0;
+    const T* Dn = D + (k + 1) * c.np + c.i0;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       // the shared-memory operands in two halves, so at most half of them are held at once
@@ -208,10 +237,11 @@ __device__ __forceinline__ float diag_product(cg::cluster_group& cl, const Onchi
 #pragma unroll
       for (int jj = 0; jj < G4 / 2; ++jj) {
         const int j = h * (G4 / 2) + jj;
-        zq[j].x = fmaf(a4[j].x, pv[jj].x, zq[j].x);
-        zq[j].y = fmaf(a4[j].y, pv[jj].y, zq[j].y);
-        zq[j].z = fmaf(a4[j].z, pv[jj].z, zq[j].z);
-        zq[j].w = fmaf(a4[j].w, pv[jj].w, zq[j].w);
+        const float4 av = DL::wide(a4[j]);
+        zq[j].x = fmaf(av.x, pv[jj].x, zq[j].x);
+        zq[j].y = fmaf(av.y, pv[jj].y, zq[j].y);
+        zq[j].z = fmaf(av.z, pv[jj].z, zq[j].z);
+        zq[j].w = fmaf(av.w, pv[jj].w, zq[j].w);
       }
       // this half's registers are free: they take the same half of the next diagonal, so the other
       // half's loads are still in flight when these are issued (the stream never drains between
@@ -220,7 +250,7 @@ __device__ __forceinline__ float diag_product(cg::cluster_group& cl, const Onchi
 #pragma unroll
         for (int jj = 0; jj < G4 / 2; ++jj) {
           const int j = h * (G4 / 2) + jj;
-          a4[j] = ld4(Dn + 4 * (c.tid + j * kOT));
+          a4[j] = DL::load(Dn + 4 * (c.tid + j * kOT));
         }
       }
     }
@@ -237,9 +267,9 @@ __device__ __forceinline__ float diag_product(cg::cluster_group& cl, const Onchi
 // x.  FSAI: `published` says a cluster_arrive() publishing r's own rows is outstanding.
 template <int CL, int G4>
 __device__ __forceinline__ float apply_z(cg::cluster_group& cl, const OnchipCta& c, float4 (&zq)[G4], int prec,
-                                         const OnchipArgs& a, const float* M, const float* Dv, float* rs,
+                                         const OnchipArgs& a, const __nv_bfloat16* M, const float* Dv, float* rs,
                                          bool published) {
-  if (prec == COLAGB_PREC_FSAI) return diag_product<CL, G4>(cl, c, zq, M, a.moff, a.nm, rs, published);
+  if (prec == COLAGB_PREC_FSAI) return diag_product<CL, G4, __nv_bfloat16>(cl, c, zq, M, a.moff, a.nm, rs, published);
   if (prec == COLAGB_PREC_JACOBI) {
 #pragma unroll
     for (int j = 0; j < G4; ++j) {
@@ -284,7 +314,7 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
   const int64_t i0 = (int64_t)rank * R;  // first row of this CTA (rows >= n are zero padding)
   float* A = a.adia + slot * a.nd * np;
   float* Gd = a.gdia ? a.gdia + slot * a.ng * np : nullptr;
-  float* M = a.mdia ? a.mdia + slot * a.nm * np : nullptr;
+  __nv_bfloat16* M = a.mdia ? reinterpret_cast<__nv_bfloat16*>(a.mdia + slot * a.nm * np) : nullptr;
   float* Dv = a.dinv + slot * np;
   const OnchipCta ctx{rank, R, H, tid, np, i0};
   constexpr int G4 = G / 4;  // 4-row groups per thread
@@ -329,6 +359,10 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
     if (M) {  // M = G^T G on this CTA's rows, from G's diagonals (rows k >= i may belong to the next CTA)
 #pragma unroll 1
       for (int l0 = tid; l0 < R; l0 += kRowBatch * kOT) {  // eight rows' loads in flight per product
+        float asum[kRowBatch], ctr[kRowBatch];  // row absolute sums, main-diagonal values
+#pragma unroll
+        for (int u = 0; u < kRowBatch; ++u) asum[u] = ctr[u] = 0.f;
+        int mc = 0;
 #pragma unroll 1
         for (int m = 0; m < a.nm; ++m) {
           float v[kRowBatch];
@@ -347,8 +381,19 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
             }
           }
 #pragma unroll
-          for (int u = 0; u < kRowBatch; ++u) M[m * np + i0 + l0 + u * kOT] = v[u];
+          for (int u = 0; u < kRowBatch; ++u) asum[u] += fabsf(v[u]);
+          if (a.moff[m] == 0) {
+            mc = m;
+#pragma unroll
+            for (int u = 0; u < kRowBatch; ++u) ctr[u] = v[u];
+          } else {
+#pragma unroll
+            for (int u = 0; u < kRowBatch; ++u) M[m * np + i0 + l0 + u * kOT] = __float2bfloat16_rn(v[u]);
+          }
         }
+#pragma unroll
+        for (int u = 0; u < kRowBatch; ++u)
+          M[mc * np + i0 + l0 + u * kOT] = __float2bfloat16_rn(ctr[u] + kMBoost * asum[u]);
       }
     }
     const double bnorm = sqrt(v1[0]);
@@ -417,7 +462,7 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
     const float delta = (float)a.inner_tol;
     while (status == COLAGB_SYS_RUNNING) {
       // A: A p into zq ; <p, A p>
-      const float paf = diag_product<CL, G4>(cl, ctx, zq, A, a.off, a.nd, ps, true);
+      const float paf = diag_product<CL, G4, float>(cl, ctx, zq, A, a.off, a.nd, ps, true);
       arrived = false;
       float qa[1] = {paf};
       cluster_sum_f<1, CL>(cl, qa, wpart, next_fslot());
