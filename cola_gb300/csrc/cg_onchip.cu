@@ -183,8 +183,8 @@ __device__ __forceinline__ void push_halos(cg::cluster_group& cl, const OnchipCt
   }
 }
 
-// zq[j] = sum_k D[k][rows of group j] * v[rows + off[k]], k ascending (the CSR column order); returns
-// this thread's part of <v, D v>.  One diagonal at a time over all of the thread's groups (G4 128-bit
+// zq[j] = sum_k D[k][rows of group j] * v[rows + off[k]], k ascending (the host puts the main
+// diagonal last, the others in column order); returns this thread's part of <v, D v>.  One diagonal at a time over all of the thread's groups (G4 128-bit
 // loads per thread, ~64 KB per SM), pipelined by halves: once the first half of diagonal k has been
 // used, its registers load the first half of diagonal k + 1 while the second half of k is still
 // arriving.  (Waiting for a whole diagonal before issuing the next cost one L2 round trip plus the
@@ -224,6 +224,7 @@ __device__ __forceinline__ float diag_product(cg::cluster_group& cl, const Onchi
   if (pending) cluster_wait();  // v's own rows and both halos complete
 #pragma unroll
   for (int j = 0; j < G4; ++j) zq[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+  float dotv = 0.f;
   for (int k = 0; k < nk; ++k) {
     const int o = off[k];
     const bool more = k + 1 < nk;  // the same for every thread
@@ -243,6 +244,10 @@ __device__ __forceinline__ float diag_product(cg::cluster_group& cl, const Onchi
         zq[j].z = fmaf(av.z, pv[jj].z, zq[j].z);
         zq[j].w = fmaf(av.w, pv[jj].w, zq[j].w);
       }
+      if (!more && o == 0) {  // the last diagonal is the main one: pv holds v's own rows
+#pragma unroll
+        for (int jj = 0; jj < G4 / 2; ++jj) dotv += dot4(pv[jj], zq[h * (G4 / 2) + jj]);
+      }
       // this half's registers are free: they take the same half of the next diagonal, so the other
       // half's loads are still in flight when these are issued (the stream never drains between
       // diagonals, and no register is added)
@@ -255,9 +260,10 @@ __device__ __forceinline__ float diag_product(cg::cluster_group& cl, const Onchi
       }
     }
   }
-  float dotv = 0.f;
+  if (off[nk - 1] != 0) {  // no main diagonal: read v's own rows again
 #pragma unroll
-  for (int j = 0; j < G4; ++j) dotv += dot4(ld4(v + 4 * (c.tid + j * kOT)), zq[j]);
+    for (int j = 0; j < G4; ++j) dotv += dot4(ld4(v + 4 * (c.tid + j * kOT)), zq[j]);
+  }
   return dotv;
 }
 
@@ -796,6 +802,9 @@ int onchip_pcg_solve(const colagb_batched_csr* Acsr, const double* B, double* X,
   std::vector<int> off, goff;
   COLAGB_TRY(diag_offsets(Acsr->indptr, Acsr->indices, n, bits, dout, off, st));
   if (off.empty() || (int)off.size() > kMaxDiagA) return COLAGB_OK;
+  // the main diagonal last: its operand is then the thread's own rows, still in registers when the
+  // product is complete, for <v, D v> (diag_product)
+  std::stable_partition(off.begin(), off.end(), [](int o) { return o != 0; });
   OnchipArgs a = {};
   a.nd = (int)off.size();
   a.center = -1;
@@ -816,6 +825,7 @@ int onchip_pcg_solve(const colagb_batched_csr* Acsr, const double* B, double* X,
     std::sort(moff.begin(), moff.end());
     moff.erase(std::unique(moff.begin(), moff.end()), moff.end());
     if ((int)moff.size() > kMaxDiagM) return COLAGB_OK;
+    std::stable_partition(moff.begin(), moff.end(), [](int o) { return o != 0; });  // main diagonal last
     a.ng = (int)goff.size();
     a.nm = (int)moff.size();
     for (int k = 0; k < a.ng; ++k) a.goff[k] = goff[k];
