@@ -193,3 +193,35 @@ def test_workload_generators_small():
         A = torch.sparse_csr_tensor(fam.indptr.long(), fam.indices.long(), fam.values[s].double(), (n, n)).to_dense()
         assert torch.allclose(A, A.T)
         assert torch.linalg.eigvalsh(A)[0] > 0
+
+
+def _bf16_round(x: np.ndarray) -> np.ndarray:
+    """float32 -> bfloat16 (round to nearest, ties to even) -> float32, as __float2bfloat16_rn."""
+    u = np.ascontiguousarray(x, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32)
+
+
+def test_bfloat16_preconditioner_boost_keeps_it_spd():
+    """The on-chip schedule stores M = G^T G in bfloat16 with each main-diagonal entry raised by
+    2^-7 times its row's absolute sum (kMBoost, cg_onchip.cu).  For any symmetric M that makes the
+    stored M' - M diagonally dominant with a non-negative diagonal, so M' >= M: checked here on
+    FSAI-shaped banded matrices and on dense symmetric ones with large off-diagonals, including M
+    that is barely positive definite."""
+    rng = np.random.default_rng(7)
+    m, n = 8, 64
+    cases = []
+    for _ in range(20):  # G lower with offsets {0, -1, -m}, M = G^T G (7 diagonals)
+        G = np.diag(rng.uniform(0.5, 2.0, n))
+        G += np.diag(-rng.uniform(0.0, 1.0, n - 1), -1) + np.diag(-rng.uniform(0.0, 1.0, n - m), -m)
+        cases.append((G.T @ G).astype(np.float32))
+    for _ in range(20):  # dense symmetric, shifted to be barely positive definite
+        B = rng.standard_normal((32, 32)).astype(np.float32)
+        S = B + B.T
+        cases.append((S - (np.linalg.eigvalsh(S.astype(np.float64))[0] - 1e-3) * np.eye(32)).astype(np.float32))
+    for M in cases:
+        Mp = _bf16_round(M)
+        np.fill_diagonal(Mp, _bf16_round(np.diag(M) + np.float32(1 / 128) * np.abs(M).sum(1, dtype=np.float32)))
+        assert np.array_equal(Mp, Mp.T)
+        assert np.linalg.eigvalsh((Mp - M).astype(np.float64))[0] >= -1e-12 * np.abs(M).max()
+        assert np.linalg.eigvalsh(Mp.astype(np.float64))[0] > 0
