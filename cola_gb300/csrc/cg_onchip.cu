@@ -10,9 +10,11 @@
 //     column indices, no row pointers;
 //   * CTA `rank` of the cluster owns rows [rank * R, rank * R + R); its p and r (plus a halo of H
 //     rows on each side) and d live in its shared memory for the whole solve, so the only memory
-//     traffic per iteration is the matrix (and the FSAI operator M = G^T G, also diagonal);
-//   * halos are copied from the neighbouring CTAs' shared memory (distributed shared memory) after
-//     the cluster barrier that follows their update;
+//     traffic per iteration is the matrix (and the FSAI operator M = G^T G, also diagonal, in
+//     bfloat16);
+//   * each CTA stores its edge rows straight into the neighbouring CTAs' halos (distributed shared
+//     memory) before the cluster barrier that publishes them, and its reduction partials into every
+//     peer, so nothing is loaded from a peer on the critical path;
 //   * per-row values that stay with the same thread between phases (A p, then z) stay in registers;
 //   * clusters are persistent: each takes the next system from an atomic counter, converts that
 //     system's CSR values into its own diagonal slot, solves it and moves on.
@@ -471,7 +473,14 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
       const float paf = diag_product<CL, G4, float>(cl, ctx, zq, A, a.off, a.nd, ps, true);
       arrived = false;
       float qa[1] = {paf};
-      cluster_sum_f<1, CL>(cl, qa, wpart, next_fslot());
+      float4 rown[G4];  // r's own rows, loaded while the reduction's barrier completes
+      {
+        float* sl = next_fslot();
+        cluster_sum_f_begin<1, CL>(cl, qa, wpart, sl);
+#pragma unroll
+        for (int j = 0; j < G4; ++j) rown[j] = ld4(rs + 4 * (tid + j * kOT));
+        cluster_sum_f_end<1, CL>(qa, sl);
+      }
       const float pap = qa[0];
       if (!(pap > 0.f)) {  // not SPD in FP32 (or NaN)
         status = (pap == pap) ? COLAGB_SYS_BREAKDOWN : COLAGB_SYS_NAN;
@@ -490,7 +499,7 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
 #pragma unroll
         for (int jj = 0; jj < H4; ++jj) {
           const int j = h * H4 + jj;
-          rv[jj] = ld4(rs + 4 * (tid + j * kOT));
+          rv[jj] = rown[j];
           dv[jj] = prec == COLAGB_PREC_JACOBI ? ld4(Dv + i0 + 4 * (tid + j * kOT)) : make_float4(1.f, 1.f, 1.f, 1.f);
         }
 #pragma unroll

@@ -72,4 +72,38 @@ __device__ __forceinline__ void cluster_sum_f(cooperative_groups::cluster_group&
   for (int q = 0; q < NQ; ++q) v[q] = warp_sum(lane < CL ? slot[q * CL + lane] : 0.f);
 }
 
+// cluster_sum_f in two halves, so that work which does not need the sums runs while the cluster
+// barrier completes: _begin publishes this CTA's partials into every peer and arrives on the
+// barrier (release), _end waits on it (acquire) and combines.  Same results as cluster_sum_f.
+template <int NQ, int CL>
+__device__ __forceinline__ void cluster_sum_f_begin(cooperative_groups::cluster_group& cl, float (&v)[NQ],
+                                                    float* wpart, float* slot) {
+  static_assert(CL <= 32, "one warp combines the CTA partials");
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nw = blockDim.x >> 5;
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    const float x = warp_sum(v[q]);
+    if (lane == 0) wpart[q * 32 + warp] = x;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    const int rank = (int)cl.block_rank();
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      const float x = warp_sum(lane < nw ? wpart[q * 32 + lane] : 0.f);
+      if (lane < CL) *cl.map_shared_rank(slot + q * CL + rank, lane) = x;
+    }
+  }
+  cluster_arrive();
+}
+
+template <int NQ, int CL>
+__device__ __forceinline__ void cluster_sum_f_end(float (&v)[NQ], const float* slot) {
+  const int lane = threadIdx.x & 31;
+  cluster_wait();
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) v[q] = warp_sum(lane < CL ? slot[q * CL + lane] : 0.f);
+}
+
 }  // namespace colagb
