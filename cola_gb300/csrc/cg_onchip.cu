@@ -136,52 +136,64 @@ __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast
 __device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
 __device__ __forceinline__ float dot4(float4 a, float4 b) { return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w; }
 
-// v[l + o .. l + o + 3] for a 4-aligned l: one aligned 128-bit load when o is a multiple of 4, else
-// two aligned loads and a register shuffle (o & 3 is the same for every thread).  Loads of the same
-// aligned block by neighbouring offsets (-1, 0, +1) are merged by the compiler.
-__device__ __forceinline__ float4 ld4_off(const float* v, int l, int o) {
-  const int rem = o & 3;
-  const float* b = v + l + (o - rem);
-  const float4 x = ld4(b);
-  if (rem == 0) return x;
-  const float4 y = ld4(b + 4);
-  if (rem == 1) return make_float4(x.y, x.z, x.w, y.x);
-  if (rem == 2) return make_float4(x.z, x.w, y.x, y.y);
-  return make_float4(x.w, y.x, y.y, y.z);
-}
+// Strip layout of the on-chip vectors and diagonals.  A CTA's R own rows are four strips of
+// S = R / 4 rows; float4 number q (0 <= q < S) holds rows q, q + S, q + 2S, q + 3S, so a shift of
+// the row index by any offset o is a shift of q by o: every operand of a diagonal product is one
+// aligned 128-bit load.  Vectors with a halo also hold q in [-H, 0) and [S, S + H): there component
+// c is row q + c S, i.e. the adjacent strip of this CTA -- except component 0 of the left halo and
+// component 3 of the right one, which are the neighbouring CTAs' edge rows (zero at the ends of the
+// cluster).  Local row l sits at float index sidx(l).
+__device__ __forceinline__ int sidx(int l, int S) { return 4 * (l % S) + l / S; }
 
-// Halo rows of v (own rows at v[0, R), H a multiple of 4) from the neighbouring CTAs' shared memory.
+// The halo of v (strip layout): the components from this CTA's adjacent strips, and the neighbouring
+// CTAs' edge rows read from their shared memory (after a cluster barrier that published them).
 template <int CL>
 __device__ __forceinline__ void fill_halo(cg::cluster_group& cl, const OnchipCta& c, float* v) {
-  for (int h = 4 * c.tid; h < c.H; h += 4 * kOT) {
-    const float4 lv = c.rank > 0 ? ld4(cl.map_shared_rank(v + (c.R - c.H + h), c.rank - 1)) : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 rv = c.rank + 1 < CL ? ld4(cl.map_shared_rank(v + h, c.rank + 1)) : make_float4(0.f, 0.f, 0.f, 0.f);
-    st4(v + h - c.H, lv);
-    st4(v + c.R + h, rv);
+  const int S = c.R / 4;
+  for (int h = c.tid; h < c.H; h += kOT) {
+    const int qe = S - c.H + h;  // left halo index h - H <- the strips' ends
+    const float4 e = ld4(v + 4 * qe);
+    const float l0 = c.rank > 0 ? *cl.map_shared_rank(v + 4 * qe + 3, c.rank - 1) : 0.f;
+    st4(v + 4 * (h - c.H), make_float4(l0, e.x, e.y, e.z));
+    const float4 b = ld4(v + 4 * h);  // right halo index S + h <- the strips' starts
+    const float r3 = c.rank + 1 < CL ? *cl.map_shared_rank(v + 4 * h, c.rank + 1) : 0.f;
+    st4(v + 4 * (S + h), make_float4(b.y, b.z, b.w, r3));
   }
 }
 
-// Group `l` (4 rows from local row l) of a vector v whose own rows sit at v[0, R), just computed by
-// this thread: rows within H of either edge are also stored into the neighbouring CTA's halo of the
-// same vector (its rows [R, R + H) for our first H rows, its rows [-H, 0) for our last H rows).  The
-// cluster barrier that follows (arrive.release, then wait.acquire in the reader) makes them visible,
-// so the reader's halo is complete when its wait returns, with no load on its critical path.  The
-// halos at the two ends of the cluster are never written (zero from the system's setup).  A writer
-// only pushes after the cluster barrier that ends the neighbour's last read of that halo.
-template <int CL>
-__device__ __forceinline__ void push_halo(cg::cluster_group& cl, const OnchipCta& c, float* v, int l, float4 x) {
-  if (l < c.H && c.rank > 0) st4(cl.map_shared_rank(v + c.R + l, c.rank - 1), x);
-  if (l >= c.R - c.H && c.rank + 1 < CL) st4(cl.map_shared_rank(v + (l - c.R), c.rank + 1), x);
-}
-
-// push_halo for every edge group of this thread, re-read from its own just-written rows (the same
-// thread wrote them, so no barrier is needed; a pass of its own keeps the phase loops' registers).
+// After this thread has written its own float4s of v (strip layout), the halo entries they feed:
+//   * strip 0's first H rows (component x of q < H) into the left neighbour's right-halo component 3,
+//     strip 3's last H rows (component w of q >= S - H) into the right neighbour's left-halo
+//     component 0 -- stores into the neighbours' shared memory, so the reader's halo is complete
+//     when the cluster barrier that follows (arrive.release / wait.acquire) returns, with no load on
+//     its critical path;
+//   * the components of this CTA's own halo that come from its adjacent strips.
+// Scalar stores: the neighbour writes the remaining component of the same 16 bytes.  The halos'
+// cluster-end components are never written (zero from the system's setup).  A writer only writes
+// after the cluster barrier that ends the reader's last use of that halo.  The thread re-reads its
+// own just-written float4s (no barrier needed; a pass of its own keeps the phase loops' registers).
 template <int CL, int G4>
 __device__ __forceinline__ void push_halos(cg::cluster_group& cl, const OnchipCta& c, float* v) {
+  const int S = c.R / 4;
 #pragma unroll 1
   for (int j = 0; j < G4; ++j) {
-    const int l = 4 * (c.tid + j * kOT);
-    if (l < c.H || l >= c.R - c.H) push_halo<CL>(cl, c, v, l, ld4(v + l));
+    const int q = c.tid + j * kOT;
+    if (q < c.H) {
+      const float4 x = ld4(v + 4 * q);
+      if (c.rank > 0) *cl.map_shared_rank(v + 4 * (S + q) + 3, c.rank - 1) = x.x;
+      float* h = v + 4 * (S + q);
+      h[0] = x.y;
+      h[1] = x.z;
+      h[2] = x.w;
+    }
+    if (q >= S - c.H) {
+      const float4 x = ld4(v + 4 * q);
+      if (c.rank + 1 < CL) *cl.map_shared_rank(v + 4 * (q - S), c.rank + 1) = x.w;
+      float* h = v + 4 * (q - S);
+      h[1] = x.x;
+      h[2] = x.y;
+      h[3] = x.z;
+    }
   }
 }
 
@@ -236,7 +248,7 @@ __device__ __forceinline__ float diag_product(cg::cluster_group& cl, const Onchi
       // the shared-memory operands in two halves, so at most half of them are held at once
       float4 pv[G4 / 2];
 #pragma unroll
-      for (int jj = 0; jj < G4 / 2; ++jj) pv[jj] = ld4_off(v, 4 * (c.tid + (h * (G4 / 2) + jj) * kOT), o);
+      for (int jj = 0; jj < G4 / 2; ++jj) pv[jj] = ld4(v + 4 * (c.tid + (h * (G4 / 2) + jj) * kOT + o));
 #pragma unroll
       for (int jj = 0; jj < G4 / 2; ++jj) {
         const int j = h * (G4 / 2) + jj;
@@ -315,9 +327,10 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
 
   const int R = a.R, H = a.H;
   const int64_t n = a.n, np = a.np;
-  float* ps = smem + H;                  // p: local rows [-H, R + H)
-  float* rs = smem + (R + 2 * H) + H;    // r: local rows [-H, R + H)
-  float* ds = smem + 2 * (R + 2 * H);    // d: local rows [0, R)
+  const int S = R / 4;                     // strip length (strip layout, see sidx)
+  float* ps = smem + 4 * H;                // p: float4 indices [-H, S + H)
+  float* rs = smem + (R + 8 * H) + 4 * H;  // r: float4 indices [-H, S + H)
+  float* ds = smem + 2 * (R + 8 * H);      // d: float4 indices [0, S)
   const int tid = threadIdx.x;
   const int64_t i0 = (int64_t)rank * R;  // first row of this CTA (rows >= n are zero padding)
   float* A = a.adia + slot * a.nd * np;
@@ -345,16 +358,17 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
     for (int l = tid; l < R; l += kOT) {
       const int64_t i = i0 + l;
       const bool live = i < n;
-      csr_row_to_diagonals(a.indptr, a.indices, vals, i, live, a.off, a.nd, A + i, np);
-      Dv[i] = a.center >= 0 && A[a.center * np + i] != 0.f ? 1.f / A[a.center * np + i] : 1.f;
+      const int64_t si = i0 + sidx(l, S);  // this row's place in the diagonal slots
+      csr_row_to_diagonals(a.indptr, a.indices, vals, i, live, a.off, a.nd, A + si, np);
+      Dv[si] = a.center >= 0 && A[a.center * np + si] != 0.f ? 1.f / A[a.center * np + si] : 1.f;
       if (Gd) csr_row_to_diagonals(a.g_indptr, a.g_indices, a.g_vals + s * a.g_nnz, i, live, a.goff, a.ng, Gd + i, np);
       ps[l] = 0.f;
       rs[l] = 0.f;
       ds[l] = 0.f;
-      if (l < H) {  // halos (those at the ends of the cluster stay zero)
-        ps[l - H] = 0.f;
+      if (l < 4 * H) {  // halos (their components at the ends of the cluster stay zero)
+        ps[l - 4 * H] = 0.f;
         ps[R + l] = 0.f;
-        rs[l - H] = 0.f;
+        rs[l - 4 * H] = 0.f;
         rs[R + l] = 0.f;
       }
       if (live) {
@@ -396,12 +410,12 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
             for (int u = 0; u < kRowBatch; ++u) ctr[u] = v[u];
           } else {
 #pragma unroll
-            for (int u = 0; u < kRowBatch; ++u) M[m * np + i0 + l0 + u * kOT] = __float2bfloat16_rn(v[u]);
+            for (int u = 0; u < kRowBatch; ++u) M[m * np + i0 + sidx(l0 + u * kOT, S)] = __float2bfloat16_rn(v[u]);
           }
         }
 #pragma unroll
         for (int u = 0; u < kRowBatch; ++u)
-          M[mc * np + i0 + l0 + u * kOT] = __float2bfloat16_rn(ctr[u] + kMBoost * asum[u]);
+          M[mc * np + i0 + sidx(l0 + u * kOT, S)] = __float2bfloat16_rn(ctr[u] + kMBoost * asum[u]);
       }
     }
     const double bnorm = sqrt(v1[0]);
@@ -430,7 +444,7 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
           for (int u = 0; u < kRowBatch; ++u) {
             const int l = l0 + u * kOT;
             const int64_t c = i0 + l + o;
-            const float av = Ak[l];  // 0 where row i0 + l has no entry on this diagonal (and past n)
+            const float av = Ak[sidx(l, S)];  // 0 where row i0 + l has no entry on this diagonal (and past n)
             const double xv = c >= 0 && c < n ? X[c] : 0.0;
             ax[u] += (double)av * xv;
           }
@@ -441,7 +455,7 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
           const int64_t i = i0 + l;
           if (i < n) {
             const double rv = B[i] * binv - ax[u];
-            rs[l] = (float)rv;
+            rs[sidx(l, S)] = (float)rv;
             rr += rv * rv;
           }
         }
@@ -555,9 +569,10 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
           for (int u = 0; u < kRowBatch; ++u) {
             const int l = l0 + u * kOT;
             const int64_t i = i0 + l;
-            const float dn = ds[l] + alpha * ps[l];
+            const int sl = sidx(l, S);
+            const float dn = ds[sl] + alpha * ps[sl];
             if (i < n) X[i] = xv[u] + (double)dn;
-            ds[l] = 0.f;
+            ds[sl] = 0.f;
           }
         }
         dpend = false;
@@ -628,7 +643,7 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
       for (int u = 0; u < kRowBatch; ++u) {
         const int l = l0 + u * kOT;
         const int64_t i = i0 + l;
-        if (i < n) X[i] = (xv[u] + (double)ds[l]) * (bnorm > 0.0 ? bnorm : 1.0);
+        if (i < n) X[i] = (xv[u] + (double)ds[sidx(l, S)]) * (bnorm > 0.0 ? bnorm : 1.0);
       }
     }
     if (rank == 0 && tid == 0) {
@@ -701,6 +716,9 @@ static int diag_offsets(const int32_t* indptr, const int32_t* indices, int64_t n
   if (h[0] > 32) offs.push_back(0);  // more than 32: marks the pattern as not diagonal-structured
   return COLAGB_OK;
 }
+
+// Dynamic shared memory per CTA: p and r with their halos (S + 2H float4s each, S = R / 4), d.
+static size_t onchip_smem_bytes(int R, int H) { return (size_t)(3 * R + 16 * H) * sizeof(float); }
 
 // Cluster size and rows per CTA for the on-chip schedule, from n alone (also used to size the
 // workspace).  Returns 0 when n is too large to keep p, r and d on chip.
@@ -855,8 +873,8 @@ int onchip_pcg_solve(const colagb_batched_csr* Acsr, const double* B, double* X,
     a.pstart[a.nm] = q;
   }
   H = (H + 3) / 4 * 4;  // halo rows in whole 16-byte words
-  if (H > R) return COLAGB_OK;
-  const size_t smem = (size_t)(3 * R + 4 * H) * sizeof(float);
+  if (H > R / 4) return COLAGB_OK;  // a halo reaches at most one strip (strip layout)
+  const size_t smem = onchip_smem_bytes(R, H);
   if (smem > kOnchipSmemMax) return COLAGB_OK;
 
   a.n = n;
@@ -915,9 +933,10 @@ extern "C" int colagb_onchip_schedule_info(int64_t n, int32_t halo, int32_t* inf
   info[2] = 0;
   info[3] = 0;
   if (CL == 0) return COLAGB_OK;
-  const size_t smem = (size_t)(3 * R + 4 * halo) * sizeof(float);
+  const int H = (halo + 3) / 4 * 4;
+  const size_t smem = onchip_smem_bytes(R, H);
   info[3] = (int32_t)smem;
-  if (smem > kOnchipSmemMax || halo > R) return COLAGB_OK;
+  if (smem > kOnchipSmemMax || H > R / 4) return COLAGB_OK;
   int nc = 0, rc;
   if (CL == 8)
     rc = G == 8 ? onchip_active_clusters<8, 8>(smem, &nc)
