@@ -172,28 +172,36 @@ __device__ __forceinline__ void fill_halo(cg::cluster_group& cl, const OnchipCta
 // cluster-end components are never written (zero from the system's setup).  A writer only writes
 // after the cluster barrier that ends the reader's last use of that halo.  The thread re-reads its
 // own just-written float4s (no barrier needed; a pass of its own keeps the phase loops' registers).
+template <int CL>
+__device__ __forceinline__ void push_edge_lo(cg::cluster_group& cl, const OnchipCta& c, float* v, int S, int q) {
+  const float4 x = ld4(v + 4 * q);  // q < H: strip starts
+  if (c.rank > 0) *cl.map_shared_rank(v + 4 * (S + q) + 3, c.rank - 1) = x.x;
+  float* h = v + 4 * (S + q);  // own right halo, components 0..2
+  *reinterpret_cast<float2*>(h) = make_float2(x.y, x.z);
+  h[2] = x.w;
+}
+template <int CL>
+__device__ __forceinline__ void push_edge_hi(cg::cluster_group& cl, const OnchipCta& c, float* v, int S, int q) {
+  const float4 x = ld4(v + 4 * q);  // q >= S - H: strip ends
+  if (c.rank + 1 < CL) *cl.map_shared_rank(v + 4 * (q - S), c.rank + 1) = x.w;
+  float* h = v + 4 * (q - S);  // own left halo, components 1..3
+  h[1] = x.x;
+  *reinterpret_cast<float2*>(h + 2) = make_float2(x.y, x.z);
+}
 template <int CL, int G4>
 __device__ __forceinline__ void push_halos(cg::cluster_group& cl, const OnchipCta& c, float* v) {
   const int S = c.R / 4;
+  if (c.H <= kOT) {  // the edge float4s are this thread's first and last groups only
+    if (c.tid < c.H) push_edge_lo<CL>(cl, c, v, S, c.tid);
+    const int q = c.tid + (G4 - 1) * kOT;
+    if (q >= S - c.H) push_edge_hi<CL>(cl, c, v, S, q);
+    return;
+  }
 #pragma unroll 1
   for (int j = 0; j < G4; ++j) {
     const int q = c.tid + j * kOT;
-    if (q < c.H) {
-      const float4 x = ld4(v + 4 * q);
-      if (c.rank > 0) *cl.map_shared_rank(v + 4 * (S + q) + 3, c.rank - 1) = x.x;
-      float* h = v + 4 * (S + q);
-      h[0] = x.y;
-      h[1] = x.z;
-      h[2] = x.w;
-    }
-    if (q >= S - c.H) {
-      const float4 x = ld4(v + 4 * q);
-      if (c.rank + 1 < CL) *cl.map_shared_rank(v + 4 * (q - S), c.rank + 1) = x.w;
-      float* h = v + 4 * (q - S);
-      h[1] = x.x;
-      h[2] = x.y;
-      h[3] = x.z;
-    }
+    if (q < c.H) push_edge_lo<CL>(cl, c, v, S, q);
+    if (q >= S - c.H) push_edge_hi<CL>(cl, c, v, S, q);
   }
 }
 
