@@ -113,7 +113,7 @@ SIGNATURES = {
     "colagb_fsai_features": (C.c_int, [_vp, _i64, _i64, _vp, _vp]),
     "colagb_fsai_assemble": (C.c_int, [_vp, _vp, _i64, _i64, _vp, _vp]),
     "colagb_fsai_compact": (C.c_int, [_vp, _vp, _i64, _i64, _i64, _vp, _vp]),
-    "colagb_fsai_net_build": (C.c_int, [_vp, _vp, _i64, _i64, _i64, _vp, _i64, _vp, _vp]),
+    "colagb_fsai_net_build": (C.c_int, [_vp, _vp, _i64, _i64, _i64, _vp, _i64, _vp, _vp, _vp]),
     "colagb_fsai_closed_build": (C.c_int, [_vp, _i64, _i64, _vp, _i64, _vp, _vp]),
     "colagb_conv3x3_forward": (C.c_int, [_vp, _i64, _i32, _i32, _i64, _i64, _vp, _vp, _i32, _vp, _vp]),
     "colagb_conv3x3_backward_scratch_bytes": (C.c_int, [_i32, _i32, _P(_sz)]),

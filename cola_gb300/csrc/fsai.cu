@@ -282,7 +282,8 @@ __device__ __forceinline__ void net_store(const float (&acc)[PPT][COUT / NG], in
 
 __global__ void __launch_bounds__(kNetThreads, 1)
     k_fsai_net_build(const float* __restrict__ st, const float* __restrict__ params, int64_t m, int64_t S,
-                     const int32_t* __restrict__ g_indptr, int64_t g_nnz, float* __restrict__ out) {
+                     const int32_t* __restrict__ g_indptr, int64_t g_nnz, float* __restrict__ out,
+                     unsigned int* tile_counter) {
   extern __shared__ __align__(16) float nsm[];
   float* bufA = nsm;
   float* bufB = bufA + kNetBufA;
@@ -308,11 +309,20 @@ __global__ void __launch_bounds__(kNetThreads, 1)
 
   const int64_t n = m * m;
   const int64_t side = (m + kNetTile - 1) / kNetTile, per_sys = side * side;
-  for (int64_t tile = blockIdx.x; tile < per_sys * S; tile += gridDim.x) {
+  __shared__ unsigned int s_tile;
+  // tiles from an atomic counter, so that the CTAs that get an SM early (e.g. beside another
+  // kernel that holds the others) take the work of the ones that start late
+  for (int64_t tile0 = blockIdx.x;; tile0 += gridDim.x) {
+    __syncthreads();  // weights in; the previous tile's reads of buffer A and of s_tile done
+    if (tile_counter) {
+      if (tid == 0) s_tile = atomicAdd(tile_counter, 1u);
+      __syncthreads();
+    }
+    const int64_t tile = tile_counter ? (int64_t)s_tile : tile0;
+    if (tile >= per_sys * S) break;
     const int64_t s = tile / per_sys, r = tile % per_sys;
     const int y0 = (int)(r / side) * kNetTile, x0 = (int)(r % side) * kNetTile;
     const float* a = st + s * 5 * n;
-    __syncthreads();  // weights in; the previous tile's reads of buffer A done
     // features (as k_fsai_features) on the 38^2 region from (y0 - 3, x0 - 3)
     for (int q = tid; q < kNetF * kNetF; q += kNetThreads) {
       const int y = y0 - 3 + q / kNetF, x = x0 - 3 + q % kNetF;
@@ -731,7 +741,8 @@ extern "C" int colagb_fsai_compact(const float* g_stencil, const int32_t* g_indp
 }
 
 extern "C" int colagb_fsai_net_build(const float* stencil, const float* params, int64_t n_params, int64_t m, int64_t S,
-                                     const int32_t* g_indptr, int64_t g_nnz, float* g_values, void* stream) {
+                                     const int32_t* g_indptr, int64_t g_nnz, float* g_values, uint32_t* tile_counter,
+                                     void* stream) {
   if (!stencil || !params || !g_indptr || !g_values || m < 1 || S < 0)
     return fail(COLAGB_ERR_INVALID, "colagb_fsai_net_build: bad arguments");
   if (n_params != kNetParams)
@@ -742,8 +753,9 @@ extern "C" int colagb_fsai_net_build(const float* stencil, const float* params, 
   const int64_t side = (m + kNetTile - 1) / kNetTile;
   const int64_t tiles = side * side * S;
   const int grid = (int)std::min<int64_t>(tiles, num_sms());
+  if (tile_counter) COLAGB_CUDA(cudaMemsetAsync(tile_counter, 0, sizeof(uint32_t), as_stream(stream)));
   k_fsai_net_build<<<grid, kNetThreads, kNetSmemBytes, as_stream(stream)>>>(stencil, params, m, S, g_indptr, g_nnz,
-                                                                            g_values);
+                                                                            g_values, tile_counter);
   COLAGB_CUDA(cudaGetLastError());
   return COLAGB_OK;
 }

@@ -214,6 +214,7 @@ def g_values(fam: BatchedCSR, net: FsaiNet | None, pat: FsaiPattern | None = Non
     pat = pat or FsaiPattern(fam.indptr, fam.indices)
     out = torch.empty((fam.num_systems, pat.g_nnz), dtype=torch.float32, device=fam.values.device)
     err = torch.zeros(1, dtype=torch.int32, device=fam.values.device)
+    counter = torch.empty(1, dtype=torch.int32, device=fam.values.device)  # tiles in arrival order
     lib = _lib()
     for s0 in range(0, fam.num_systems, batch):
         sub = BatchedCSR(fam.indptr, fam.indices, fam.values[s0: s0 + batch])
@@ -222,7 +223,7 @@ def g_values(fam: BatchedCSR, net: FsaiNet | None, pat: FsaiPattern | None = Non
         if net is not None:
             _capi.check(lib.colagb_fsai_net_build(st.data_ptr(), net.params.data_ptr(), net.params.numel(), m,
                                                   sub.num_systems, pat.g_indptr.data_ptr(), pat.g_nnz,
-                                                  dst.data_ptr(), _sp(st)), "net build")
+                                                  dst.data_ptr(), counter.data_ptr(), _sp(st)), "net build")
         else:
             _capi.check(lib.colagb_fsai_closed_build(st.data_ptr(), m, sub.num_systems, pat.g_indptr.data_ptr(),
                                                      pat.g_nnz, dst.data_ptr(), _sp(st)), "closed build")

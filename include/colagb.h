@@ -327,9 +327,12 @@ int colagb_fsai_compact(const float* g_stencil, const int32_t* g_indptr, int64_t
  * from the stencil and the network's parameters (n_params = 3635 floats in FsaiNet's flat layout:
  * per layer W (cout, cin, 3, 3) then b (cout), layers 6->16 ReLU, 16->16 ReLU, 16->3).  The same
  * values as colagb_fsai_features -> 3 x colagb_conv3x3_forward -> colagb_fsai_assemble ->
- * colagb_fsai_compact, without the intermediate fields. */
+ * colagb_fsai_compact, without the intermediate fields.  tile_counter (device, one word, may be NULL):
+ * scratch that lets the CTAs take 32 x 32 tiles in arrival order -- pass one when the build shares
+ * the GPU with another kernel (e.g. the previous batch's solve on another stream). */
 int colagb_fsai_net_build(const float* stencil, const float* params, int64_t n_params, int64_t m, int64_t S,
-                          const int32_t* g_indptr, int64_t g_nnz, float* g_values, void* stream);
+                          const int32_t* g_indptr, int64_t g_nnz, float* g_values, uint32_t* tile_counter,
+                          void* stream);
 /* closed-form FSAI straight to CSR values (colagb_fsai_assemble with NULL, then colagb_fsai_compact) */
 int colagb_fsai_closed_build(const float* stencil, int64_t m, int64_t S, const int32_t* g_indptr, int64_t g_nnz,
                              float* g_values, void* stream);

@@ -203,5 +203,5 @@ def test_fused_build_rejects_other_network_shapes():
     out = torch.empty((1, pat.g_nnz), dtype=torch.float32, device=DEV)
     bad = torch.zeros(100, dtype=torch.float32, device=DEV)
     rc = _capi.load().colagb_fsai_net_build(st.data_ptr(), bad.data_ptr(), bad.numel(), 16, 1, pat.g_indptr.data_ptr(),
-                                            pat.g_nnz, out.data_ptr(), _capi.stream_ptr(DEV))
+                                            pat.g_nnz, out.data_ptr(), None, _capi.stream_ptr(DEV))
     assert rc != 0
