@@ -469,6 +469,29 @@ def test_onchip_three_d_shared_values_and_unsupported_patterns():
     assert float((R.norm(dim=1) / B.norm(dim=1)).max()) <= 1.01e-8
 
 
+@pytest.mark.parametrize("precond", ["none", "jacobi"])
+def test_onchip_halo_as_long_as_a_strip(precond):
+    """3-D 7-point operator on 32^3 cells: the halo (m^2 = 1024 rows) is exactly one strip of a CTA
+    (R = 4096 rows in strips of 1024), the longest halo the on-chip strip layout takes.  Same
+    solutions as the CSR cluster schedule."""
+    from cola_gb300.linalg.batched import BatchedCSR, onchip_schedule_info
+    from cola_gb300.workloads import diffusion_3d
+    ip, ix, v = diffusion_3d(m=32, device=DEV)
+    fam = BatchedCSR(ip, ix, v[None, :], shared=True)
+    geo = onchip_schedule_info(fam.n, 32 * 32)
+    assert geo["cluster_size"] == 8 and geo["rows_per_cta"] == 4096 and geo["clusters_in_flight"] > 0
+    B = torch.randn(3, fam.n, device=DEV, dtype=torch.float64, generator=torch.Generator(DEV).manual_seed(9))
+    X1, i1 = cola.linalg.solve_batched(fam, B, precond=precond, tol=1e-8, schedule="onchip")
+    X2, i2 = cola.linalg.solve_batched(fam, B, precond=precond, tol=1e-8, schedule="cluster8")
+    assert i1["schedule"] == "onchip"
+    assert torch.all(i1["status"] == 1) and torch.all(i2["status"] == 1)
+    R = B - fam.matvec(X1)
+    assert float((R.norm(dim=1) / B.norm(dim=1)).max()) <= 1.01e-8
+    assert rel(X1, X2) < 1e-6
+    k1, k2 = i1["iterations"].double(), i2["iterations"].double()
+    assert float(((k1 - k2).abs() - (0.15 * k2 + 3)).max()) <= 0, (k1.tolist(), k2.tolist())
+
+
 def test_dense_batched_uneven_matches_per_system_reference_loop():
     """Uneven dense systems in one launch; each equals a separate reference CG call (oracle, float32)."""
     from cola_gb300.linalg.batched import solve_dense_batched
