@@ -188,6 +188,36 @@ __device__ __forceinline__ void push_edge_hi(cg::cluster_group& cl, const Onchip
   h[1] = x.x;
   *reinterpret_cast<float2*>(h + 2) = make_float2(x.y, x.z);
 }
+// Phases B and C visit the groups edge-first (0, G4 - 1, 1, 2, ...) and push an edge group as soon
+// as it is stored (push_group), so that the stores into the neighbours are in flight while the
+// other groups are updated instead of holding up the barrier's release.  When H > kOT the edge
+// rows span more groups and push_halos_wide pushes them after the phase.
+template <int G4>
+__device__ constexpr int edge_first(int t) { return t == 0 ? 0 : (t == 1 ? G4 - 1 : t - 1); }
+
+template <int CL, int G4>
+__device__ __forceinline__ void push_group(cg::cluster_group& cl, const OnchipCta& c, float* v, int j) {
+  if (c.H > kOT) return;
+  const int S = c.R / 4;
+  if (j == 0 && c.tid < c.H) push_edge_lo<CL>(cl, c, v, S, c.tid);
+  if (j == G4 - 1) {
+    const int q = c.tid + (G4 - 1) * kOT;
+    if (q >= S - c.H) push_edge_hi<CL>(cl, c, v, S, q);
+  }
+}
+
+template <int CL, int G4>
+__device__ __forceinline__ void push_halos_wide(cg::cluster_group& cl, const OnchipCta& c, float* v) {
+  if (c.H <= kOT) return;
+  const int S = c.R / 4;
+#pragma unroll 1
+  for (int j = 0; j < G4; ++j) {
+    const int q = c.tid + j * kOT;
+    if (q < c.H) push_edge_lo<CL>(cl, c, v, S, q);
+    if (q >= S - c.H) push_edge_hi<CL>(cl, c, v, S, q);
+  }
+}
+
 template <int CL, int G4>
 __device__ __forceinline__ void push_halos(cg::cluster_group& cl, const OnchipCta& c, float* v) {
   const int S = c.R / 4;
@@ -520,13 +550,13 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
         float4 rv[H4], dv[H4];
 #pragma unroll
         for (int jj = 0; jj < H4; ++jj) {
-          const int j = h * H4 + jj;
+          const int j = edge_first<G4>(h * H4 + jj);
           rv[jj] = rown[j];
           dv[jj] = prec == COLAGB_PREC_JACOBI ? ld4(Dv + i0 + 4 * (tid + j * kOT)) : make_float4(1.f, 1.f, 1.f, 1.f);
         }
 #pragma unroll
         for (int jj = 0; jj < H4; ++jj) {
-          const int j = h * H4 + jj;
+          const int j = edge_first<G4>(h * H4 + jj);
           rv[jj].x -= alpha * zq[j].x;
           rv[jj].y -= alpha * zq[j].y;
           rv[jj].z -= alpha * zq[j].z;
@@ -542,11 +572,15 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
           }
         }
 #pragma unroll
-        for (int jj = 0; jj < H4; ++jj) st4(rs + 4 * (tid + (h * H4 + jj) * kOT), rv[jj]);
+        for (int jj = 0; jj < H4; ++jj) {
+          const int j = edge_first<G4>(h * H4 + jj);
+          st4(rs + 4 * (tid + j * kOT), rv[jj]);
+          if (prec == COLAGB_PREC_FSAI) push_group<CL, G4>(cl, ctx, rs, j);  // M r reads r's halo
+        }
       }
       float qb[2] = {rrf, rzf};
       if (prec == COLAGB_PREC_FSAI) {
-        push_halos<CL, G4>(cl, ctx, rs);  // M r reads r's halo
+        push_halos_wide<CL, G4>(cl, ctx, rs);
         __syncthreads();
         cluster_arrive();
         qb[1] = apply_z<CL, G4>(cl, ctx, zq, prec, a, M, Dv, rs, true);
@@ -617,20 +651,22 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
         float4 po[H4], dd[H4];
 #pragma unroll
         for (int jj = 0; jj < H4; ++jj) {
-          po[jj] = ld4(ps + 4 * (tid + (h * H4 + jj) * kOT));
-          dd[jj] = ld4(ds + 4 * (tid + (h * H4 + jj) * kOT));
+          const int j = edge_first<G4>(h * H4 + jj);
+          po[jj] = ld4(ps + 4 * (tid + j * kOT));
+          dd[jj] = ld4(ds + 4 * (tid + j * kOT));
         }
 #pragma unroll
         for (int jj = 0; jj < H4; ++jj) {
-          const int j = h * H4 + jj;
+          const int j = edge_first<G4>(h * H4 + jj);
           st4(ps + 4 * (tid + j * kOT), make_float4(zq[j].x + beta * po[jj].x, zq[j].y + beta * po[jj].y,
                                                     zq[j].z + beta * po[jj].z, zq[j].w + beta * po[jj].w));
           if (dpend)
             st4(ds + 4 * (tid + j * kOT), make_float4(dd[jj].x + alpha * po[jj].x, dd[jj].y + alpha * po[jj].y,
                                                       dd[jj].z + alpha * po[jj].z, dd[jj].w + alpha * po[jj].w));
+          push_group<CL, G4>(cl, ctx, ps, j);
         }
       }
-      push_halos<CL, G4>(cl, ctx, ps);
+      push_halos_wide<CL, G4>(cl, ctx, ps);
       __syncthreads();
       cluster_arrive();  // p and its halos published; waited for at the start of the next step
       arrived = true;
