@@ -198,10 +198,10 @@ BUILD_LAUNCHES_PER_64 = {"learned": 2, "fsai": 2}
 
 PRECOND = {"plain": "none", "jacobi": "jacobi", "learned": "fsai", "fsai": "fsai"}
 # DRAM bytes (read + write) of one on-chip solve launch per system, from one ncu capture of
-# k_onchip_pcg on 7 systems of this workload (FSAI, ~1070 steps each): 371.1 MB + 186.6 MB.  DRAM
+# k_onchip_pcg on 7 systems of this workload (FSAI, ~1056 steps each): 210.8 MB + 145.8 MB.  DRAM
 # traffic is per system (reading its CSR values and right-hand side, writing its diagonals and x):
 # the diagonals of the systems in flight are re-read from L2 at every step.
-ONCHIP_DRAM_BYTES_PER_SYSTEM = 557.7e6 / 7
+ONCHIP_DRAM_BYTES_PER_SYSTEM = 356.6e6 / 7
 KERNEL_OF = {"onchip": "k_onchip_pcg", "cluster8": "k_cluster_pcg", "cluster16": "k_cluster_pcg",
              "grid": "k_batched_ir"}
 
