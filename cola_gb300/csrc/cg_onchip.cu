@@ -129,9 +129,10 @@ struct OnchipCta {
   int64_t np, i0;  // padded rows per diagonal, first row of this CTA
 };
 
-// Thread `tid` owns row groups q = tid + j kOT (j < G4) of its CTA, i.e. local rows 4q .. 4q + 3:
-// every load and store of the hot loops is 128 bits wide and consecutive threads touch consecutive
-// 16-byte words (coalesced global accesses, conflict-free shared-memory accesses).
+// Thread `tid` owns the float4s q = tid + j kOT (j < G4) of its CTA (rows q, q + S, q + 2S, q + 3S
+// in the strip layout below): every load and store of the hot loops is 128 bits wide and
+// consecutive threads touch consecutive 16-byte words (coalesced global accesses, conflict-free
+// shared-memory accesses).
 __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
 __device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
 __device__ __forceinline__ float dot4(float4 a, float4 b) { return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w; }
@@ -235,18 +236,8 @@ __device__ __forceinline__ void push_halos(cg::cluster_group& cl, const OnchipCt
   }
 }
 
-// zq[j] = sum_k D[k][rows of group j] * v[rows + off[k]], k ascending (the host puts the main
-// diagonal last, the others in column order); returns this thread's part of <v, D v>.  One diagonal at a time over all of the thread's groups (G4 128-bit
-// loads per thread, ~64 KB per SM), pipelined by halves: once the first half of diagonal k has been
-// used, its registers load the first half of diagonal k + 1 while the second half of k is still
-// arriving.  (Waiting for a whole diagonal before issuing the next cost one L2 round trip plus the
-// transfer per diagonal, ~1.9k cycles for 64 KB per SM; double-buffering whole diagonals needs more
-// registers than the 128 a thread has here next to the G4 result registers.)  `pending`: a
-// cluster_arrive() publishing v's own rows and the halos pushed into the neighbours (push_halo) is
-// outstanding; the first diagonal's loads are issued before waiting on it (the matrix does not
-// depend on it).
-// Four consecutive diagonal values as they sit in registers between load and use: FP32 (A) or
-// bfloat16 (M, 8 bytes per 4 rows, widened to FP32 when used).
+// The four diagonal values of one float4 group as they sit in registers between load and use: FP32
+// (A) or bfloat16 (M, 8 bytes per group, widened to FP32 when used).
 template <typename T>
 struct Diag4;
 template <>
@@ -265,6 +256,17 @@ struct Diag4<__nv_bfloat16> {
   }
 };
 
+// zq[j] = sum_k D[k][rows of group j] * v[rows + off[k]], k ascending (the host puts the main
+// diagonal last, the others in column order); returns this thread's part of <v, D v>.  One
+// diagonal at a time over all of the thread's groups (G4 128-bit loads per thread, ~64 KB per SM
+// for FP32), pipelined by halves: once the first half of diagonal k has been
+// used, its registers load the first half of diagonal k + 1 while the second half of k is still
+// arriving.  (Waiting for a whole diagonal before issuing the next cost one L2 round trip plus the
+// transfer per diagonal, ~1.9k cycles for 64 KB per SM; double-buffering whole diagonals needs more
+// registers than the 128 a thread has here next to the G4 result registers.)  `pending`: a
+// cluster_arrive() publishing v's own rows and the halos pushed into the neighbours (push_halos) is
+// outstanding; the first diagonal's loads are issued before waiting on it (the matrix does not
+// depend on it).
 template <int CL, int G4, typename T>
 __device__ __forceinline__ float diag_product(cg::cluster_group& cl, const OnchipCta& c, float4 (&zq)[G4],
                                               const T* D, const int* off, int nk, float* v, bool pending) {
