@@ -225,3 +225,20 @@ def test_bfloat16_preconditioner_boost_keeps_it_spd():
         assert np.array_equal(Mp, Mp.T)
         assert np.linalg.eigvalsh((Mp - M).astype(np.float64))[0] >= -1e-12 * np.abs(M).max()
         assert np.linalg.eigvalsh(Mp.astype(np.float64))[0] > 0
+
+
+def test_bench_byte_model_and_launch_count():
+    """The roofline's algorithmic bytes and the launch count the bench reports: on-chip steps move
+    only the matrix diagonals (A in FP32, M = G^T G in bfloat16); the CSR schedules move the values
+    and six vector streams; each timed step launches the build (two kernels per 64 systems), the
+    pattern analysis and the solve."""
+    import sys
+    sys.path.insert(0, str(ROOT))
+    import bench
+    n, nnz = 512 * 512, 1308672
+    assert bench.bytes_per_system_iter(n, nnz, "learned", "onchip", 5, 7) == (5 * 4 + 7 * 2) * n
+    assert bench.bytes_per_system_iter(n, nnz, "jacobi", "onchip", 5, 7) == 5 * 4 * n + 4 * n
+    assert bench.bytes_per_system_iter(n, nnz, "plain", "cluster8") == nnz * 4 + 6 * n * 4
+    assert bench.launches_per_solve("onchip", "learned", 256) == 4 * 2 + (1 + 2 * 2)
+    assert bench.launches_per_solve("onchip", "plain", 256) == 1 + 2
+    assert bench.launches_per_solve("cluster8", "jacobi", 2048) == 2
