@@ -242,3 +242,39 @@ def test_bench_byte_model_and_launch_count():
     assert bench.launches_per_solve("onchip", "learned", 256) == 4 * 2 + (1 + 2 * 2)
     assert bench.launches_per_solve("onchip", "plain", 256) == 1 + 2
     assert bench.launches_per_solve("cluster8", "jacobi", 2048) == 2
+
+
+def test_c_program_links_and_calls_the_abi(tmp_path):
+    """The drop-in boundary from C, without Python: a program compiled against include/colagb.h and
+    linked to libcolagb.so calls entry points that need no GPU (version, argument validation and the
+    per-thread error text) and gets the documented status codes."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lib = _capi.LIB_PATH
+    src = tmp_path / "abi.c"
+    src.write_text(r'''
+#include <stdio.h>
+#include <string.h>
+#include "colagb.h"
+int main(void) {
+  int32_t v = 0, a = 0;
+  if (colagb_version(&v, &a) != COLAGB_OK || a != 1003) return 1;
+  /* a null output pointer is an argument error with a message */
+  if (colagb_onchip_schedule_info(1024, 32, NULL) != COLAGB_ERR_INVALID) return 2;
+  if (strlen(colagb_last_error()) == 0) return 3;
+  /* an empty operator description is rejected before any device work */
+  colagb_op* h = NULL;
+  if (colagb_op_create(NULL, 0, 0, &h) == COLAGB_OK) return 4;
+  printf("ok %d\n", (int)v);
+  return 0;
+}
+''')
+    exe = tmp_path / "abi"
+    subprocess.run([cc, str(src), "-I", str(ROOT / "include"), "-L", str(lib.parent), "-lcolagb",
+                    f"-Wl,-rpath,{lib.parent}", "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, (out.returncode, out.stderr)
+    assert out.stdout.startswith("ok ")
