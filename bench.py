@@ -488,8 +488,8 @@ def run_reference(args, world, rank):
                                        device=dev)
     vals = []
     cb = None
-    for _ in range(args.warmup if args.warmup < 1 else 0):
-        pass
+    if args.warmup > 0:  # untimed: a short sample warms the host's thread pool and caches
+        cpu_baseline(args, fam, B, sample_s=min(2.0, args.ref_seconds))
     for _ in range(args.steps):
         cb = cpu_baseline(args, fam, B, sample_s=args.ref_seconds)
         vals.append(cb["value"])
