@@ -488,8 +488,12 @@ def run_reference(args, world, rank):
                                        device=dev)
     vals = []
     cb = None
-    if args.warmup > 0:  # untimed: a short sample warms the host's thread pool and caches
-        cpu_baseline(args, fam, B, sample_s=min(2.0, args.ref_seconds))
+    if args.warmup > 0:  # untimed: 50 steps of the same loop warm the host's thread pool and caches
+        from oracle.torch_ref import csr_matmat, run_batched_cg
+        torch.set_num_threads(os.cpu_count() or 1)
+        mm = csr_matmat(fam.indptr.cpu(), fam.indices.cpu(), fam.values[0].double().cpu(), fam.n)
+        b0 = B[0].double().cpu()[:, None]
+        run_batched_cg(mm, b0, torch.zeros_like(b0), 50, 5e-9)
     for _ in range(args.steps):
         cb = cpu_baseline(args, fam, B, sample_s=args.ref_seconds)
         vals.append(cb["value"])
