@@ -205,3 +205,29 @@ def test_fused_build_rejects_other_network_shapes():
     rc = _capi.load().colagb_fsai_net_build(st.data_ptr(), bad.data_ptr(), bad.numel(), 16, 1, pat.g_indptr.data_ptr(),
                                             pat.g_nnz, out.data_ptr(), None, _capi.stream_ptr(DEV))
     assert rc != 0
+
+
+def test_overlapped_build_and_no_wait_pipeline_matches_sequential():
+    """The bench's pipeline: family i + 1's learned factor is built on a side stream while family i
+    solves (wait=False returns at once); every solution equals the sequential calls' bit for bit."""
+    from cola_gb300.linalg.batched import BatchedCSR
+    fam, B, _, _ = diffusion_family_2d(list(range(80, 88)), m=64, device=DEV)
+    fam2 = BatchedCSR(fam.indptr, fam.indices, fam.values.flip(0).contiguous())
+    net = L.FsaiNet.load(device=DEV) if L.WEIGHTS.exists() else L.FsaiNet(DEV, seed=1)
+    pat = FsaiPattern(fam.indptr, fam.indices)
+    seq = [solve_batched(f, B, precond="fsai", fsai=L.g_values(f, net, pat), tol=1e-8)[0] for f in (fam, fam2)]
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream()
+    side = torch.cuda.Stream()
+    X0, i0 = solve_batched(fam, B, precond="fsai", fsai=L.g_values(fam, net, pat), tol=1e-8, wait=False)
+    with torch.cuda.stream(side):
+        fs1 = L.g_values(fam2, net, pat)
+        ready = torch.cuda.Event()
+        ready.record(side)
+    st.wait_event(ready)
+    fs1[1].record_stream(st)
+    X1, i1 = solve_batched(fam2, B, precond="fsai", fsai=fs1, tol=1e-8, wait=False)
+    torch.cuda.synchronize()
+    assert i0["schedule"] == "onchip" and i0["sweeps"] is None
+    assert torch.equal(X0, seq[0]) and torch.equal(X1, seq[1])
+    assert bool((i1["status"] == 1).all())
