@@ -181,8 +181,12 @@ _ws_cache: dict = {}
 
 
 def workspace(nbytes: int, device: torch.device) -> torch.Tensor:
-    """A device scratch buffer of at least nbytes (cached per device, grown on demand)."""
-    key = (device.type, device.index if device.index is not None else torch.cuda.current_device())
+    """A device scratch buffer of at least nbytes for work on the device's current stream, cached per
+    (device, stream) and grown on demand: calls on one stream reuse it in stream order (also calls
+    that return before their kernels finish, e.g. a batched solve with wait=False), calls on
+    different streams never share it."""
+    idx = device.index if device.index is not None else torch.cuda.current_device()
+    key = (device.type, idx, stream_ptr(torch.device(device.type, idx)))
     buf = _ws_cache.get(key)
     if buf is None or buf.numel() < nbytes:
         buf = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)

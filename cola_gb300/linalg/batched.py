@@ -165,8 +165,8 @@ def solve_batched(A: BatchedCSR, B: torch.Tensor, precond: str = "jacobi", tol: 
             every system together; "auto" (default) -- "onchip" when it applies, else a cluster.
         wait: False returns once the solve is enqueued on the current stream (the on-chip and cluster
             schedules); X and the per-system tensors of info are then ready in stream order and
-            info["sweeps"] is None.  Later calls on other streams must not run before it completes
-            (the library's scratch buffer is shared).
+            info["sweeps"] is None.  The scratch buffer is per stream, so solves on other streams may
+            run meanwhile.
     Returns (X (S, n) float64, info) with per-system iterations, status and FP64 relative residuals.
     """
     _capi.require_cuda(A.values, B)

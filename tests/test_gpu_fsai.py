@@ -231,3 +231,21 @@ def test_overlapped_build_and_no_wait_pipeline_matches_sequential():
     assert i0["schedule"] == "onchip" and i0["sweeps"] is None
     assert torch.equal(X0, seq[0]) and torch.equal(X1, seq[1])
     assert bool((i1["status"] == 1).all())
+
+
+def test_no_wait_solves_on_two_streams_do_not_share_scratch():
+    """Two batched solves enqueued with wait=False on different streams at once: each stream has its
+    own library scratch (the on-chip schedule's diagonal slots and system counter live there), so
+    both give the sequential solutions bit for bit."""
+    from cola_gb300.linalg.batched import BatchedCSR
+    fam, B, _, _ = diffusion_family_2d(list(range(90, 96)), m=64, device=DEV)
+    fam2 = BatchedCSR(fam.indptr, fam.indices, (1.5 * fam.values).contiguous())
+    seq = [solve_batched(f, B, precond="jacobi", tol=1e-8)[0] for f in (fam, fam2)]
+    torch.cuda.synchronize()
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    X0, _ = solve_batched(fam, B, precond="jacobi", tol=1e-8, wait=False)
+    with torch.cuda.stream(side):
+        X1, _ = solve_batched(fam2, B, precond="jacobi", tol=1e-8, wait=False)
+    torch.cuda.synchronize()
+    assert torch.equal(X0, seq[0]) and torch.equal(X1, seq[1])
