@@ -7,6 +7,7 @@ the reason.
 """
 from __future__ import annotations
 
+import collections
 import ctypes as C
 import threading
 from pathlib import Path
@@ -123,6 +124,7 @@ SIGNATURES = {
     "colagb_fsai_rq_loss_grad": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _i64, _i64, _vp, _vp, _vp, _sz, _vp]),
     "colagb_adam_step": (C.c_int, [_vp, _vp, _vp, _vp, _i64, C.c_float, C.c_float, C.c_float, C.c_float, _i32,
                                    _vp]),
+    "colagb_read_bandwidth_probe": (C.c_int, [_vp, _sz, _i32, _vp, _vp]),
 }
 
 _lib = None
@@ -177,18 +179,24 @@ def require_cuda(*tensors: torch.Tensor) -> None:
                              f"{t.device}); there is no CPU execution path")
 
 
-_ws_cache: dict = {}
+_ws_cache: "collections.OrderedDict" = collections.OrderedDict()
+_WS_CACHE_STREAMS = 8
 
 
 def workspace(nbytes: int, device: torch.device) -> torch.Tensor:
     """A device scratch buffer of at least nbytes for work on the device's current stream, cached per
     (device, stream) and grown on demand: calls on one stream reuse it in stream order (also calls
     that return before their kernels finish, e.g. a batched solve with wait=False), calls on
-    different streams never share it."""
+    different streams never share it.  The cache keeps the buffers of the 8 most recently used
+    streams; an older stream's buffer is dropped, and torch's allocator hands its memory out again
+    only in that stream's order, so work still queued there is not disturbed."""
     idx = device.index if device.index is not None else torch.cuda.current_device()
     key = (device.type, idx, stream_ptr(torch.device(device.type, idx)))
     buf = _ws_cache.get(key)
     if buf is None or buf.numel() < nbytes:
         buf = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
         _ws_cache[key] = buf
+    _ws_cache.move_to_end(key)
+    while len(_ws_cache) > _WS_CACHE_STREAMS:
+        _ws_cache.popitem(last=False)
     return buf

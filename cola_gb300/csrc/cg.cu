@@ -19,6 +19,7 @@
 //     syncs twice per step, torch_tqdm.py:42 and cg.py:136).
 // Column sums are reduced in a fixed order so every CTA derives bit-identical alpha / beta.
 #include <cooperative_groups.h>
+#include <cuda.h>
 
 #include <cmath>
 #include <mutex>
@@ -692,9 +693,10 @@ static int plan_cg(const colagb_op* A, const colagb_op* P, int64_t k, CgPlan& pl
   return COLAGB_OK;
 }
 
+// Carves the solver's buffers out of ws; fails when an operator's own workspace cannot be sized.
 template <class T>
-static size_t cg_ws(const colagb_op* A, const colagb_op* P, const CgPlan& pl, Bump& ws, CgScalars<T>* out,
-                    T** R, T** Pv, T** AP, T** Z, T** hist_dummy, void** opws, size_t* opws_bytes) {
+static int cg_ws(const colagb_op* A, const colagb_op* P, const CgPlan& pl, Bump& ws, CgScalars<T>* out,
+                 T** R, T** Pv, T** AP, T** Z, T** hist_dummy, void** opws, size_t* opws_bytes) {
   const int64_t n = pl.n, k = pl.k;
   CgScalars<T> s = carve<T>(ws, k, pl.nb > pl.fused_blocks ? pl.nb : pl.fused_blocks);
   *R = ws.take<T>(n * k);
@@ -703,12 +705,12 @@ static size_t cg_ws(const colagb_op* A, const colagb_op* P, const CgPlan& pl, Bu
   *Z = pl.pk == 2 ? ws.take<T>(n * k) : nullptr;
   (void)hist_dummy;
   size_t a_b = 0, p_b = 0;
-  colagb_matmat_workspace_bytes(A, k, &a_b);
-  if (P && pl.pk == 2) colagb_matmat_workspace_bytes(P, k, &p_b);
+  COLAGB_TRY(colagb_matmat_workspace_bytes(A, k, &a_b));
+  if (P && pl.pk == 2) COLAGB_TRY(colagb_matmat_workspace_bytes(P, k, &p_b));
   *opws_bytes = a_b > p_b ? a_b : p_b;
   *opws = ws.take<char>(*opws_bytes > 0 ? *opws_bytes : 1);
   if (out) *out = s;
-  return ws.peak;
+  return COLAGB_OK;
 }
 
 template <class T>
@@ -893,7 +895,7 @@ static int cg_solve_t(const colagb_op* A, const colagb_op* P, const void* Bv, in
   T *R, *Pv, *AP, *Z, *hd;
   void* opws;
   size_t opws_b;
-  cg_ws<T>(A, P, pl, ws, &s, &R, &Pv, &AP, &Z, &hd, &opws, &opws_b);
+  COLAGB_TRY(cg_ws<T>(A, P, pl, ws, &s, &R, &Pv, &AP, &Z, &hd, &opws, &opws_b));
   if (ws.overflow() || workspace == nullptr)
     return fail(COLAGB_ERR_WORKSPACE, "colagb_cg_solve: workspace too small (need " + std::to_string(ws.peak) + ")");
   const T* B = static_cast<const T*>(Bv);
@@ -931,10 +933,10 @@ extern "C" int colagb_cg_workspace_bytes(const colagb_op* A, const colagb_op* P,
   size_t ob;
   if (A->compute_dtype == COLAGB_F64) {
     double *R, *Pv, *AP, *Z, *h;
-    cg_ws<double>(A, P, pl, ws, nullptr, &R, &Pv, &AP, &Z, &h, &opws, &ob);
+    COLAGB_TRY(cg_ws<double>(A, P, pl, ws, nullptr, &R, &Pv, &AP, &Z, &h, &opws, &ob));
   } else {
     float *R, *Pv, *AP, *Z, *h;
-    cg_ws<float>(A, P, pl, ws, nullptr, &R, &Pv, &AP, &Z, &h, &opws, &ob);
+    COLAGB_TRY(cg_ws<float>(A, P, pl, ws, nullptr, &R, &Pv, &AP, &Z, &h, &opws, &ob));
   }
   *bytes = ws.peak;
   return COLAGB_OK;
@@ -963,20 +965,63 @@ namespace colagb {
 constexpr size_t kNoAllocScratchBytes = (size_t)8 << 20;  // 8 MiB
 static __device__ __align__(256) unsigned char g_cg_noalloc_scratch[kNoAllocScratchBytes];
 
-// Device address of the scratch array on the current device, looked up once per device.
+// The array's device address belongs to a CUDA context, not to a device: a caller that pushes its
+// own driver context, or a cudaDeviceReset, makes the runtime load the library's module again at
+// another address.  So the address is looked up once per context (keyed on the driver's unique
+// context id, reached through the runtime's driver entry points without linking libcuda) and cached.
+using PfnCtxGetCurrent = CUresult (*)(CUcontext*);
+using PfnCtxGetId = CUresult (*)(CUcontext, unsigned long long*);
+
+// Unique id of the calling thread's current context; 0 when there is none yet or it cannot be read.
+static unsigned long long current_context_id() {
+  static PfnCtxGetCurrent get_cur = nullptr;
+  static PfnCtxGetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_cur = reinterpret_cast<PfnCtxGetCurrent>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<PfnCtxGetId>(f);
+    cudaGetLastError();
+  });
+  if (!get_cur || !get_id) return 0;
+  CUcontext ctx = nullptr;
+  if (get_cur(&ctx) != CUDA_SUCCESS || ctx == nullptr) return 0;
+  unsigned long long id = 0;
+  if (get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
+
+// Device address of the scratch array in the calling thread's current context.
 static int noalloc_scratch(void** out) {
   static std::mutex mu;
-  static std::vector<void*> addr;
-  int dev = 0;
-  COLAGB_CUDA(cudaGetDevice(&dev));
-  std::lock_guard<std::mutex> lk(mu);
-  if ((int)addr.size() <= dev) addr.resize(dev + 1, nullptr);
-  if (addr[dev] == nullptr) {
-    void* p = nullptr;
-    COLAGB_CUDA(cudaGetSymbolAddress(&p, g_cg_noalloc_scratch));
-    addr[dev] = p;
+  static std::vector<std::pair<unsigned long long, void*>> addr;  // (context id, address)
+  unsigned long long id = current_context_id();
+  if (id == 0) {
+    // no context current yet (or no driver entry points): the lookup itself makes the device's
+    // primary context current; cache under that context when its id can be read
+    COLAGB_CUDA(cudaGetSymbolAddress(out, g_cg_noalloc_scratch));
+    id = current_context_id();
+    if (id == 0) return COLAGB_OK;
+    std::lock_guard<std::mutex> lk(mu);
+    addr.emplace_back(id, *out);
+    return COLAGB_OK;
   }
-  *out = addr[dev];
+  std::lock_guard<std::mutex> lk(mu);
+  for (const auto& e : addr)
+    if (e.first == id) {
+      *out = e.second;
+      return COLAGB_OK;
+    }
+  void* p = nullptr;
+  COLAGB_CUDA(cudaGetSymbolAddress(&p, g_cg_noalloc_scratch));
+  addr.emplace_back(id, p);
+  *out = p;
   return COLAGB_OK;
 }
 }  // namespace colagb

@@ -146,7 +146,7 @@ def onchip_schedule_info(n: int, halo: int) -> dict:
 def solve_batched(A: BatchedCSR, B: torch.Tensor, precond: str = "jacobi", tol: float = 1e-8,
                   inner_tol: float | None = None, max_sweeps: int = 200, max_inner_iters: int = 50000,
                   fsai: tuple | None = None, fallback: bool = True, mode: str = "reliable",
-                  schedule: str = "auto", wait: bool = True):
+                  schedule: str = "auto", wait: bool = True, spin_limit: int = 0):
     """Solve A_s x_s = b_s for every system s to |b_s - A_s x_s| / |b_s| <= tol (FP64 residual).
 
     Args:
@@ -167,6 +167,8 @@ def solve_batched(A: BatchedCSR, B: torch.Tensor, precond: str = "jacobi", tol: 
             schedules); X and the per-system tensors of info are then ready in stream order and
             info["sweeps"] is None.  The scratch buffer is per stream, so solves on other streams may
             run meanwhile.
+        spin_limit: naps a CTA of the "grid" schedule may take in one grid barrier before the solve
+            gives up with COLAGB_ERR_TIMEOUT (a ColagbError); 0 keeps the library default (seconds).
     Returns (X (S, n) float64, info) with per-system iterations, status and FP64 relative residuals.
     """
     _capi.require_cuda(A.values, B)
@@ -202,7 +204,7 @@ def solve_batched(A: BatchedCSR, B: torch.Tensor, precond: str = "jacobi", tol: 
         inner_tol = 0.01 if mode == "reliable" else 1e-4
     prm = _capi.IrParams(tol=float(tol), inner_tol=float(inner_tol), max_sweeps=int(max_sweeps),
                          max_inner_iters=int(max_inner_iters), preconditioner=pk, fallback=1 if fallback else 0,
-                         spin_limit=0, mode=_capi.IR_RELIABLE if mode == "reliable" else _capi.IR_RESTART,
+                         spin_limit=int(spin_limit), mode=_capi.IR_RELIABLE if mode == "reliable" else _capi.IR_RESTART,
                          schedule=_SCHED[schedule], no_wait=0 if wait else 1)
     iters = torch.zeros(S, dtype=torch.int32, device=dev)
     status = torch.zeros(S, dtype=torch.int32, device=dev)

@@ -138,10 +138,14 @@ int colagb_cg_solve(const colagb_op* A, const colagb_op* P, const void* B, int64
  * no workspace: its scratch is one fixed 8 MiB device array inside this library (every GPU that loads
  * the library keeps it until the process exits).  Problems whose colagb_cg_workspace_bytes exceeds
  * 8 MiB (roughly n*k above 600,000 in FP32 or 300,000 in FP64) are rejected with COLAGB_ERR_INVALID.
- * The first call on a device looks up the array's device address; make that first call before any
- * stream capture.  All calls share the array: calls whose GPU work overlaps (other streams, other
- * threads) race and corrupt each other's results.  This entry point has no counterpart in the
- * reference; otherwise it behaves exactly like colagb_cg_solve. */
+ * The array's device address belongs to the CUDA context current on the calling thread (the
+ * device's primary context for runtime-API callers; the caller's own context if it pushed one).  The
+ * first call in each context looks that address up and caches it under the context's unique id, so
+ * a new context (a pushed driver context, or the primary context re-created after cudaDeviceReset)
+ * gets its own lookup; make the first call in a context before any stream capture.  All calls in a
+ * context share the array: calls whose GPU work overlaps (other streams, other threads) race and
+ * corrupt each other's results.  This entry point has no counterpart in the reference; otherwise it
+ * behaves exactly like colagb_cg_solve. */
 int colagb_cg_solve_noalloc(const colagb_op* A, const colagb_op* P, const void* B, int64_t ldb, void* X,
                             int64_t ldx, int64_t k, const colagb_cg_params* params, void* residual_history,
                             colagb_cg_result* result, void* stream);
@@ -361,6 +365,16 @@ int colagb_fsai_rq_loss_grad(const float* stencil, const float* net_out, const f
 /* Adam update of count parameters (bias-corrected, step >= 1) */
 int colagb_adam_step(float* param, const float* grad, float* m1, float* m2, int64_t count, float lr, float beta1,
                      float beta2, float eps, int32_t step, void* stream);
+
+/* ======================================================================== *
+ *  Measurement                                                             *
+ * ======================================================================== */
+/* No counterpart in the reference: the roofline denominator for kernels whose operands L2 serves.
+ * Streams `bytes` (16-byte aligned) of `buffer` `reps` times with 128-bit loads that bypass L1 and
+ * reduces them; sink (device, 1 float) is written only for impossible data.  Time two launches with
+ * different reps on the caller's stream: (bytes * reps difference) / time difference is the
+ * L2 -> SM read bandwidth when the buffer fits in L2, the HBM read bandwidth when it does not. */
+int colagb_read_bandwidth_probe(const void* buffer, size_t bytes, int32_t reps, void* sink, void* stream);
 
 #ifdef __cplusplus
 }

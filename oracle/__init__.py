@@ -6,8 +6,8 @@ tests/, by __graft_entry__.smoke() and by bench.py's CPU-baseline leg as the che
 reference timing, never by the cola_gb300 package.
 
 Parity pinning: every function here is checked against golden vectors produced by running the
-reference itself (tests/golden/make_golden.py imports /root/reference through test-only stand-ins
-for its two missing dependencies) and against the reference test suite's known-answer cases.
+reference itself (tests/golden/make_golden.py imports the reference's source tree through test-only
+stand-ins for its two missing dependencies) and against the reference test suite's known-answer cases.
 """
 from .cg import run_batched_cg, cg_solve  # noqa: F401
 from .lanczos import lanczos, lanczos_eigs, lanczos_unary_matmat, slq_estimate, hutchinson_diag  # noqa: F401

@@ -2,7 +2,7 @@
 
 Run in a container that holds the reference source (it is not needed anywhere else):
 
-    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [/root/reference]
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py <path of the reference source tree>
 
 The reference needs `plum` and `optree`, which this image lacks; the test-only stand-ins in
 tests/golden/_shims provide the API surface CoLA uses.  Every case stores its inputs and the
@@ -17,7 +17,9 @@ from pathlib import Path
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
-REF = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+if len(sys.argv) < 2 or not (Path(sys.argv[1]) / "cola").is_dir():
+    sys.exit("usage: make_golden.py <path of the reference source tree (the directory holding cola/)>")
+REF = Path(sys.argv[1])
 sys.path[:0] = [str(HERE / "_shims"), str(REF)]
 
 import torch  # noqa: E402
