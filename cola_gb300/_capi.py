@@ -26,6 +26,7 @@ ERR_WORKSPACE = 5
 F32, F64, BF16 = 0, 1, 2
 
 OP_DENSE, OP_CSR, OP_DIAG, OP_SCALAR, OP_IDENTITY, OP_SUM, OP_PRODUCT, OP_KRON, OP_BLOCKDIAG = range(1, 10)
+KRON_PRECISION = {"auto": 0, "fp32": 1, "bf16": 2, "bf16x3": 3}
 
 PREC_NONE, PREC_JACOBI, PREC_FSAI = 0, 1, 2
 IR_RELIABLE, IR_RESTART = 0, 1
@@ -43,6 +44,7 @@ class OpNode(C.Structure):
         ("data", C.c_void_p), ("ld", C.c_int64), ("indptr", C.c_void_p), ("indices", C.c_void_p),
         ("nnz", C.c_int64), ("scalar", C.c_double), ("children", C.POINTER(C.c_int32)),
         ("num_children", C.c_int32), ("multiplicities", C.POINTER(C.c_int64)),
+        ("precision", C.c_int32), ("reserved", C.c_int32),
     ]
 
 

@@ -14,6 +14,7 @@
 // Kronecker factors are applied as strided-batched contractions on the (pre, c_i, post*k) view,
 // so no moveaxis copy is materialised.
 #include <mutex>
+#include <type_traits>
 #include <string>
 #include <vector>
 
@@ -351,6 +352,21 @@ struct LeafLaunch {
 // --------------------------------------------------------------------------------------------
 // executor
 
+// Whether factor f of a Kronecker node is contracted on the tensor cores (FP32 compute only; see
+// COLAGB_KRON_* in colagb.h), and with the three-product split.  pre / q as in the KRON branch below.
+template <class T>
+static bool kron_on_tensor_cores(int32_t precision, const colagb_op_node& f, int64_t pre, int64_t q, int64_t r,
+                                 int64_t c, bool* split) {
+  if (!std::is_same<T, float>::value || precision == COLAGB_KRON_FP32) return false;
+  if (f.kind != COLAGB_OP_DENSE || (f.dtype != COLAGB_F32 && f.dtype != COLAGB_BF16)) return false;
+  if (q > 1 && q < 32) return false;  // few columns per block: the axis-swapped SIMT form
+  const int64_t batch = q > 1 ? pre : 1, M = q > 1 ? q : pre;
+  if (!tc_contract_supported(batch, M, r, c)) return false;
+  if (precision == COLAGB_KRON_AUTO && (double)pre * (double)q * (double)r * (double)c < (double)(1 << 26)) return false;
+  *split = precision != COLAGB_KRON_BF16;
+  return true;
+}
+
 template <class T>
 int op_apply(const colagb_op* op, int node, const T* X, int64_t ldx, int64_t bsx, T* Y, int64_t ldy, int64_t bsy,
              int64_t k, int64_t batch, T alpha, T beta, Bump& ws, const int* skip, cudaStream_t st) {
@@ -442,7 +458,23 @@ int op_apply(const colagb_op* op, int node, const T* X, int64_t ldx, int64_t bsx
           const bool direct = last && ldy == k;
           T* out = direct ? (Y + b * bsy) : buf[which];
           const int64_t q = post * k;
-          if (q <= 8 && pre >= 16 && pre <= 65535 && c[i] <= 65535) {
+          bool split = true;
+          if (kron_on_tensor_cores<T>(nd.precision, op->nodes[ch[i]], pre, q, r[i], c[i], &split)) {
+            // out[p, r, q] on the tensor cores: the operand (p, c, q) transposed per p into K-major
+            // BF16 when q > 1, taken row by row when q == 1
+            const colagb_op_node& f = op->nodes[ch[i]];
+            const float a_f = direct ? (float)alpha : 1.f, b_f = direct ? (float)beta : 0.f;
+            float* o = reinterpret_cast<float*>(out);
+            const float* a_in = reinterpret_cast<const float*>(in);
+            const size_t tmark = ws.used;
+            if (q > 1)
+              COLAGB_TRY(tc_contract(a_in, true, pre, q, c[i], f.data, f.dtype, f.ld, r[i], o, r[i] * q, 1, q, a_f, b_f,
+                                     split, ws, skip, st));
+            else
+              COLAGB_TRY(tc_contract(a_in, false, 1, pre, c[i], f.data, f.dtype, f.ld, r[i], o, 0, r[i], 1, a_f, b_f,
+                                     split, ws, skip, st));
+            ws.release(tmark);
+          } else if (q <= 8 && pre >= 16 && pre <= 65535 && c[i] <= 65535) {
             // `pre` products of M_i with (c_i x q) blocks re-read M_i `pre` times; with the first two
             // axes swapped they are one product M_i @ (c_i x pre*q), then swapped back
             COLAGB_TRY(launch_axpby_b<T>(in, c[i] * q, q, sw[0], q, pre * q, pre, q, c[i], T(1), T(0), skip, st));
@@ -460,9 +492,23 @@ int op_apply(const colagb_op* op, int node, const T* X, int64_t ldx, int64_t bsx
           which ^= 1;
         }
       }
-      if (measuring) {  // children of a Kronecker may need workspace of their own
+      if (measuring) {  // children of a Kronecker may need workspace of their own, and so do the
+                        // tensor-core contractions
         for (int i = 0; i < m; ++i)
           COLAGB_TRY(op_apply<T>(op, ch[i], nullptr, k, 0, nullptr, k, 0, k, 1, T(1), T(0), ws, skip, st));
+        for (int i = 0; i < m; ++i) {
+          int64_t pre = 1, post = 1;
+          for (int j = 0; j < i; ++j) pre *= r[j];
+          for (int j = i + 1; j < m; ++j) post *= c[j];
+          const int64_t q = post * k;
+          bool split = true;
+          if (!kron_on_tensor_cores<T>(nd.precision, op->nodes[ch[i]], pre, q, r[i], c[i], &split)) continue;
+          const colagb_op_node& f = op->nodes[ch[i]];
+          const size_t tmark = ws.used;
+          COLAGB_TRY(tc_contract(nullptr, q > 1, q > 1 ? pre : 1, q > 1 ? q : pre, c[i], f.data, f.dtype, f.ld, r[i],
+                                 nullptr, 0, 1, 1, 1.f, 0.f, split, ws, skip, st));
+          ws.release(tmark);
+        }
       }
       ws.release(mark);
       return COLAGB_OK;

@@ -37,4 +37,14 @@ struct FusedForm {
 };
 FusedForm fused_form(const colagb_op* op);
 
+// Tensor-core factor contraction of the Kronecker matvec (tc_gemm.cu):
+// out[b * s_b + m * s_m + n * s_n] = alpha * sum_k A_b[m, k] B[n, k] + beta * out[...], with
+// A_b[m, k] = a_src[b * K * M + k * M + m] (transposed_a) or A[m, k] = a_src[m * K + k] (batch 1),
+// B[n, k] = b_src[n * ldb + k].  BF16 products with FP32 accumulation; `split` adds the lo terms of
+// the three-product BF16 split.  Scratch is taken from ws (sizes only when ws.measure).
+bool tc_contract_supported(int64_t batch, int64_t M, int64_t N, int64_t K);
+int tc_contract(const float* a_src, bool transposed_a, int64_t batch, int64_t M, int64_t K, const void* b_src,
+                int32_t b_dtype, int64_t ldb, int64_t N, float* out, int64_t s_b, int64_t s_m, int64_t s_n,
+                float alpha, float beta, bool split, Bump& ws, const int* skip, cudaStream_t st);
+
 }  // namespace colagb

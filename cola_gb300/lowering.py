@@ -111,11 +111,15 @@ class Lowered:
             kids = [self._lower(M) for M in Ms]
             ptr, nk = self._children(kids)
             return self._add(kind=_capi.OP_PRODUCT, rows=rows, cols=cols, children=ptr, num_children=nk)
-        if isinstance(op, (O.Sum, O.Kronecker)):
+        if isinstance(op, O.Sum):
             kids = [self._lower(M) for M in op.Ms]
             ptr, nk = self._children(kids)
-            kind = _capi.OP_SUM if isinstance(op, O.Sum) else _capi.OP_KRON
-            return self._add(kind=kind, rows=rows, cols=cols, children=ptr, num_children=nk)
+            return self._add(kind=_capi.OP_SUM, rows=rows, cols=cols, children=ptr, num_children=nk)
+        if isinstance(op, O.Kronecker):
+            kids = [self._lower(M) for M in op.Ms]
+            ptr, nk = self._children(kids)
+            return self._add(kind=_capi.OP_KRON, rows=rows, cols=cols, children=ptr, num_children=nk,
+                             precision=_capi.KRON_PRECISION[op.precision])
         if isinstance(op, O.BlockDiag):
             kids = [self._lower(M) for M in op.Ms]
             ptr, nk = self._children(kids)

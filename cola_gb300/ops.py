@@ -274,9 +274,17 @@ class Sum(LinearOperator):
 
 
 class Kronecker(LinearOperator):
-    """Kronecker product M1 (x) M2 (x) ... (operators.py:199-228)."""
+    """Kronecker product M1 (x) M2 (x) ... (operators.py:199-228).
 
-    def __init__(self, *Ms):
+    ``precision`` (keyword only; FP32 operators) selects the arithmetic of the factor contractions:
+    "auto" (default) runs large contractions (>= 2^26 multiply-adds, Dense factors) on the tensor
+    cores with the three-product BF16 split and the rest in FP32; "bf16x3", "bf16" and "fp32" force
+    one kind.  FP64 operators always contract in FP64."""
+
+    def __init__(self, *Ms, precision: str = "auto"):
+        if precision not in ("auto", "fp32", "bf16", "bf16x3"):
+            raise ValueError(f"unknown Kronecker precision {precision!r}")
+        self.precision = precision
         self.Ms = tuple(_lazify(M) for M in Ms)
         self.device = _find_device(self.Ms)
         shape = (reduce(lambda a, b: a * b, [M.shape[-2] for M in self.Ms]),

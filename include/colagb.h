@@ -82,7 +82,19 @@ typedef struct colagb_op_node {
   const int32_t* children; /* host: indices of child nodes in the node array */
   int32_t num_children;
   const int64_t* multiplicities; /* host, BLOCKDIAG: one per child, NULL = all 1 */
+  int32_t precision;       /* KRON: arithmetic of the factor contractions, COLAGB_KRON_* below */
+  int32_t reserved;
 } colagb_op_node;
+
+/* Kronecker contraction arithmetic (FP32 compute type; FP64 operators always use FP64 arithmetic).
+ * AUTO: tensor cores with the three-product BF16 split (BF16X3) for contractions of at least 2^26
+ * multiply-adds whose factor is Dense and has a multiple-of-8 column count, FP32 SIMT otherwise.
+ * BF16: one BF16 product per term (FP32 accumulation).  BF16X3: hi = bf16(v), lo = bf16(v - hi);
+ * hi.hi + hi.lo + lo.hi in FP32 (about 2^-16 relative per product).  FP32: FP32 SIMT only. */
+#define COLAGB_KRON_AUTO 0
+#define COLAGB_KRON_FP32 1
+#define COLAGB_KRON_BF16 2
+#define COLAGB_KRON_BF16X3 3
 
 typedef struct colagb_op colagb_op; /* opaque */
 
