@@ -642,6 +642,8 @@ struct BatchedWs {
   int* nrep;
   float* onchip;
   size_t onchip_bytes;
+  __nv_bfloat16* v16;  // BF16 inner matvec: off-diagonal values and the consistent diagonal
+  float* dg16;
 };
 
 size_t onchip_workspace_floats(int64_t n, bool fsai);
@@ -667,19 +669,26 @@ static BatchedWs carve_batched(Bump& ws, const colagb_batched_csr& A, const cola
   w.bar = ws.take<unsigned int>(8);
   w.summary = ws.take<int>(8);
   w.nrep = ws.take<int>(S);
-  const bool onchip = prm.schedule == COLAGB_SCHED_AUTO || prm.schedule == COLAGB_SCHED_ONCHIP;
+  const bool bf = prm.matvec == COLAGB_MATVEC_BF16;
+  const bool onchip = !bf && (prm.schedule == COLAGB_SCHED_AUTO || prm.schedule == COLAGB_SCHED_ONCHIP);
   const size_t nf = onchip ? onchip_workspace_floats(A.n, fsai) : 0;
   w.onchip = nf ? ws.take<float>(nf) : nullptr;
   w.onchip_bytes = nf * sizeof(float);
+  const int64_t sets = A.shared_values ? 1 : S;
+  w.v16 = bf ? ws.take<__nv_bfloat16>((size_t)(sets * A.nnz)) : nullptr;
+  w.dg16 = bf ? ws.take<float>((size_t)(sets * A.n)) : nullptr;
   return w;
 }
 
 int cluster_pcg_solve(const colagb_batched_csr* A, const double* B, double* X, const colagb_ir_params* prm,
                       int32_t* iters, int32_t* status, double* relres, float* r, float* p, float* ap, float* d,
-                      float* z, float* t, float* dinv, int* nrep, int cluster_size, cudaStream_t st);
+                      float* z, float* t, float* dinv, int* nrep, int cluster_size, __nv_bfloat16* v16,
+                      float* dg16, cudaStream_t st);
 
 // Cluster size for the cluster schedule: 0 = use the cooperative grid kernel.
 static int pick_cluster(const colagb_ir_params& prm, int64_t n) {
+  if (prm.matvec == COLAGB_MATVEC_BF16 && (prm.schedule == COLAGB_SCHED_AUTO || prm.schedule == COLAGB_SCHED_ONCHIP))
+    return n >= 16 * 1024 ? 16 : 8;  // the BF16 inner matvec runs on the cluster schedule
   if (prm.schedule == COLAGB_SCHED_GRID || prm.schedule == COLAGB_SCHED_ONCHIP) return 0;
   if (prm.schedule == COLAGB_SCHED_CLUSTER8) return 8;
   if (prm.schedule == COLAGB_SCHED_CLUSTER16) return 16;
@@ -703,6 +712,10 @@ static int validate_batched(const colagb_batched_csr* A, const colagb_ir_params*
   if (!(prm->tol > 0) || !(prm->inner_tol > 0) || !(prm->inner_tol < 1))
     return fail(COLAGB_ERR_INVALID, "batched CG: need tol > 0 and 0 < inner_tol < 1");
   if (prm->max_sweeps < 0 || prm->max_inner_iters < 0) return fail(COLAGB_ERR_INVALID, "batched CG: negative limits");
+  if (prm->matvec != COLAGB_MATVEC_FP32 && prm->matvec != COLAGB_MATVEC_BF16)
+    return fail(COLAGB_ERR_INVALID, "batched CG: unknown matvec storage");
+  if (prm->matvec == COLAGB_MATVEC_BF16 && (prm->schedule == COLAGB_SCHED_GRID || prm->schedule == COLAGB_SCHED_ONCHIP))
+    return fail(COLAGB_ERR_UNSUPPORTED, "batched CG: the BF16 inner matvec runs on the cluster schedules only");
   if (A->n >= (int64_t)1 << 31 || A->nnz >= (int64_t)1 << 31)
     return fail(COLAGB_ERR_INVALID, "batched CG: n and nnz must fit int32 indices");
   return COLAGB_OK;
@@ -743,7 +756,8 @@ extern "C" int colagb_cg_batched_csr_solve(const colagb_batched_csr* A, const do
     return fail(COLAGB_ERR_WORKSPACE, "batched CG: workspace too small (need " + std::to_string(ws.peak) + ")");
   cudaStream_t st = as_stream(stream);
   const int csize = pick_cluster(*params, A->n);
-  const bool try_onchip = params->schedule == COLAGB_SCHED_AUTO || params->schedule == COLAGB_SCHED_ONCHIP;
+  const bool try_onchip = params->matvec == COLAGB_MATVEC_FP32 &&
+                          (params->schedule == COLAGB_SCHED_AUTO || params->schedule == COLAGB_SCHED_ONCHIP);
   for (int64_t s0 = 0; s0 < S_all; s0 += kMaxBatch) {
     const int64_t S = (S_all - s0) < kMaxBatch ? (S_all - s0) : kMaxBatch;
     colagb_batched_csr sub = *A;
@@ -769,7 +783,7 @@ extern "C" int colagb_cg_batched_csr_solve(const colagb_batched_csr* A, const do
                                      per_system_iters ? per_system_iters + s0 : nullptr,
                                      per_system_status ? per_system_status + s0 : nullptr,
                                      relres ? relres + s0 : nullptr, w.r, w.p, w.ap, w.d, w.z, w.t, w.dinv, w.nrep,
-                                     csize, st));
+                                     csize, w.v16, w.dg16, st));
       if (params->no_wait) {
         result->sweeps = -1;
         continue;

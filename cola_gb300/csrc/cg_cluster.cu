@@ -14,6 +14,7 @@
 //     in the 126 MB L2 across iterations.
 #include <cooperative_groups.h>
 
+#include <algorithm>
 #include <string>
 
 #include "cluster.cuh"
@@ -30,6 +31,11 @@ struct ClusterArgs {
   const int32_t* __restrict__ indptr;
   const int32_t* __restrict__ indices;
   const float* __restrict__ vals;
+  // BF16 inner matvec: off-diagonal values in BF16 (diagonal slots zero) and the consistent FP32
+  // diagonal, one array per value set (stride vstride / n, 0 for shared values)
+  const __nv_bfloat16* __restrict__ v16;
+  const float* __restrict__ dg16;
+  int64_t dstride;
   int64_t g_nnz;
   const int32_t* g_indptr;
   const int32_t* g_indices;
@@ -61,7 +67,44 @@ __device__ __forceinline__ float row_dot_f(const ClusterArgs& a, const float* __
   return acc;
 }
 
-template <int CL>
+// BF16 form: A' x at row i = d'_i x_i + sum_j bf16(a_ij) x_j (the diagonal slot of v16 holds zero).
+__device__ __forceinline__ float row_dot_b(const ClusterArgs& a, const __nv_bfloat16* __restrict__ v16,
+                                          const float* __restrict__ dg, const float* x, int64_t i) {
+  const int32_t b = __ldg(a.indptr + i), e = __ldg(a.indptr + i + 1);
+  float acc = dg[i] * x[i];
+#pragma unroll
+  for (int k = 0; k < 6; ++k)
+    if (b + k < e) acc += __bfloat162float(v16[b + k]) * x[__ldg(a.indices + b + k)];
+  for (int32_t j = b + 6; j < e; ++j) acc += __bfloat162float(v16[j]) * x[__ldg(a.indices + j)];
+  return acc;
+}
+
+// One value set per block row: v16 / dg16 from FP32 CSR values (see COLAGB_MATVEC_BF16).
+__global__ void k_bf16_consistent(const int32_t* __restrict__ indptr, const int32_t* __restrict__ indices,
+                                  const float* __restrict__ vals, int64_t n, int64_t nnz,
+                                  __nv_bfloat16* __restrict__ v16, float* __restrict__ dg16) {
+  const int64_t s = blockIdx.y;
+  vals += s * nnz;
+  v16 += s * nnz;
+  dg16 += s * n;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double d = 0.0, corr = 0.0;
+    for (int32_t j = indptr[i]; j < indptr[i + 1]; ++j) {
+      const float v = vals[j];
+      if (indices[j] == i) {
+        d += (double)v;
+        v16[j] = __float2bfloat16_rn(0.f);
+      } else {
+        const __nv_bfloat16 h = __float2bfloat16_rn(v);
+        v16[j] = h;
+        corr += (double)__bfloat162float(h) - (double)v;
+      }
+    }
+    dg16[i] = (float)(d - corr);
+  }
+}
+
+template <int CL, bool BF>
 __global__ void __launch_bounds__(kCT, 1) k_cluster_pcg(const __grid_constant__ ClusterArgs a) {
   cg::cluster_group cl = cg::this_cluster();
   const int rank = (int)cl.block_rank();
@@ -82,6 +125,8 @@ __global__ void __launch_bounds__(kCT, 1) k_cluster_pcg(const __grid_constant__ 
   const int64_t i1 = (rank + 1) * rows < n ? (rank + 1) * rows : n;
   const int64_t so = s * n;
   const float* __restrict__ vals = a.vals + s * a.vstride;
+  const __nv_bfloat16* __restrict__ v16 = BF ? a.v16 + s * a.vstride : nullptr;
+  const float* __restrict__ dg16 = BF ? a.dg16 + s * a.dstride : nullptr;
   // vectors written by several CTAs of the cluster: plain pointers (see row_dot_f)
   float* r = a.r + so;
   float* p = a.p + so;
@@ -185,8 +230,14 @@ __global__ void __launch_bounds__(kCT, 1) k_cluster_pcg(const __grid_constant__ 
     float qaf = 0.f;
     for (int64_t i = i0 + tid; i < i1; i += 2 * kCT) {
       const int64_t i2 = i + kCT;
-      const float y0 = row_dot_f(a, vals, p, i);
-      const float y1 = i2 < i1 ? row_dot_f(a, vals, p, i2) : 0.f;
+      float y0, y1;
+      if constexpr (BF) {
+        y0 = row_dot_b(a, v16, dg16, p, i);
+        y1 = i2 < i1 ? row_dot_b(a, v16, dg16, p, i2) : 0.f;
+      } else {
+        y0 = row_dot_f(a, vals, p, i);
+        y1 = i2 < i1 ? row_dot_f(a, vals, p, i2) : 0.f;
+      }
       ap[i] = y0;
       float acc = p[i] * y0;
       if (i2 < i1) {
@@ -318,7 +369,7 @@ __global__ void __launch_bounds__(kCT, 1) k_cluster_pcg(const __grid_constant__ 
   cl.sync();  // no CTA leaves while another may still read its shared memory
 }
 
-template <int CL>
+template <int CL, bool BF>
 static int launch_cluster(const ClusterArgs& a, cudaStream_t st) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(a.S * CL));
@@ -332,21 +383,34 @@ static int launch_cluster(const ClusterArgs& a, cudaStream_t st) {
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  if (CL > 8) COLAGB_CUDA(cudaFuncSetAttribute(k_cluster_pcg<CL>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  if (CL > 8)
+    COLAGB_CUDA(cudaFuncSetAttribute(k_cluster_pcg<CL, BF>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
   int nclusters = 0;
-  if (cudaOccupancyMaxActiveClusters(&nclusters, k_cluster_pcg<CL>, &cfg) != cudaSuccess || nclusters < 1) {
+  if (cudaOccupancyMaxActiveClusters(&nclusters, k_cluster_pcg<CL, BF>, &cfg) != cudaSuccess || nclusters < 1) {
     cudaGetLastError();
     return fail(COLAGB_ERR_UNSUPPORTED, "cluster PCG: cluster size not schedulable");
   }
-  COLAGB_CUDA(cudaLaunchKernelEx(&cfg, k_cluster_pcg<CL>, a));
+  COLAGB_CUDA(cudaLaunchKernelEx(&cfg, k_cluster_pcg<CL, BF>, a));
   return COLAGB_OK;
 }
 
 // Called by colagb_cg_batched_csr_solve for the cluster schedule.
 int cluster_pcg_solve(const colagb_batched_csr* A, const double* B, double* X, const colagb_ir_params* prm,
                       int32_t* iters, int32_t* status, double* relres, float* r, float* p, float* ap, float* d,
-                      float* z, float* t, float* dinv, int* nrep, int cluster_size, cudaStream_t st) {
+                      float* z, float* t, float* dinv, int* nrep, int cluster_size, __nv_bfloat16* v16,
+                      float* dg16, cudaStream_t st) {
   ClusterArgs a;
+  const bool bf = prm->matvec == COLAGB_MATVEC_BF16;
+  a.v16 = v16;
+  a.dg16 = dg16;
+  a.dstride = A->shared_values ? 0 : A->n;
+  if (bf) {
+    const int64_t sets = A->shared_values ? 1 : A->num_systems;
+    if (!v16 || !dg16) return fail(COLAGB_ERR_INVALID, "cluster PCG: BF16 matvec without its workspace");
+    dim3 grid((unsigned)std::min<int64_t>(ceil_div(A->n, 256), (int64_t)num_sms() * 4), (unsigned)sets);
+    k_bf16_consistent<<<grid, 256, 0, st>>>(A->indptr, A->indices, A->values, A->n, A->nnz, v16, dg16);
+    COLAGB_CUDA(cudaGetLastError());
+  }
   a.n = A->n;
   a.nnz = A->nnz;
   a.S = A->num_systems;
@@ -375,8 +439,8 @@ int cluster_pcg_solve(const colagb_batched_csr* A, const double* B, double* X, c
   a.prec_kind = prm->preconditioner;
   a.fallback = prm->fallback;
   a.mode = prm->mode;
-  if (cluster_size == 16) return launch_cluster<16>(a, st);
-  return launch_cluster<8>(a, st);
+  if (bf) return cluster_size == 16 ? launch_cluster<16, true>(a, st) : launch_cluster<8, true>(a, st);
+  return cluster_size == 16 ? launch_cluster<16, false>(a, st) : launch_cluster<8, false>(a, st);
 }
 
 }  // namespace colagb

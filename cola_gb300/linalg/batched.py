@@ -146,7 +146,7 @@ def onchip_schedule_info(n: int, halo: int) -> dict:
 def solve_batched(A: BatchedCSR, B: torch.Tensor, precond: str = "jacobi", tol: float = 1e-8,
                   inner_tol: float | None = None, max_sweeps: int = 200, max_inner_iters: int = 50000,
                   fsai: tuple | None = None, fallback: bool = True, mode: str = "reliable",
-                  schedule: str = "auto", wait: bool = True, spin_limit: int = 0):
+                  schedule: str = "auto", wait: bool = True, spin_limit: int = 0, matvec: str = "fp32"):
     """Solve A_s x_s = b_s for every system s to |b_s - A_s x_s| / |b_s| <= tol (FP64 residual).
 
     Args:
@@ -169,6 +169,10 @@ def solve_batched(A: BatchedCSR, B: torch.Tensor, precond: str = "jacobi", tol: 
             run meanwhile.
         spin_limit: naps a CTA of the "grid" schedule may take in one grid barrier before the solve
             gives up with COLAGB_ERR_TIMEOUT (a ColagbError); 0 keeps the library default (seconds).
+        matvec: "fp32" -- the inner CG multiplies by the FP32 values; "bf16" -- by BF16 off-diagonal
+            values with an FP32 diagonal made consistent with them (within 2^-9 of A in the energy norm
+            for weighted-Laplacian-type operators), on the cluster schedules; the FP64 residual
+            replacements always use the FP32 values.
     Returns (X (S, n) float64, info) with per-system iterations, status and FP64 relative residuals.
     """
     _capi.require_cuda(A.values, B)
@@ -205,7 +209,8 @@ def solve_batched(A: BatchedCSR, B: torch.Tensor, precond: str = "jacobi", tol: 
     prm = _capi.IrParams(tol=float(tol), inner_tol=float(inner_tol), max_sweeps=int(max_sweeps),
                          max_inner_iters=int(max_inner_iters), preconditioner=pk, fallback=1 if fallback else 0,
                          spin_limit=int(spin_limit), mode=_capi.IR_RELIABLE if mode == "reliable" else _capi.IR_RESTART,
-                         schedule=_SCHED[schedule], no_wait=0 if wait else 1)
+                         schedule=_SCHED[schedule], no_wait=0 if wait else 1,
+                         matvec={"fp32": _capi.MATVEC_FP32, "bf16": _capi.MATVEC_BF16}[matvec])
     iters = torch.zeros(S, dtype=torch.int32, device=dev)
     status = torch.zeros(S, dtype=torch.int32, device=dev)
     relres = torch.zeros(S, dtype=torch.float64, device=dev)

@@ -213,7 +213,18 @@ typedef struct colagb_ir_params {
                             (per-system outputs valid when the stream gets there, result->sweeps
                             = -1); 0: wait and report the largest replacement count.  The grid
                             schedule always waits (it reads its barrier-timeout flag). */
+  int32_t matvec;        /* COLAGB_MATVEC_*: storage of A in the inner FP32 CG's matvec */
 } colagb_ir_params;
+
+/* Inner matvec storage.  FP32: the CSR values as given.  BF16 (cluster schedules only; AUTO then
+ * picks the cluster schedule): off-diagonal values rounded to BF16 and a separate FP32 diagonal
+ * d'_i = a_ii - sum_j (bf16(a_ij) - a_ij), so that A' - A = -1/2 sum_ij delta_ij (e_i - e_j)(e_i - e_j)^T.
+ * For a weighted-Laplacian-type operator (off-diagonals <= 0, diagonal >= the row's off-diagonal sum)
+ * this keeps A' within 2^-9 of A in the energy norm: |x^T (A' - A) x| <= 2^-9 x^T A x, whatever the
+ * condition number, so the FP64 residual replacements converge.  The FP64 residual b - A x always
+ * uses the FP32 values.  6 bytes per nonzero + 4 per row instead of 8 per nonzero. */
+#define COLAGB_MATVEC_FP32 0
+#define COLAGB_MATVEC_BF16 1
 
 #define COLAGB_SCHED_AUTO 0     /* on-chip when the pattern allows it, else a cluster per system */
 #define COLAGB_SCHED_GRID 1     /* one cooperative grid advancing every system together */

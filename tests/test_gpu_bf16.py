@@ -1,0 +1,52 @@
+"""The batched solver's BF16 inner matvec (COLAGB_MATVEC_BF16): off-diagonal values in BF16 with an FP32
+diagonal made consistent with them, inside FP64 residual replacement.  Both storages must reach the
+same FP64 true residual and the same solution (within 1e-6 relative, the benchmark's solution
+tolerance), on 2-D and 3-D variable-coefficient diffusion families with and without a Jacobi
+preconditioner; the unsupported schedules are refused."""
+import pytest
+import torch
+
+from cola_gb300.linalg.batched import BatchedCSR, solve_batched
+from cola_gb300.workloads import diffusion_3d, diffusion_family_2d
+
+pytestmark = pytest.mark.gpu
+DEV = torch.device("cuda")
+
+
+def rel(a, b):
+    return float((a - b).norm() / b.norm())
+
+
+@pytest.mark.parametrize("prec", ["jacobi", "none"])
+def test_bf16_matvec_2d_family_matches_fp32(prec):
+    fam, B, _, _ = diffusion_family_2d(range(7000, 7006), m=64, device=DEV)
+    X32, i32 = solve_batched(fam, B, precond=prec, tol=1e-10, schedule="cluster8")
+    X16, i16 = solve_batched(fam, B, precond=prec, tol=1e-10, matvec="bf16")
+    assert i16["schedule"] in ("cluster8", "cluster16")
+    assert bool((i16["status"] == 1).all()) and float(i16["relres"].max()) <= 1e-10
+    R = B - fam.matvec(X16)
+    assert float((R.norm(dim=1) / B.norm(dim=1)).max()) <= 1.01e-10
+    assert rel(X16, X32) < 1e-6
+    # BF16 values perturb the inner operator by at most 2^-9 in the energy norm: the step count stays close
+    k16, k32 = i16["iterations"].double(), i32["iterations"].double()
+    assert float((k16 / k32).max()) < 1.5, (k16.tolist(), k32.tolist())
+
+
+def test_bf16_matvec_3d_shared_values_many_rhs():
+    ip, ix, v = diffusion_3d(m=24, seed=1, shift=1e-3, device=DEV)
+    fam = BatchedCSR(ip, ix, v[None, :], shared=True)
+    B = torch.randn(6, fam.n, device=DEV, dtype=torch.float64, generator=torch.Generator("cuda").manual_seed(2))
+    X32, i32 = solve_batched(fam, B, precond="jacobi", tol=1e-9)
+    X16, i16 = solve_batched(fam, B, precond="jacobi", tol=1e-9, matvec="bf16")
+    assert bool((i16["status"] == 1).all())
+    A = torch.sparse_csr_tensor(ip.long(), ix.long(), v.double(), (fam.n, fam.n))
+    R = B.T - A @ X16.T
+    assert float((R.norm(dim=0) / B.norm(dim=1)).max()) <= 1.01e-9
+    assert rel(X16, X32) < 1e-6
+
+
+def test_bf16_matvec_refused_on_grid_and_onchip():
+    fam, B, _, _ = diffusion_family_2d(range(7000, 7002), m=32, device=DEV)
+    for sched in ("grid", "onchip"):
+        with pytest.raises(NotImplementedError, match="cluster schedules"):
+            solve_batched(fam, B, precond="jacobi", schedule=sched, matvec="bf16")
