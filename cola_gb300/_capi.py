@@ -51,11 +51,11 @@ class OpNode(C.Structure):
 
 class CgParams(C.Structure):
     _fields_ = [("tol", C.c_double), ("max_iters", C.c_int32), ("check_every", C.c_int32),
-                ("allow_fused", C.c_int32), ("reserved", C.c_int32), ("spin_limit", C.c_int64)]
+                ("allow_fused", C.c_int32), ("graph", C.c_int32), ("spin_limit", C.c_int64)]
 
 
 class CgResult(C.Structure):
-    _fields_ = [("iterations", C.c_int32), ("fused", C.c_int32), ("status", C.c_int32), ("reserved", C.c_int32)]
+    _fields_ = [("iterations", C.c_int32), ("fused", C.c_int32), ("status", C.c_int32), ("graph", C.c_int32)]
 
 
 class BatchedCsr(C.Structure):

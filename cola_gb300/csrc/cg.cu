@@ -32,6 +32,56 @@
 
 namespace colagb {
 
+// Unique id of the calling thread's current CUDA context (0 when there is none yet or it cannot be
+// read), through the runtime's driver entry points so that the library does not link libcuda.
+using PfnCtxGetCurrent = CUresult (*)(CUcontext*);
+using PfnCtxGetId = CUresult (*)(CUcontext, unsigned long long*);
+
+static unsigned long long current_context_id() {
+  static PfnCtxGetCurrent get_cur = nullptr;
+  static PfnCtxGetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_cur = reinterpret_cast<PfnCtxGetCurrent>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<PfnCtxGetId>(f);
+    cudaGetLastError();
+  });
+  if (!get_cur || !get_id) return 0;
+  CUcontext ctx = nullptr;
+  if (get_cur(&ctx) != CUDA_SUCCESS || ctx == nullptr) return 0;
+  unsigned long long id = 0;
+  if (get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
+
+
+// A private non-blocking stream per CUDA context, used only to capture the generic CG loop's launch
+// block into a graph (capture is not allowed on the legacy default stream callers often use); the
+// graph is then launched on the caller's stream.  Null when no context id can be read.
+static cudaStream_t capture_stream() {
+  static std::mutex mu;
+  static std::vector<std::pair<unsigned long long, cudaStream_t>> streams;
+  const unsigned long long id = current_context_id();
+  if (id == 0) return nullptr;
+  std::lock_guard<std::mutex> lk(mu);
+  for (const auto& e : streams)
+    if (e.first == id) return e.second;
+  cudaStream_t cs = nullptr;
+  if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  streams.emplace_back(id, cs);
+  return cs;
+}
+
 template <class T> struct SmallValue;
 template <> struct SmallValue<float> { static constexpr float v = 1e-40f; };
 template <> struct SmallValue<double> { static constexpr double v = 1e-40; };
@@ -741,41 +791,74 @@ static int run_generic(const colagb_op* A, const colagb_op* P, const CgPlan& pl,
   COLAGB_CUDA(cudaGetLastError());
   int h_done[2] = {0, 0};
   const int every = prm.check_every > 0 ? prm.check_every : 16;
+  // One step of the loop: Ap, alpha, x / r update (+ z = P r and gamma for a general P), p update.
+  // Every kernel reads the device stop flag and does nothing once it is set, so a block of steps may
+  // run past convergence or max_iters (the device counts the steps and enforces max_iters).
+  auto enqueue_steps = [&](cudaStream_t q, int nsteps) -> int {
+    for (int j = 0; j < nsteps; ++j) {
+      Bump w(opws, opws_bytes);
+      COLAGB_TRY(op_apply<T>(A, A->root, Pv, k, 0, AP, k, 0, k, 1, T(1), T(0), w, s.done, q));
+      k_alpha<T><<<nb, 256, 0, q>>>(Pv, AP, n, k, s);
+      switch (pl.pk) {
+        case 0: k_update<T, 0><<<nb, 256, 0, q>>>(X, ldx, R, Pv, AP, dinv, n, k, prm.max_iters, hist, s); break;
+        case 1: k_update<T, 1><<<nb, 256, 0, q>>>(X, ldx, R, Pv, AP, dinv, n, k, prm.max_iters, hist, s); break;
+        default: {
+          k_update<T, 2><<<nb, 256, 0, q>>>(X, ldx, R, Pv, AP, dinv, n, k, prm.max_iters, hist, s);
+          Bump w2(opws, opws_bytes);
+          COLAGB_TRY(op_apply<T>(P, P->root, R, k, 0, Z, k, 0, k, 1, T(1), T(0), w2, s.done, q));
+          k_gamma<T><<<nb, 256, 0, q>>>(R, Z, n, k, prm.max_iters, hist, s);
+        }
+      }
+      // p update runs only when the step did not finish the loop (done flag now set => skip)
+      switch (pl.pk) {
+        case 0: k_pupdate<T, 0><<<eg, 256, 0, q>>>(Pv, R, Z, dinv, n, k, s, s.done); break;
+        case 1: k_pupdate<T, 1><<<eg, 256, 0, q>>>(Pv, R, Z, dinv, n, k, s, s.done); break;
+        default: k_pupdate<T, 2><<<eg, 256, 0, q>>>(Pv, R, Z, dinv, n, k, s, s.done); break;
+      }
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return check_cuda(e, "cg step launch");
+    }
+    return COLAGB_OK;
+  };
+  // The loop's launch block of `every` steps has the same arguments every time (all state lives on
+  // the device), so it is captured once as a CUDA graph and replayed: one launch per block instead of
+  // four to six per step.  Falls back to plain launches when capture is not possible.
+  cudaGraphExec_t exec = nullptr;
+  if (prm.graph == 0 && prm.max_iters >= 2 * every) {
+    cudaStream_t cs = capture_stream();
+    if (cs && cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      const int sb = enqueue_steps(cs, every);
+      cudaGraph_t g = nullptr;
+      const cudaError_t ee = cudaStreamEndCapture(cs, &g);
+      if (sb == COLAGB_OK && ee == cudaSuccess && g) {
+        if (cudaGraphInstantiate(&exec, g, 0) != cudaSuccess) exec = nullptr;
+      }
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();
+    } else {
+      cudaGetLastError();
+    }
+  }
   int launched = 0;
   int status = COLAGB_OK;
   while (true) {
-    for (int j = 0; j < every && launched < prm.max_iters; ++j, ++launched) {
-      Bump w(opws, opws_bytes);
-      status = op_apply<T>(A, A->root, Pv, k, 0, AP, k, 0, k, 1, T(1), T(0), w, s.done, st);
+    if (exec) {
+      cudaError_t e = cudaGraphLaunch(exec, st);
+      if (e != cudaSuccess) { status = check_cuda(e, "cg graph launch"); break; }
+      launched += every;
+    } else {
+      const int nsteps = std::min(every, prm.max_iters - launched);
+      status = enqueue_steps(st, nsteps);
       if (status != COLAGB_OK) break;
-      k_alpha<T><<<nb, 256, 0, st>>>(Pv, AP, n, k, s);
-      switch (pl.pk) {
-        case 0: k_update<T, 0><<<nb, 256, 0, st>>>(X, ldx, R, Pv, AP, dinv, n, k, prm.max_iters, hist, s); break;
-        case 1: k_update<T, 1><<<nb, 256, 0, st>>>(X, ldx, R, Pv, AP, dinv, n, k, prm.max_iters, hist, s); break;
-        default: {
-          k_update<T, 2><<<nb, 256, 0, st>>>(X, ldx, R, Pv, AP, dinv, n, k, prm.max_iters, hist, s);
-          Bump w2(opws, opws_bytes);
-          status = op_apply<T>(P, P->root, R, k, 0, Z, k, 0, k, 1, T(1), T(0), w2, s.done, st);
-          if (status != COLAGB_OK) break;
-          k_gamma<T><<<nb, 256, 0, st>>>(R, Z, n, k, prm.max_iters, hist, s);
-        }
-      }
-      if (status != COLAGB_OK) break;
-      // p update runs only when the step did not finish the loop (done flag now set => skip)
-      switch (pl.pk) {
-        case 0: k_pupdate<T, 0><<<eg, 256, 0, st>>>(Pv, R, Z, dinv, n, k, s, s.done); break;
-        case 1: k_pupdate<T, 1><<<eg, 256, 0, st>>>(Pv, R, Z, dinv, n, k, s, s.done); break;
-        default: k_pupdate<T, 2><<<eg, 256, 0, st>>>(Pv, R, Z, dinv, n, k, s, s.done); break;
-      }
-      cudaError_t e = cudaGetLastError();
-      if (e != cudaSuccess) { status = check_cuda(e, "cg step launch"); break; }
+      launched += nsteps;
     }
-    if (status != COLAGB_OK) break;
     cudaError_t e = cudaMemcpyAsync(h_done, s.done, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) { status = check_cuda(e, "cg poll"); break; }
     if (h_done[0] || launched >= prm.max_iters) break;
   }
+  if (exec) cudaGraphExecDestroy(exec);
+  res->graph = exec != nullptr ? 1 : 0;
   if (status != COLAGB_OK) return status;
   k_scale_x<T><<<eg, 256, 0, st>>>(X, ldx, n, k, s);
   COLAGB_CUDA(cudaGetLastError());
@@ -797,6 +880,7 @@ static int finish_fused(const CgScalars<T>& s, colagb_cg_result* res, cudaStream
   COLAGB_CUDA(cudaStreamSynchronize(st));
   res->iterations = h[0];
   res->fused = 1;
+  res->graph = 0;
   res->status = h[1];
   if (h[1] != 0) return fail(COLAGB_ERR_TIMEOUT, "fused CG: a grid barrier timed out");
   return COLAGB_OK;
@@ -903,6 +987,7 @@ static int cg_solve_t(const colagb_op* A, const colagb_op* P, const void* Bv, in
   T* hist = static_cast<T*>(histv);
   if (pl.n == 0 || k == 0) {
     res->iterations = 0;
+    res->graph = 0;
     res->fused = 0;
     res->status = COLAGB_OK;
     return COLAGB_OK;
@@ -969,34 +1054,6 @@ static __device__ __align__(256) unsigned char g_cg_noalloc_scratch[kNoAllocScra
 // own driver context, or a cudaDeviceReset, makes the runtime load the library's module again at
 // another address.  So the address is looked up once per context (keyed on the driver's unique
 // context id, reached through the runtime's driver entry points without linking libcuda) and cached.
-using PfnCtxGetCurrent = CUresult (*)(CUcontext*);
-using PfnCtxGetId = CUresult (*)(CUcontext, unsigned long long*);
-
-// Unique id of the calling thread's current context; 0 when there is none yet or it cannot be read.
-static unsigned long long current_context_id() {
-  static PfnCtxGetCurrent get_cur = nullptr;
-  static PfnCtxGetId get_id = nullptr;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    void* f = nullptr;
-    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
-    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      get_cur = reinterpret_cast<PfnCtxGetCurrent>(f);
-    f = nullptr;
-    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      get_id = reinterpret_cast<PfnCtxGetId>(f);
-    cudaGetLastError();
-  });
-  if (!get_cur || !get_id) return 0;
-  CUcontext ctx = nullptr;
-  if (get_cur(&ctx) != CUDA_SUCCESS || ctx == nullptr) return 0;
-  unsigned long long id = 0;
-  if (get_id(ctx, &id) != CUDA_SUCCESS) return 0;
-  return id;
-}
-
 // Device address of the scratch array in the calling thread's current context.
 static int noalloc_scratch(void** out) {
   static std::mutex mu;

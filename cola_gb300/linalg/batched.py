@@ -162,7 +162,9 @@ def solve_batched(A: BatchedCSR, B: torch.Tensor, precond: str = "jacobi", tol: 
             the cluster's shared memory and the matrix stored by diagonals (patterns of at most 9
             constant-offset diagonals, n <= 262144); "cluster8" / "cluster16" -- one cluster per system
             on the CSR pattern, vectors in global memory; "grid" -- one cooperative grid that advances
-            every system together; "auto" (default) -- "onchip" when it applies, else a cluster.
+            every system together; "auto" (default) -- "onchip" when it applies, else a cluster;
+            "tuned" -- the fastest applicable schedule for this GPU, pattern, size and preconditioner,
+            measured once and kept in the autotuner's JSON cache (cola_gb300.tuning).
         wait: False returns once the solve is enqueued on the current stream (the on-chip and cluster
             schedules); X and the per-system tensors of info are then ready in stream order and
             info["sweeps"] is None.  The scratch buffer is per stream, so solves on other streams may
@@ -176,6 +178,11 @@ def solve_batched(A: BatchedCSR, B: torch.Tensor, precond: str = "jacobi", tol: 
     Returns (X (S, n) float64, info) with per-system iterations, status and FP64 relative residuals.
     """
     _capi.require_cuda(A.values, B)
+    if schedule == "tuned":
+        from .. import tuning
+        S_t = B.shape[0]
+        key = tuning.key_of(A, S_t, precond, matvec, A.values.device)
+        schedule = tuning.choose(key, tuning.probe_measure(solve_batched, A, B, precond, fsai, matvec))
     lib = _capi.load()
     dev = A.values.device
     n = A.n

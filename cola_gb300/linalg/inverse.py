@@ -39,8 +39,11 @@ class IterativeOperatorWInfo(O.LinearOperator):
 
 
 def cg(A: O.LinearOperator, rhs: torch.Tensor, x0=None, P=None, tol=1e-6, max_iters=5000, pbar=False,
-       check_every: int = 16, allow_fused: bool = True):
+       check_every: int = 16, allow_fused: bool = True, graph: bool = True):
     """Solve A X = B by CG (cg.py:39-69).  Returns (solution, info).
+
+    ``graph``: when the multi-launch loop runs (general operators / preconditioners), replay one
+    captured CUDA graph per block of ``check_every`` steps instead of launching every kernel.
 
     Differentiable in ``rhs`` and in the operator's tensors with the reference's rule (cg_bwd,
     cg.py:72-86): the adjoint is one more CG solve with the same tolerance, iterations and P."""
@@ -49,12 +52,12 @@ def cg(A: O.LinearOperator, rhs: torch.Tensor, x0=None, P=None, tol=1e-6, max_it
         def solve(b, first=[True]):
             use_x0 = x0 if first[0] else None
             first[0] = False
-            return _cg_device(A, b.detach(), use_x0, P, tol, max_iters, check_every, allow_fused)
+            return _cg_device(A, b.detach(), use_x0, P, tol, max_iters, check_every, allow_fused, graph)
         return cg_with_grad(A, rhs, solve)
-    return _cg_device(A, rhs, x0, P, tol, max_iters, check_every, allow_fused)
+    return _cg_device(A, rhs, x0, P, tol, max_iters, check_every, allow_fused, graph)
 
 
-def _cg_device(A, rhs, x0, P, tol, max_iters, check_every, allow_fused):
+def _cg_device(A, rhs, x0, P, tol, max_iters, check_every, allow_fused, graph=True):
     low = lower(A)
     dev = operator_device(A, low)
     _capi.require_cuda(rhs)
@@ -74,7 +77,7 @@ def _cg_device(A, rhs, x0, P, tol, max_iters, check_every, allow_fused):
     max_iters = int(max_iters)
     hist = torch.zeros(max_iters + 1, dtype=dt, device=dev)
     prm = _capi.CgParams(tol=float(tol), max_iters=max_iters, check_every=int(check_every),
-                         allow_fused=1 if allow_fused else 0, reserved=0, spin_limit=0)
+                         allow_fused=1 if allow_fused else 0, graph=0 if graph else 1, spin_limit=0)
     res = _capi.CgResult()
     nbytes = C.c_size_t()
     _capi.check(lib.colagb_cg_workspace_bytes(low.handle, plow.handle if plow else None, k, C.byref(nbytes)), "cg")
@@ -89,7 +92,8 @@ def _cg_device(A, rhs, x0, P, tol, max_iters, check_every, allow_fused):
     # while_loop_winfo records the error at every cond evaluation plus once more at the end and drops
     # the first two entries (torch_tqdm.py:45-62)
     errors = np.concatenate([h, h[-1:]])[2:]
-    info = {"iterations": its + 1, "errors": errors, "iteration_time": elapsed / (its + 1), "fused": bool(res.fused)}
+    info = {"iterations": its + 1, "errors": errors, "iteration_time": elapsed / (its + 1), "fused": bool(res.fused),
+            "graph": bool(res.graph)}
     soln = X.reshape(-1) if is_vector else X
     return soln, info
 

@@ -277,8 +277,8 @@ class Kronecker(LinearOperator):
     """Kronecker product M1 (x) M2 (x) ... (operators.py:199-228).
 
     ``precision`` (keyword only; FP32 operators) selects the arithmetic of the factor contractions:
-    "auto" (default) runs large contractions (>= 2^26 multiply-adds, Dense factors) on the tensor
-    cores with the three-product BF16 split and the rest in FP32; "bf16x3", "bf16" and "fp32" force
+    "auto" (default) runs large contractions (>= 2^26 multiply-adds, Dense factors with >= 256
+    columns) on the tensor cores with the three-product BF16 split and the rest in FP32; "bf16x3", "bf16" and "fp32" force
     one kind.  FP64 operators always contract in FP64."""
 
     def __init__(self, *Ms, precision: str = "auto"):

@@ -88,7 +88,7 @@ typedef struct colagb_op_node {
 
 /* Kronecker contraction arithmetic (FP32 compute type; FP64 operators always use FP64 arithmetic).
  * AUTO: tensor cores with the three-product BF16 split (BF16X3) for contractions of at least 2^26
- * multiply-adds whose factor is Dense and has a multiple-of-8 column count, FP32 SIMT otherwise.
+ * multiply-adds whose factor is Dense with at least 256 columns, FP32 SIMT otherwise.
  * BF16: one BF16 product per term (FP32 accumulation).  BF16X3: hi = bf16(v), lo = bf16(v - hi);
  * hi.hi + hi.lo + lo.hi in FP32 (about 2^-16 relative per product).  FP32: FP32 SIMT only. */
 #define COLAGB_KRON_AUTO 0
@@ -125,7 +125,8 @@ typedef struct colagb_cg_params {
   int32_t max_iters;     /* CG(max_iters=...) */
   int32_t check_every;   /* host polls the device stop flag every this many iterations (0 = 16) */
   int32_t allow_fused;   /* 1: use the single-launch persistent kernel when the operator allows it */
-  int32_t reserved;
+  int32_t graph;         /* multi-launch loop: 0 = capture one block of check_every steps as a CUDA graph
+                            and replay it (when max_iters >= 2 * check_every); 1 = plain launches */
   int64_t spin_limit;    /* grid-barrier spin bound of the persistent kernel (0 = default) */
 } colagb_cg_params;
 
@@ -133,7 +134,7 @@ typedef struct colagb_cg_result {
   int32_t iterations;    /* k, the number of CG steps taken (state[1] of run_batched_cg) */
   int32_t fused;         /* 1 if the persistent single-launch kernel ran */
   int32_t status;        /* COLAGB_OK or COLAGB_ERR_TIMEOUT */
-  int32_t reserved;
+  int32_t graph;         /* 1 if the multi-launch loop ran as replays of a captured CUDA graph */
 } colagb_cg_result;
 
 /* P may be NULL (identity).  X holds x0 on entry and the solution on exit.

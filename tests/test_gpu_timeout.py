@@ -22,7 +22,7 @@ def _dense_cg(op, B, spin_limit):
     low = Lowered(op)
     n, k = B.shape
     X = torch.zeros_like(B)
-    prm = _capi.CgParams(tol=0.0, max_iters=200, check_every=16, allow_fused=1, reserved=0, spin_limit=spin_limit)
+    prm = _capi.CgParams(tol=0.0, max_iters=200, check_every=16, allow_fused=1, graph=0, spin_limit=spin_limit)
     res = _capi.CgResult()
     nb = C.c_size_t()
     _capi.check(lib.colagb_cg_workspace_bytes(low.handle, None, k, C.byref(nb)), "ws")

@@ -24,7 +24,7 @@ def _solve(op, B, x0, allocating: bool, tol=1e-7, max_iters=600, P=None, allow_f
     ph = lowp.handle if lowp is not None else None
     k = B.shape[1]
     X = x0.clone()
-    prm = _capi.CgParams(tol=tol, max_iters=max_iters, check_every=16, allow_fused=allow_fused, reserved=0,
+    prm = _capi.CgParams(tol=tol, max_iters=max_iters, check_every=16, allow_fused=allow_fused, graph=0,
                          spin_limit=0)
     res = _capi.CgResult()
     st = _capi.stream_ptr(DEV)
@@ -102,7 +102,7 @@ def test_noalloc_rejects_problems_beyond_its_scratch():
     low = Lowered(op)
     B = torch.ones(n, k, device=DEV)
     X = torch.zeros_like(B)
-    prm = _capi.CgParams(tol=1e-6, max_iters=10, check_every=16, allow_fused=1, reserved=0, spin_limit=0)
+    prm = _capi.CgParams(tol=1e-6, max_iters=10, check_every=16, allow_fused=1, graph=0, spin_limit=0)
     res = _capi.CgResult()
     st = lib.colagb_cg_solve_noalloc(low.handle, None, B.data_ptr(), k, X.data_ptr(), k, k, C.byref(prm), None,
                                      C.byref(res), _capi.stream_ptr(DEV))
