@@ -606,11 +606,30 @@ def cpu_baseline(args, fam, B, sample_s=15.0):
     n = fam.n
     done, t_used, iters, worst = 0, 0.0, [], 0.0
     s = 0
+    op_kind = "Sparse"
     while t_used < sample_s and s < fam.num_systems:
         indptr, indices, rows, vals, dg, b = _jacobi_inputs(fam, B, s)
+        Acsr = torch.sparse_csr_tensor(indptr, indices, vals, (n, n))
         if cola_ref is not None:
-            # the reference's own operator and algorithm objects; building the CSR (host scipy) is set-up
-            A = cola_ref.PSD(cola_ref.ops.Sparse(vals, rows, indices, (n, n)))
+            # the reference's own operator and algorithm objects; building the CSR (host scipy) is set-up.
+            # Its Sparse pairs row-argsorted values with scipy's column-sorted indices through an
+            # unstable argsort (operators.py:64-76): where that reorders the (row-sorted) triplets, the
+            # operator is not the given matrix, and the same CSR product (Sparse._matmat, operators.py:77-78)
+            # is wrapped in the reference's LinearOperator base class instead.
+            A0 = cola_ref.ops.Sparse(vals, rows, indices, (n, n))
+            probe = torch.randn(n, dtype=torch.float64, generator=torch.Generator().manual_seed(s))
+            if not torch.allclose(A0 @ probe, Acsr @ probe, rtol=1e-12, atol=0.0):
+                op_kind = "LinearOperator(CSR @ X) (the reference's Sparse reordered the values on this host)"
+
+                class _CSR(cola_ref.ops.LinearOperator):
+                    def __init__(self, M):
+                        super().__init__(dtype=M.dtype, shape=M.shape)
+                        self.M = M
+
+                    def _matmat(self, X):
+                        return self.M @ X
+                A0 = _CSR(Acsr)
+            A = cola_ref.PSD(A0)
             P = cola_ref.ops.Diagonal(1.0 / dg)
             alg = cola_ref.linalg.CG(tol=5e-9, max_iters=100000, P=P)
             t0 = time.perf_counter()
@@ -629,12 +648,12 @@ def cpu_baseline(args, fam, B, sample_s=15.0):
             t_used += time.perf_counter() - t0
             x = xk[:, 0]
             iters.append(k)
-        Acsr = torch.sparse_csr_tensor(indptr, indices, vals, (n, n))
-        worst = max(worst, float((b - Acsr @ x).norm() / b.norm()))
+        rr = float((b - Acsr @ x).norm() / b.norm())
+        worst = rr if (rr != rr or worst != worst) else max(worst, rr)  # a NaN stays visible
         done += 1
         s += 1
     kind = "reference" if cola_ref is not None else "port"
-    what = ("cola.linalg.inv(PSD(Sparse), CG(tol=5e-9, P=Diagonal(1/diag))) @ b of the reference package"
+    what = (f"cola.linalg.inv(PSD({op_kind}), CG(tol=5e-9, P=Diagonal(1/diag))) @ b of the reference package"
             if cola_ref is not None else "the reference CG loop restated on torch CPU ops")
     return {"value": done / t_used, "unit": UNIT, "cores": threads, "kind": kind,
             "sample": f"{done} of the {fam.num_systems} instances, {what}, float64, "

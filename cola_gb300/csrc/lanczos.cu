@@ -209,6 +209,45 @@ __global__ void __launch_bounds__(256) k_lz_project(const T* basis, const T* w, 
   }
 }
 
+// Single-vector form (bs == 1, n % 4 == 0): block blk owns rows [blk * chunk, (blk + 1) * chunk) with
+// chunk a multiple of 128.  w's chunk is staged once in shared memory; warp q takes slots j = 1 + q,
+// 1 + q + nwarps, ...: its lanes stream the slot's chunk with 128-bit loads (all of a slot's loads in
+// flight at once), multiply by w from shared memory and finish with one shuffle reduction per slot.
+// One pass reads each filled slot once, with no block-wide barrier per slot.
+__global__ void __launch_bounds__(256) k_lz_project1(const float* __restrict__ basis, const float* __restrict__ w,
+                                                     int64_t n, int64_t chunk, int64_t slots, LzState<float> s) {
+  if (*s.done) return;
+  extern __shared__ float4 wsm[];
+  const int i = *s.step;
+  const int64_t r0 = (int64_t)blockIdx.x * chunk;
+  const int64_t r1 = r0 + chunk < n ? r0 + chunk : n;
+  const int64_t n4 = (r1 - r0) / 4;  // float4 groups in this chunk (n and chunk are multiples of 4)
+  const float4* w4 = reinterpret_cast<const float4*>(w + r0);
+  for (int64_t u = threadIdx.x; u < n4; u += blockDim.x) wsm[u] = w4[u];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  float* out = s.hpart + (int64_t)blockIdx.x * slots;
+  for (int j = 1 + warp; j <= i; j += nw) {
+    const float4* v4 = reinterpret_cast<const float4*>(basis + (int64_t)j * n + r0);
+    float acc0 = 0.f, acc1 = 0.f;
+    int64_t u = lane;
+#pragma unroll 4
+    for (; u + 32 < n4; u += 64) {
+      const float4 a = __ldg(v4 + u), b = __ldg(v4 + u + 32);
+      const float4 x = wsm[u], y = wsm[u + 32];
+      acc0 += a.x * x.x + a.y * x.y + a.z * x.z + a.w * x.w;
+      acc1 += b.x * y.x + b.y * y.y + b.z * y.z + b.w * y.w;
+    }
+    for (; u < n4; u += 32) {
+      const float4 a = __ldg(v4 + u);
+      const float4 x = wsm[u];
+      acc0 += a.x * x.x + a.y * x.y + a.z * x.z + a.w * x.w;
+    }
+    const float t = warp_sum(acc0 + acc1);
+    if (lane == 0) out[j] = t;
+  }
+}
+
 // h[j][b] = sum over blocks of hpart  (one warp per (j, b): lanes take strided blocks, then a
 // shuffle tree; a thread per (j, b) would wait on nblk dependent loads)
 template <class T>
@@ -234,6 +273,29 @@ __global__ void k_lz_subtract(const T* basis, T* w, int64_t n, int64_t bs, LzSta
   if (*s.done) return;
   const int i = *s.step;
   if constexpr (std::is_same<T, float>::value) {
+    if (bs == 1 && n % 4 == 0) {  // one coefficient per slot, four rows per 128-bit access
+      const int64_t n4 = n / 4;
+      float4* w4 = reinterpret_cast<float4*>(w);
+      for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n4; u += (int64_t)gridDim.x * blockDim.x) {
+        float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll 8
+        for (int j = 1; j <= i; ++j) {
+          const float4 v = __ldg(reinterpret_cast<const float4*>(basis + (int64_t)j * n) + u);
+          const float h = s.hbuf[j];
+          acc.x += v.x * h;
+          acc.y += v.y * h;
+          acc.z += v.z * h;
+          acc.w += v.w * h;
+        }
+        float4 wv = w4[u];
+        wv.x -= acc.x;
+        wv.y -= acc.y;
+        wv.z -= acc.z;
+        wv.w -= acc.w;
+        w4[u] = wv;
+      }
+      return;
+    }
     if (bs % 4 == 0) {
       const int64_t n4 = n * bs / 4;
       float4* w4 = reinterpret_cast<float4*>(w);
@@ -557,6 +619,21 @@ static int lanczos_t(const colagb_op* A, const T* V0, int64_t ldv0, int64_t bs, 
   k_lz_scale<T><<<eg, 256, 0, st>>>(v1, n, bs, s);
   COLAGB_CUDA(cudaGetLastError());
   const int every = prm.check_every > 0 ? prm.check_every : 8;
+  // single-vector FP32 runs project with k_lz_project1 (w's chunk in shared memory, a warp per slot)
+  bool p1 = false;
+  int64_t chunk = 0;
+  int nb1 = nb;
+  if constexpr (std::is_same<T, float>::value) {
+    if (bs == 1 && n % 4 == 0 && (uintptr_t)basis % 16 == 0) {
+      chunk = ceil_div(ceil_div(n, nb), 128) * 128;
+      if (chunk * (int64_t)sizeof(float) <= 160 * 1024) {
+        p1 = true;
+        nb1 = (int)ceil_div(n, chunk);
+        COLAGB_CUDA(cudaFuncSetAttribute(k_lz_project1, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(chunk * sizeof(float))));
+      }
+    }
+  }
   int host_step = 1;  // the step index the next launch group starts at (upper bound)
   int hdone = 0;
   while (true) {
@@ -572,9 +649,16 @@ static int lanczos_t(const colagb_op* A, const T* V0, int64_t ldv0, int64_t bs, 
       k_lz_alpha<T><<<nb, 256, 0, st>>>(w, vi, n, bs, diag, m, s);
       k_lz_three_term<T><<<eg, 256, 0, st>>>(w, vi, vim1, n, bs, diag, subdiag, m, s);
       for (int pass = 0; pass < 2; ++pass) {
-        k_lz_project<T><<<nb, 256, 0, st>>>(basis, w, n, bs, slots, s);
+        if constexpr (std::is_same<T, float>::value) {
+          if (p1)
+            k_lz_project1<<<nb1, 256, chunk * sizeof(float), st>>>(basis, w, n, chunk, slots, s);
+          else
+            k_lz_project<T><<<nb, 256, 0, st>>>(basis, w, n, bs, slots, s);
+        } else {
+          k_lz_project<T><<<nb, 256, 0, st>>>(basis, w, n, bs, slots, s);
+        }
         k_lz_reduce_h<T><<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div((int64_t)(i + 1) * bs, 8), 4096)),
-                           256, 0, st>>>(nb, bs, slots, s);
+                           256, 0, st>>>(p1 ? nb1 : nb, bs, slots, s);
         k_lz_subtract<T><<<eg, 256, 0, st>>>(basis, w, n, bs, s);
       }
       k_lz_finish<T><<<nb, 256, 0, st>>>(w, n, bs, subdiag, m, prm.tol, s);

@@ -312,3 +312,37 @@ def train(net: FsaiNet, st_train: torch.Tensor, r_train: torch.Tensor, e_train: 
         if on_epoch is not None:
             on_epoch(ep, hist[-1])
     return hist
+
+
+# ---------------------------------------------------------------------------------------------
+# the CG(P=...) hook: P = G^T G as a LinearOperator
+
+def factor_operator(pat: FsaiPattern, g: torch.Tensor):
+    """P = G^T G of one system as a LinearOperator (a Product of the two CSR factors), for the
+    reference's preconditioner hook ``CG(P=...)`` (cola/linalg/inverse/cg.py:124, 150): CG applies it
+    as P @ r on the device with the structured-matvec runtime.  ``g``: the (g_nnz,) G values of one
+    system in the lower pattern's CSR order."""
+    from .. import ops as O
+    n = pat.g_indptr.numel() - 1
+    g = g.to(torch.float32).contiguous()
+    G = O.Sparse.from_csr(pat.g_indptr, pat.g_indices, g, (n, n))
+    Gt = O.Sparse.from_csr(pat.gt_indptr, pat.gt_indices, g[pat.gt_perm.long()].contiguous(), (n, n))
+    return O.Product(Gt, G)
+
+
+def learned_preconditioner(A, net: FsaiNet | None = None, weights=WEIGHTS, closed_form: bool = False):
+    """The trained network's FSAI preconditioner of a 5-point operator A (a Sparse LinearOperator on an
+    m x m grid, rows i * m + j, FP32 values) as a LinearOperator P = G^T G, ready for
+    ``cola.linalg.solve(PSD(A), b, CG(P=learned_preconditioner(A)))``.  ``closed_form`` builds the
+    closed-form FSAI factor instead of the network's."""
+    from .. import ops as O
+    A0 = A  # PSD(...) / SelfAdjoint(...) keep the operator's class
+    if not isinstance(A0, O.Sparse):
+        raise NotImplementedError("the learned FSAI preconditioner is built for Sparse 5-point operators")
+    fam = BatchedCSR(A0.indptr, A0.indices, A0.values.to(torch.float32)[None, :])
+    if not closed_form and net is None:
+        if not Path(weights).exists():
+            raise FileNotFoundError(f"trained weights {weights} not found")
+        net = FsaiNet.load(weights, device=A0.values.device)
+    pat, g = g_values(fam, None if closed_form else net)
+    return factor_operator(pat, g[0])
