@@ -79,9 +79,10 @@ def _fp64_pcg_oracle(ip, ix, v, B, tol=1e-12, max_iters=20000):
 
 
 def c2_diffusion3d(nrhs=32, m=128, steps=1, warmup=1):
-    """7-point 128^3 diffusion + 1e-3 I, 32 right-hand sides, each to a 1e-8 FP64 true residual: FP32 against
-    BF16 inner matvecs (FP64 residual replacement in both), with and without Jacobi; solution error
-    against an FP64 CG oracle run in plain torch ops."""
+    """7-point 128^3 diffusion + 1e-3 I, 32 right-hand sides, each to a 1e-8 FP64 true residual: the lockstep
+    block schedule (matrix read once per step for all 32) and one cluster per right-hand side, FP32
+    against BF16 inner matvecs (FP64 residual replacement in all), with and without Jacobi; solution
+    error against an FP64 CG oracle run in plain torch ops."""
     ip, ix, v = diffusion_3d(m=m, device="cuda")
     fam = BatchedCSR(ip, ix, v[None, :], shared=True)
     B = torch.randn(nrhs, fam.n, device="cuda", dtype=torch.float64, generator=torch.Generator("cuda").manual_seed(2))
@@ -89,10 +90,11 @@ def c2_diffusion3d(nrhs=32, m=128, steps=1, warmup=1):
     out = {"config": f"diffusion3d-{m}^3-{nrhs}rhs", "n": fam.n, "nnz": int(ix.numel()),
            "fp64_oracle": f"Jacobi-PCG in torch FP64 ops to relres 1e-12 ({it64} steps)"}
     for prec in ("jacobi", "none"):
-        for mv in ("fp32", "bf16"):
-            (X, info), t = _timed(lambda: solve_batched(fam, B, precond=prec, tol=1e-8, matvec=mv), steps, warmup)
+        for mv, sched in (("fp32", "block"), ("fp32", "cluster16"), ("bf16", "cluster16")):
+            (X, info), t = _timed(lambda: solve_batched(fam, B, precond=prec, tol=1e-8, matvec=mv, schedule=sched),
+                                  steps, warmup)
             err = ((X - X64).norm(dim=1) / X64.norm(dim=1)).max()
-            out[f"{prec}_{mv}"] = {"rhs_per_s": nrhs / t, "s_per_call": t,
+            out[f"{prec}_{mv}_{sched}"] = {"rhs_per_s": nrhs / t, "s_per_call": t,
                                    "mean_iters": float(info["iterations"].double().mean()),
                                    "max_true_relres": float(info["relres"].max()),
                                    "max_sol_err_vs_fp64": float(err), "schedule": info["schedule"]}

@@ -644,9 +644,24 @@ struct BatchedWs {
   size_t onchip_bytes;
   __nv_bfloat16* v16;  // BF16 inner matvec: off-diagonal values and the consistent diagonal
   float* dg16;
+  char* block;         // block schedule buffers (cg_block.cu)
+  size_t block_bytes;
 };
 
 size_t onchip_workspace_floats(int64_t n, bool fsai);
+size_t block_workspace_bytes(int64_t n, int64_t S, int nb_max);
+int block_grid_blocks();
+int block_pcg_solve(const colagb_batched_csr* A, const double* B, double* X, const colagb_ir_params* prm,
+                    int32_t* iters, int32_t* status, double* relres, void* ws_ptr, size_t ws_bytes, int* max_rep,
+                    cudaStream_t st);
+
+// Whether the lockstep block schedule runs: asked for, or AUTO on a shared-values family of >= 4
+// right-hand sides with a Jacobi / no preconditioner and the FP32 matvec.
+static bool use_block(const colagb_batched_csr& A, const colagb_ir_params& prm) {
+  if (prm.schedule == COLAGB_SCHED_BLOCK) return true;
+  return prm.schedule == COLAGB_SCHED_AUTO && A.shared_values && A.num_systems >= 4 &&
+         prm.preconditioner != COLAGB_PREC_FSAI && prm.matvec == COLAGB_MATVEC_FP32;
+}
 int onchip_pcg_solve(const colagb_batched_csr* A, const double* B, double* X, const colagb_ir_params* prm,
                      int32_t* iters, int32_t* status, double* relres, int* nrep, void* ws, size_t ws_bytes,
                      bool* used, cudaStream_t st);
@@ -670,6 +685,18 @@ static BatchedWs carve_batched(Bump& ws, const colagb_batched_csr& A, const cola
   w.summary = ws.take<int>(8);
   w.nrep = ws.take<int>(S);
   const bool bf = prm.matvec == COLAGB_MATVEC_BF16;
+  if (use_block(A, prm)) {  // the block schedule carves its own buffers
+    w.onchip = nullptr;
+    w.onchip_bytes = 0;
+    w.v16 = nullptr;
+    w.dg16 = nullptr;
+    const size_t bb = block_workspace_bytes(A.n, A.num_systems, num_sms() * 2);
+    w.block = ws.take<char>(bb);
+    w.block_bytes = bb;
+    return w;
+  }
+  w.block = nullptr;
+  w.block_bytes = 0;
   const bool onchip = !bf && (prm.schedule == COLAGB_SCHED_AUTO || prm.schedule == COLAGB_SCHED_ONCHIP);
   const size_t nf = onchip ? onchip_workspace_floats(A.n, fsai) : 0;
   w.onchip = nf ? ws.take<float>(nf) : nullptr;
@@ -702,8 +729,12 @@ static int validate_batched(const colagb_batched_csr* A, const colagb_ir_params*
     return fail(COLAGB_ERR_INVALID, "batched CG: missing CSR arrays");
   if (prm->preconditioner < 0 || prm->preconditioner > 2)
     return fail(COLAGB_ERR_INVALID, "batched CG: unknown preconditioner");
-  if (prm->schedule < COLAGB_SCHED_AUTO || prm->schedule > COLAGB_SCHED_ONCHIP)
+  if (prm->schedule < COLAGB_SCHED_AUTO || prm->schedule > COLAGB_SCHED_BLOCK)
     return fail(COLAGB_ERR_INVALID, "batched CG: unknown schedule");
+  if (prm->schedule == COLAGB_SCHED_BLOCK &&
+      (!A->shared_values || prm->preconditioner == COLAGB_PREC_FSAI || prm->matvec != COLAGB_MATVEC_FP32))
+    return fail(COLAGB_ERR_UNSUPPORTED,
+                "batched CG: the block schedule needs a shared-values family, no FSAI and the FP32 matvec");
   if (prm->mode != COLAGB_IR_RELIABLE && prm->mode != COLAGB_IR_RESTART)
     return fail(COLAGB_ERR_INVALID, "batched CG: unknown refinement mode");
   if (prm->preconditioner == COLAGB_PREC_FSAI &&
@@ -755,6 +786,14 @@ extern "C" int colagb_cg_batched_csr_solve(const colagb_batched_csr* A, const do
   if (workspace == nullptr || ws.overflow())
     return fail(COLAGB_ERR_WORKSPACE, "batched CG: workspace too small (need " + std::to_string(ws.peak) + ")");
   cudaStream_t st = as_stream(stream);
+  if (use_block(*A, *params)) {
+    result->schedule = COLAGB_SCHED_BLOCK;
+    int mx = 0;
+    COLAGB_TRY(block_pcg_solve(A, B, X, params, per_system_iters, per_system_status, relres, w.block, w.block_bytes,
+                               &mx, st));
+    result->sweeps = mx;
+    return COLAGB_OK;
+  }
   const int csize = pick_cluster(*params, A->n);
   const bool try_onchip = params->matvec == COLAGB_MATVEC_FP32 &&
                           (params->schedule == COLAGB_SCHED_AUTO || params->schedule == COLAGB_SCHED_ONCHIP);

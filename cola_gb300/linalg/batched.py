@@ -129,7 +129,7 @@ class FsaiPattern:
 
 
 _PREC = {"none": _capi.PREC_NONE, None: _capi.PREC_NONE, "jacobi": _capi.PREC_JACOBI, "fsai": _capi.PREC_FSAI}
-_SCHED = {"auto": 0, "grid": 1, "cluster8": 2, "cluster16": 3, "onchip": 4}
+_SCHED = {"auto": 0, "grid": 1, "cluster8": 2, "cluster16": 3, "onchip": 4, "block": 5}
 _SCHED_NAME = {v: k for k, v in _SCHED.items()}
 
 
@@ -162,7 +162,10 @@ def solve_batched(A: BatchedCSR, B: torch.Tensor, precond: str = "jacobi", tol: 
             the cluster's shared memory and the matrix stored by diagonals (patterns of at most 9
             constant-offset diagonals, n <= 262144); "cluster8" / "cluster16" -- one cluster per system
             on the CSR pattern, vectors in global memory; "grid" -- one cooperative grid that advances
-            every system together; "auto" (default) -- "onchip" when it applies, else a cluster;
+            every system together; "block" -- shared-values families: every right-hand side a column
+            of one (n, k) block advancing in lockstep, the matrix read once per step for all of them;
+            "auto" (default) -- "block" for shared-values families of >= 4 right-hand sides (no FSAI,
+            FP32 matvec), else "onchip" when it applies, else a cluster;
             "tuned" -- the fastest applicable schedule for this GPU, pattern, size and preconditioner,
             measured once and kept in the autotuner's JSON cache (cola_gb300.tuning).
         wait: False returns once the solve is enqueued on the current stream (the on-chip and cluster

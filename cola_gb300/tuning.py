@@ -22,7 +22,7 @@ from pathlib import Path
 
 import torch
 
-CANDIDATES = ("onchip", "cluster8", "cluster16", "grid")
+CANDIDATES = ("onchip", "cluster8", "cluster16", "grid", "block")
 _lock = threading.Lock()
 _mem: dict | None = None
 

@@ -235,6 +235,12 @@ typedef struct colagb_ir_params {
                                    cluster's shared memory and the matrix in diagonal storage; needs a
                                    pattern of <= 9 constant-offset diagonals (FSAI: a lower G of <= 5),
                                    n <= 262144.  AUTO takes it whenever those hold. */
+#define COLAGB_SCHED_BLOCK 5    /* shared-values families (one matrix, many right-hand sides): all
+                                   right-hand sides advance in lockstep as the columns of one (n, k)
+                                   block, so each step reads the matrix once for all of them (the
+                                   reference's own multi-column CG layout); one cooperative grid; no
+                                   FSAI, FP32 matvec.  AUTO takes it for shared-values families of at
+                                   least 4 right-hand sides with those options. */
 
 /* Geometry of the on-chip schedule for systems of n rows whose diagonals reach `halo` rows off the
  * main diagonal: info[0] cluster size (0: n too large), info[1] rows per CTA, info[2] clusters that
