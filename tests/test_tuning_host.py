@@ -16,7 +16,7 @@ def test_tuner_measures_once_then_reads_the_cache(tmp_path, monkeypatch):
 
     def measure(s):
         calls.append(s)
-        return {"onchip": 3e-6, "cluster8": 2e-6, "cluster16": None, "grid": 9e-6}[s]
+        return {"onchip": 3e-6, "cluster8": 2e-6, "cluster16": None, "grid": 9e-6, "block": None}[s]
     assert tuning.choose("k1", measure) == "cluster8"
     assert calls == list(tuning.CANDIDATES)
     rec = json.loads(path.read_text())["k1"]
