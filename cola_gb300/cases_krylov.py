@@ -3,11 +3,13 @@
     python -m cola_gb300.cases_krylov c5 [--scale 0.25] [--repeat 1] [--precision auto|fp32]
     python -m cola_gb300.cases_krylov c3b [--probes 64]
     python -m cola_gb300.cases_krylov c1
+    python -m cola_gb300.cases_krylov c2 [--scale 0.5] [--schedule block|cluster16] [--matvec fp32|bf16]
 
 c5: 256-step Lanczos top-64 of Kronecker(A1, A2) + L (random-geometric-graph Laplacian); --scale < 1
 shrinks the factors and the graph (n = (1024 s)^2 rows) so that a capture stays small.  c3b: the
 Kronecker SLQ log-determinant with 64 probes and 100 steps.  c1: the 2048 dense CG solve.  Prints one
-JSON line per run with its wall time (CUDA-synchronised).
+JSON line per run with its wall time (CUDA-synchronised).  c2: the 7-point diffusion solve of 32
+right-hand sides to a 1e-8 FP64 residual with Jacobi (grid side 128 s).
 """
 from __future__ import annotations
 
@@ -20,7 +22,9 @@ import torch
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("config", choices=["c1", "c3b", "c5"])
+    ap.add_argument("config", choices=["c1", "c2", "c3b", "c5"])
+    ap.add_argument("--schedule", default="auto")
+    ap.add_argument("--matvec", default="fp32", choices=["fp32", "bf16"])
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--repeat", type=int, default=1)
     ap.add_argument("--precision", default="auto", choices=["auto", "fp32", "bf16", "bf16x3"])
@@ -56,6 +60,15 @@ def main(argv=None):
 
         def run():
             return cola.linalg.stochastic_lanczos_quad(op, torch.log, max_iters=steps, tol=0.0, probes=Z)
+    elif args.config == "c2":
+        from cola_gb300.linalg.batched import BatchedCSR, solve_batched
+        m = max(8, int(128 * args.scale))
+        ip, ix, v = W.diffusion_3d(m=m, device=dev)
+        fam = BatchedCSR(ip, ix, v[None, :], shared=True)
+        B = torch.randn(32, fam.n, device=dev, dtype=torch.float64, generator=torch.Generator("cuda").manual_seed(2))
+
+        def run():
+            return solve_batched(fam, B, precond="jacobi", tol=1e-8, schedule=args.schedule, matvec=args.matvec)
     else:
         A, b, _ = W.dense_spd(2048, seed=0, lo=1e-2, hi=1e2, dtype=torch.float32)
         op = cola.PSD(cola.ops.Dense(A.to(dev)))

@@ -441,20 +441,30 @@ __global__ void k_tridiag_ql(const double* A, const double* Bv, int64_t m, doubl
         double s = 1.0, c = 1.0, p = 0.0;
         int i = mm - 1;
         bool underflow = false;
+        // The sweep is one dependent chain on this thread: the operands of step i - 1 (e[i-1], d[i-1],
+        // z0[i-1]), which step i does not modify, are loaded ahead, d[i] / z0[i] are carried in
+        // registers, and each rotation takes one reciprocal square root instead of a hypot and two
+        // divisions (|f|, |g| stay far inside the FP64 range here).
+        double ei = e[i], di1 = d[i + 1], di = d[i], zi1 = z0[i + 1];
         for (; i >= l; --i) {
-          double f = s * e[i], bb = c * e[i];
-          r = hypot(f, g);
-          e[i + 1] = r;
-          if (r == 0.0) {
-            d[i + 1] -= p;
+          const double e_nx = i > l ? e[i - 1] : 0.0;
+          const double d_nx = i > l ? d[i - 1] : 0.0;
+          const double zi = z0[i];
+          const double f = s * ei, bb = c * ei;
+          const double q = fma(f, f, g * g);
+          if (q == 0.0) {
+            e[i + 1] = 0.0;
+            d[i + 1] = di1 - p;
             e[mm] = 0.0;
             underflow = true;
             break;
           }
-          s = f / r;
-          c = g / r;
-          g = d[i + 1] - p;
-          r = (d[i] - g) * s + 2.0 * c * bb;
+          const double ri = rsqrt(q);
+          e[i + 1] = q * ri;
+          s = f * ri;
+          c = g * ri;
+          g = di1 - p;
+          r = (di - g) * s + 2.0 * c * bb;
           p = s * r;
           d[i + 1] = g + p;
           g = c * r - bb;
@@ -467,9 +477,13 @@ __global__ void k_tridiag_ql(const double* A, const double* Bv, int64_t m, doubl
             }
             ++nrec;
           }
-          const double zf = z0[i + 1];
-          z0[i + 1] = s * z0[i] + c * zf;
-          z0[i] = c * z0[i] - s * zf;
+          z0[i + 1] = s * zi + c * zi1;
+          const double zi_new = c * zi - s * zi1;
+          z0[i] = zi_new;
+          ei = e_nx;
+          di1 = di;
+          di = d_nx;
+          zi1 = zi_new;
         }
         if (underflow) {
           s_lo = i + 1;

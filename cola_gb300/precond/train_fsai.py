@@ -181,6 +181,32 @@ def search(net, seeds, m, device, log=print):
     return best[1], best[2], best[0], len(cache)
 
 
+def instance_headroom(net, seeds, m, device, wns, wvs, log=print):
+    """Per-instance optimum of the global over-relaxation: every (w_N, w_W) of the grid on every instance
+    (PCG iterations to 1e-8).  Returns the iteration table (combos x instances), the best single combo
+    and the mean over instances of each instance's own best -- the most any factor that picks one
+    over-relaxation per operator (which is all a network of these features can do better than the
+    constant) could gain."""
+    fam, B, _, _ = diffusion_family_2d(seeds, m=m, device=device)
+    combos, table = [], []
+    for wn in wns:
+        for wv in wvs:
+            set_constant_output(net, math.atanh(wn), math.atanh(wv))
+            pat, gv = L.g_values(fam, net)
+            _, info = solve_batched(fam, B, precond="fsai", fsai=(pat, gv), tol=1e-8, fallback=True)
+            combos.append((wn, wv))
+            table.append(info["iterations"].double())
+            log(f"headroom: w_N {wn:.3f} w_W {wv:.3f} -> {float(table[-1].mean()):.1f}")
+    T = torch.stack(table)  # (combos, instances)
+    mean = T.mean(dim=1)
+    g = int(mean.argmin())
+    per = T.min(dim=0)
+    return {"combos": combos, "global_best": combos[g], "global_best_mean_iters": float(mean[g]),
+            "per_instance_best_mean_iters": float(per.values.mean()),
+            "per_instance_best_combo": [combos[int(i)] for i in per.indices],
+            "headroom_fraction": float(1 - per.values.mean() / mean[g])}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--train", type=int, default=2048)
@@ -195,6 +221,9 @@ def main():
                     help="fit the off-diagonal over-relaxation by direct search on PCG iterations "
                          "(instances 1000 .. 1000 + --search-systems) instead of gradient training")
     ap.add_argument("--search-systems", type=int, default=64)
+    ap.add_argument("--headroom", action="store_true",
+                    help="measure how much an over-relaxation chosen per operator could save over the global "
+                         "fit: a grid around it on --search-systems training instances (report only)")
     ap.add_argument("--features", action="store_true",
                     help="after the global search, fit a per-cell over-relaxation, piecewise linear in the "
                          "local coefficient features (coordinate search on PCG iterations)")
@@ -206,6 +235,17 @@ def main():
                          "(a log-condition proxy); pair: |P r - e|_A^2 / |e|_A^2 on the smooth errors")
     args = ap.parse_args()
     dev = torch.device("cuda")
+    if args.headroom:
+        net = L.FsaiNet(dev, seed=0)
+        seeds = list(range(1000, 1000 + args.search_systems))
+        rep = instance_headroom(net, seeds, args.m, dev, wns=[0.80, 0.85, 0.90, 0.95],
+                                wvs=[0.675, 0.725, 0.775, 0.825, 0.875])
+        rep["instances"] = args.search_systems
+        print(json.dumps({k: v for k, v in rep.items() if k != "per_instance_best_combo"}, indent=1))
+        if args.report:
+            with open(args.report, "w") as f:
+                json.dump(rep, f, indent=1)
+        return
     if args.search:
         net = L.FsaiNet(dev, seed=0)
         val_seeds = list(range(4000, 4000 + args.val))
