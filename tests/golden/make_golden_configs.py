@@ -10,6 +10,8 @@ Cases (each writes tests/golden/cfg_<case>.npz):
   c3a  the first 8 uneven RBF systems K + s^2 I, one reference FP32 CG(tol=1e-6, max_iters=2000) each
   c3b  LanczosUnary(Kron(K1, K2, K3) + 0.01 I, log, max_iters=100) @ Z with the 64 Rademacher probes
        (unary.py:46-60), FP32; the per-probe quadratic forms z^T log(A) z
+  c3b64  the same in FP64 on the first 16 of those probes (in FP32 the operator's rounding, about
+       eps * |A| = 5e-4, is not small against its smallest eigenvalues, 0.01)
   c4   one 512 x 512 diffusion instance, CG(P=Diagonal(1/diag A)) in FP64 to tol 1e-12 (cg.py:124, 150)
   c5   eig(SelfAdjoint(Kron(A1, A2) + L), 64, "LM", Lanczos(max_iters=256)) with the host start vector,
        FP32 (eigs.py:106-111), and scipy's ARPACK eigsh on the FP64 operator as the FP64 oracle
@@ -119,6 +121,18 @@ def case_c3b():
          T_off=torch.diagonal(T_dense, 1, -2, -1).float())
 
 
+def case_c3b64():
+    Ks, ells, Z = c3b_inputs()
+    Z = Z[:, :16].double()
+    K = cola.ops.Kronecker(*[cola.ops.Dense(k.double()) for k in Ks])
+    op = cola.PSD(K + 0.01 * cola.ops.I_like(K))
+    t0 = time.perf_counter()
+    Y = LanczosUnary(op, torch.log, max_iters=100, tol=0.0) @ Z
+    secs = time.perf_counter() - t0
+    quad = (Z * Y).sum(0)
+    save("c3b64", quad=quad, estimate=float(quad.mean()), seconds=secs)
+
+
 def case_c4():
     fam, B, _, params = W.diffusion_family_2d([5000], m=512, device="cpu")
     n = fam.n
@@ -180,7 +194,7 @@ def case_c5():
 
 
 if __name__ == "__main__":
-    cases = {"c1": case_c1, "c3a": case_c3a, "c3b": case_c3b, "c4": case_c4, "c5": case_c5}
+    cases = {"c1": case_c1, "c3a": case_c3a, "c3b": case_c3b, "c3b64": case_c3b64, "c4": case_c4, "c5": case_c5}
     for name in (sys.argv[2:] or list(cases)):
         t = time.perf_counter()
         cases[name]()
