@@ -105,6 +105,7 @@ SIGNATURES = {
                                               _P(IrResult), _vp]),
     "colagb_onchip_schedule_info": (C.c_int, [_i64, _i32, _vp]),
     "colagb_cg_dense_batched_workspace_bytes": (C.c_int, [_i64, _i64, _P(_sz)]),
+    "colagb_dense_batched_residual64": (C.c_int, [_i64, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp]),
     "colagb_cg_dense_batched_solve": (C.c_int, [_i64, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _d, _i32, _vp, _vp, _vp,
                                                 _sz, _vp]),
     "colagb_lanczos_workspace_bytes": (C.c_int, [_vp, _i64, _i32, _P(_sz)]),

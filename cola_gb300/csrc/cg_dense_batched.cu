@@ -10,6 +10,7 @@
 // busy as small systems finish.
 //
 // Layout: A_s row-major at vals + a_off[s]; vectors of system s at v_off[s] in concatenated buffers.
+#include <algorithm>
 #include <string>
 
 #include "common.cuh"
@@ -379,5 +380,64 @@ extern "C" int colagb_cg_dense_batched_solve(int64_t num_systems, const int32_t*
   COLAGB_CUDA(cudaMemcpyAsync(&herr, bar + 2, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
   COLAGB_CUDA(cudaStreamSynchronize(st));
   if (herr != 0) return fail(COLAGB_ERR_TIMEOUT, "dense batched CG: a grid barrier timed out");
+  return COLAGB_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// FP64 residual of the uneven dense batch, for iterative refinement on top of the FP32 CG above:
+// R = B - A X in FP64 (A's FP32 values, FP64 products and sums), one warp per row, plus |r_s|^2 per
+// system.  The system of a row comes from a binary search of v_offsets.
+
+namespace colagb {
+
+__global__ void __launch_bounds__(256) k_dense_residual64(int S, const int32_t* __restrict__ sizes,
+                                                          const int64_t* __restrict__ a_off,
+                                                          const int64_t* __restrict__ v_off, int64_t total_rows,
+                                                          const float* __restrict__ vals,
+                                                          const double* __restrict__ B, const double* __restrict__ X,
+                                                          double* __restrict__ R, double* __restrict__ rr) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < total_rows; g += nwarps) {
+    int lo = 0, hi = S - 1;  // last system whose v_off <= g
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (v_off[mid] <= g) lo = mid;
+      else hi = mid - 1;
+    }
+    const int s = lo;
+    const int64_t n = sizes[s];
+    const int64_t i = g - v_off[s];
+    const float* row = vals + a_off[s] + i * n;
+    const double* x = X + v_off[s];
+    double acc = 0.0;
+    for (int64_t j = lane; j < n; j += 32) acc += (double)row[j] * x[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) {
+      const double r = B[g] - acc;
+      R[g] = r;
+      atomicAdd(rr + s, r * r);
+    }
+  }
+}
+
+}  // namespace colagb
+
+extern "C" int colagb_dense_batched_residual64(int64_t num_systems, const int32_t* sizes, const int64_t* a_offsets,
+                                               const int64_t* v_offsets, int64_t total_rows, const float* values,
+                                               const double* B, const double* X, double* R, double* rr,
+                                               void* stream) {
+  if (num_systems < 1 || num_systems > kDBMaxSystems || total_rows < 0 || !sizes || !a_offsets || !v_offsets ||
+      !values || !B || !X || !R || !rr)
+    return fail(COLAGB_ERR_INVALID, "colagb_dense_batched_residual64: bad arguments");
+  cudaStream_t st = as_stream(stream);
+  COLAGB_CUDA(cudaMemsetAsync(rr, 0, num_systems * sizeof(double), st));
+  if (total_rows == 0) return COLAGB_OK;
+  const int64_t want = ceil_div(total_rows * 32, 256);
+  const int blocks = (int)std::min<int64_t>(want, (int64_t)num_sms() * 16);
+  k_dense_residual64<<<blocks, 256, 0, st>>>((int)num_systems, sizes, a_offsets, v_offsets, total_rows, values, B, X,
+                                             R, rr);
+  COLAGB_CUDA(cudaGetLastError());
   return COLAGB_OK;
 }

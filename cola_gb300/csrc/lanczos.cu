@@ -248,6 +248,53 @@ __global__ void __launch_bounds__(256) k_lz_project1(const float* __restrict__ b
   }
 }
 
+// Block form (bs in {4, 8, 16, 32, 64, 128}, FP32): block blk owns rows [blk * chunk, ...), i.e. one
+// contiguous run of chunk * bs floats per slot.  w's run is staged in shared memory; warp q takes
+// slots j = 1 + q, 1 + q + nwarps, ...; a warp step covers 128 consecutive floats, so lane l always
+// holds column quad l % (bs / 4) and accumulates it in a float4; a shuffle tree over the lanes of
+// the same quad finishes the slot.  128-bit streams, no block-wide barrier per slot.
+__global__ void __launch_bounds__(256) k_lz_projectq(const float* __restrict__ basis, const float* __restrict__ w,
+                                                     int64_t n, int64_t bs, int64_t chunk, int64_t slots,
+                                                     LzState<float> s) {
+  if (*s.done) return;
+  extern __shared__ float4 wsm[];
+  const int i = *s.step;
+  const int64_t r0 = (int64_t)blockIdx.x * chunk;
+  const int64_t r1 = r0 + chunk < n ? r0 + chunk : n;
+  const int64_t n4 = (r1 - r0) * bs / 4;  // float4 units of this block's run
+  const float4* w4 = reinterpret_cast<const float4*>(w + r0 * bs);
+  for (int64_t u = threadIdx.x; u < n4; u += blockDim.x) wsm[u] = w4[u];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int qd = (int)(bs / 4);  // column quads per row: a power of two in [1, 32]
+  float* out = s.hpart + (int64_t)blockIdx.x * slots * bs;
+  for (int j = 1 + warp; j <= i; j += nw) {
+    const float4* v4 = reinterpret_cast<const float4*>(basis + (int64_t)j * n * bs + r0 * bs);
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f), acc2 = make_float4(0.f, 0.f, 0.f, 0.f);
+    int64_t u = lane;
+#pragma unroll 4
+    for (; u + 32 < n4; u += 64) {
+      const float4 a = __ldg(v4 + u), b = __ldg(v4 + u + 32);
+      const float4 x = wsm[u], y = wsm[u + 32];
+      acc.x += a.x * x.x; acc.y += a.y * x.y; acc.z += a.z * x.z; acc.w += a.w * x.w;
+      acc2.x += b.x * y.x; acc2.y += b.y * y.y; acc2.z += b.z * y.z; acc2.w += b.w * y.w;
+    }
+    for (; u < n4; u += 32) {
+      const float4 a = __ldg(v4 + u);
+      const float4 x = wsm[u];
+      acc.x += a.x * x.x; acc.y += a.y * x.y; acc.z += a.z * x.z; acc.w += a.w * x.w;
+    }
+    acc.x += acc2.x; acc.y += acc2.y; acc.z += acc2.z; acc.w += acc2.w;
+    for (int o = 16; o >= qd; o >>= 1) {
+      acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+      acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+      acc.z += __shfl_xor_sync(0xffffffffu, acc.z, o);
+      acc.w += __shfl_xor_sync(0xffffffffu, acc.w, o);
+    }
+    if (lane < qd) reinterpret_cast<float4*>(out + (int64_t)j * bs)[lane] = acc;
+  }
+}
+
 // h[j][b] = sum over blocks of hpart  (one warp per (j, b): lanes take strided blocks, then a
 // shuffle tree; a thread per (j, b) would wait on nblk dependent loads)
 template <class T>
@@ -637,6 +684,7 @@ static int lanczos_t(const colagb_op* A, const T* V0, int64_t ldv0, int64_t bs, 
   bool p1 = false;
   int64_t chunk = 0;
   int nb1 = nb;
+  bool pq = false;  // bs in {4, ..., 128}: k_lz_projectq
   if constexpr (std::is_same<T, float>::value) {
     if (bs == 1 && n % 4 == 0 && (uintptr_t)basis % 16 == 0) {
       chunk = ceil_div(ceil_div(n, nb), 128) * 128;
@@ -645,6 +693,16 @@ static int lanczos_t(const colagb_op* A, const T* V0, int64_t ldv0, int64_t bs, 
         nb1 = (int)ceil_div(n, chunk);
         COLAGB_CUDA(cudaFuncSetAttribute(k_lz_project1, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)(chunk * sizeof(float))));
+      }
+    } else if (bs >= 4 && bs <= 128 && (bs & (bs - 1)) == 0 && (uintptr_t)basis % 16 == 0) {
+      // rows per block so that a block's run is a whole number of 128-float warp steps
+      const int64_t rstep = 128 / bs;
+      chunk = ceil_div(ceil_div(n, nb), rstep) * rstep;
+      if (chunk * bs * (int64_t)sizeof(float) <= 160 * 1024) {
+        pq = true;
+        nb1 = (int)ceil_div(n, chunk);
+        COLAGB_CUDA(cudaFuncSetAttribute(k_lz_projectq, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(chunk * bs * sizeof(float))));
       }
     }
   }
@@ -666,13 +724,15 @@ static int lanczos_t(const colagb_op* A, const T* V0, int64_t ldv0, int64_t bs, 
         if constexpr (std::is_same<T, float>::value) {
           if (p1)
             k_lz_project1<<<nb1, 256, chunk * sizeof(float), st>>>(basis, w, n, chunk, slots, s);
+          else if (pq)
+            k_lz_projectq<<<nb1, 256, chunk * bs * sizeof(float), st>>>(basis, w, n, bs, chunk, slots, s);
           else
             k_lz_project<T><<<nb, 256, 0, st>>>(basis, w, n, bs, slots, s);
         } else {
           k_lz_project<T><<<nb, 256, 0, st>>>(basis, w, n, bs, slots, s);
         }
         k_lz_reduce_h<T><<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div((int64_t)(i + 1) * bs, 8), 4096)),
-                           256, 0, st>>>(p1 ? nb1 : nb, bs, slots, s);
+                           256, 0, st>>>((p1 || pq) ? nb1 : nb, bs, slots, s);
         k_lz_subtract<T><<<eg, 256, 0, st>>>(basis, w, n, bs, s);
       }
       k_lz_finish<T><<<nb, 256, 0, st>>>(w, n, bs, subdiag, m, prm.tol, s);

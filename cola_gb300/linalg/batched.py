@@ -76,12 +76,20 @@ class BatchedCSR:
         return torch.stack(out)
 
 
-def solve_dense_batched(matrices, rhs, tol: float = 1e-6, max_iters: int = 1000):
+def solve_dense_batched(matrices, rhs, tol: float = 1e-6, max_iters: int = 1000, refine: bool = False,
+                        inner_tol: float = 1e-3, max_sweeps: int = 30):
     """Independent dense SPD systems of uneven sizes, all solved by FP32 CG in one persistent launch.
 
     Each system reproduces ``cola.linalg.solve(PSD(Dense(A_s)), b_s, CG(tol, max_iters))`` with its
     own stop test (cg.py:94-154).  ``matrices``: list of (n_s, n_s) CUDA tensors; ``rhs``: list of
-    (n_s,) tensors.  Returns (list of solutions, per-system iterations, per-system status)."""
+    (n_s,) tensors.  Returns (list of solutions, per-system iterations, per-system status).
+
+    ``refine=True`` adds FP64 iterative refinement, which the reference does not have: the solution
+    accumulates in FP64, the residual b - A x is recomputed in FP64 after every FP32 CG pass (each pass
+    to a relative ``inner_tol`` of the current residual, at most ``max_iters`` steps) and a system stops
+    once its FP64 true relative residual is <= tol.  Ill-conditioned systems (the RBF K + s^2 I with
+    s^2 ~ 1e-3) then reach the requested residual that FP32 CG alone stagnates above.  Solutions are
+    then FP64 and the iteration counts are summed over the passes."""
     if len(matrices) != len(rhs):
         raise ValueError("one right-hand side per matrix")
     S = len(matrices)
@@ -99,24 +107,61 @@ def solve_dense_batched(matrices, rhs, tol: float = 1e-6, max_iters: int = 1000)
         a_off.append(a_off[-1] + n * n)
         v_off.append(v_off[-1] + n)
     vals = torch.cat([A.to(torch.float32).reshape(-1) for A in matrices])
-    B = torch.cat([b.to(torch.float32).reshape(-1) for b in rhs])
-    X = torch.empty_like(B)
-    total = int(B.numel())
+    total = sum(sizes)
     t_sizes = torch.tensor(sizes, dtype=torch.int32, device=dev)
     t_aoff = torch.tensor(a_off, dtype=torch.int64, device=dev)
     t_voff = torch.tensor(v_off, dtype=torch.int64, device=dev)
-    iters = torch.zeros(S, dtype=torch.int32, device=dev)
-    status = torch.zeros(S, dtype=torch.int32, device=dev)
     lib = _capi.load()
     nbytes = C.c_size_t()
     _capi.check(lib.colagb_cg_dense_batched_workspace_bytes(S, total, C.byref(nbytes)), "dense batched cg")
     ws = _capi.workspace(nbytes.value, dev)
-    _capi.check(lib.colagb_cg_dense_batched_solve(S, t_sizes.data_ptr(), t_aoff.data_ptr(), t_voff.data_ptr(), total,
-                                                  vals.data_ptr(), B.data_ptr(), X.data_ptr(), float(tol),
-                                                  int(max_iters), iters.data_ptr(), status.data_ptr(), ws.data_ptr(),
-                                                  nbytes.value, _capi.stream_ptr(dev)), "dense batched cg")
-    sols = list(torch.split(X, sizes))
-    return sols, iters, status
+
+    def fp32_pass(B32, tol_pass):
+        X = torch.empty_like(B32)
+        iters = torch.zeros(S, dtype=torch.int32, device=dev)
+        status = torch.zeros(S, dtype=torch.int32, device=dev)
+        _capi.check(lib.colagb_cg_dense_batched_solve(S, t_sizes.data_ptr(), t_aoff.data_ptr(), t_voff.data_ptr(),
+                                                      total, vals.data_ptr(), B32.data_ptr(), X.data_ptr(),
+                                                      float(tol_pass), int(max_iters), iters.data_ptr(),
+                                                      status.data_ptr(), ws.data_ptr(), nbytes.value,
+                                                      _capi.stream_ptr(dev)), "dense batched cg")
+        return X, iters, status
+
+    if not refine:
+        B = torch.cat([b.to(torch.float32).reshape(-1) for b in rhs])
+        X, iters, status = fp32_pass(B, tol)
+        return list(torch.split(X, sizes)), iters, status
+    B64 = torch.cat([b.to(torch.float64).reshape(-1) for b in rhs])
+    X64 = torch.zeros_like(B64)
+    R64 = torch.empty_like(B64)
+    rr = torch.zeros(S, dtype=torch.float64, device=dev)
+    seg = torch.repeat_interleave(torch.arange(S, device=dev), torch.tensor(sizes, device=dev))
+    bn = torch.zeros(S, dtype=torch.float64, device=dev).index_add_(0, seg, B64 * B64).sqrt()
+    iters = torch.zeros(S, dtype=torch.int32, device=dev)
+    status = torch.full((S,), 2, dtype=torch.int32, device=dev)  # COLAGB_SYS_MAX_ITERS until converged
+
+    def residual():
+        _capi.check(lib.colagb_dense_batched_residual64(S, t_sizes.data_ptr(), t_aoff.data_ptr(), t_voff.data_ptr(),
+                                                        total, vals.data_ptr(), B64.data_ptr(), X64.data_ptr(),
+                                                        R64.data_ptr(), rr.data_ptr(), _capi.stream_ptr(dev)),
+                    "dense residual")
+        return rr.sqrt() / bn.clamp_min(1e-300)
+
+    relres = residual()
+    for _ in range(max_sweeps):
+        done = (relres <= tol) | (bn == 0)
+        status = torch.where(done, torch.ones_like(status), status)
+        if bool(done.all()):
+            break
+        # converged systems get a zero right-hand side: the FP32 pass leaves them at once
+        R32 = torch.where(done[seg], torch.zeros_like(R64), R64).to(torch.float32)
+        D, it, _ = fp32_pass(R32, inner_tol)
+        iters += torch.where(done, torch.zeros_like(it), it)
+        X64 += D.to(torch.float64)
+        relres = residual()
+    done = (relres <= tol) | (bn == 0)
+    status = torch.where(done, torch.ones_like(status), status)
+    return list(torch.split(X64, sizes)), iters, status
 
 
 class FsaiPattern:

@@ -3,9 +3,18 @@
 A three-layer 3x3 convolutional network (6 -> 16 -> 16 -> 3 channels, ReLU) reads scale-free
 features of each operator's coefficients and outputs per-cell scalings of the closed-form FSAI
 factor G on the operator's lower pattern; the CG preconditioner is P = G^T G (it plugs into the
-CG(P=...) hook, cola/linalg/inverse/cg.py:124, 150).  The last layer starts at zero, so an
-untrained network reproduces closed-form FSAI; Jacobi-PCG stays the fallback and the FP64 true
-residual the judge (colagb_cg_batched_csr_solve).
+CG(P=...) hook, cola/linalg/inverse/cg.py:124, 150 -- see ``learned_preconditioner``).  The last
+layer starts at zero, so an untrained network reproduces closed-form FSAI; Jacobi-PCG stays the
+fallback and the FP64 true residual the judge (colagb_cg_batched_csr_solve).
+
+What the shipped weights are, in plain words: the network's last layer is zero and its bias is the
+constant (0, atanh 0.9, atanh 0.775), a global over-relaxation of the two off-diagonals of G found
+by direct search on PCG iteration counts.  Gradient training with this project's kernels lowered
+its losses but not the iteration count, and no per-cell or per-operator output has beaten the
+constant: choosing the best over-relaxation separately for each operator saves at most 1.0 % of
+the iterations on 128 training instances (train_fsai --headroom), about the run-to-run spread of
+FP32 CG step counts.  With this 3-entry factor pattern there is nothing left for a prediction to
+gain, so the "learned" factor is a fitted constant on top of closed-form FSAI (4-5 % fewer steps).
 
 Every forward, backward, loss and optimiser step runs in libcolagb kernels
 (colagb_conv3x3_forward/backward, colagb_fsai_*, colagb_adam_step); torch only holds memory.

@@ -277,6 +277,14 @@ int colagb_cg_dense_batched_solve(int64_t num_systems, const int32_t* sizes, con
                                   const int64_t* v_offsets, int64_t total_rows, const float* values, const float* B,
                                   float* X, double tol, int32_t max_iters, int32_t* per_system_iters,
                                   int32_t* per_system_status, void* workspace, size_t workspace_bytes, void* stream);
+/* No reference counterpart (the reference's FP32 CG stops at its FP32 recursive residual): the FP64
+ * residual R = B - A X of the same uneven batch (FP32 matrices, FP64 B, X, R) and |R_s|^2 per system
+ * into rr (num_systems doubles) -- the outer step of iterative refinement around
+ * colagb_cg_dense_batched_solve, which lets ill-conditioned systems reach a true residual that FP32
+ * CG alone stagnates above. */
+int colagb_dense_batched_residual64(int64_t num_systems, const int32_t* sizes, const int64_t* a_offsets,
+                                    const int64_t* v_offsets, int64_t total_rows, const float* values, const double* B,
+                                    const double* X, double* R, double* rr, void* stream);
 
 /* ======================================================================== *
  *  Lanczos with full reorthogonalisation                                   *
