@@ -130,6 +130,7 @@ SIGNATURES = {
     "colagb_adam_step": (C.c_int, [_vp, _vp, _vp, _vp, _i64, C.c_float, C.c_float, C.c_float, C.c_float, _i32,
                                    _vp]),
     "colagb_read_bandwidth_probe": (C.c_int, [_vp, _sz, _i32, _vp, _vp]),
+    "colagb_matmat_vjp": (C.c_int, [_vp, _vp, _i64, _vp, _i64, _i64, _d, _vp, _vp]),
 }
 
 _lib = None

@@ -8,9 +8,10 @@
   iterations (slq_bwd, cola/linalg/tbd/slq.py:10-31; like the reference, this rule is that of
   f = log).
 
-The vector-Jacobian products go through ``torch_matmat``, a differentiable tensor-op restatement
-of the operator tree's matvec (Dense, Sparse, Diagonal, ScalarMul, Identity, Sum, Product,
-Kronecker, BlockDiag); it only runs in backward passes.
+The vector-Jacobian products with respect to the operator's tensors run in the library's kernels
+(``colagb_matmat_vjp``) for Dense / Sparse / Diagonal leaves under Sum / ScalarMul / Identity; for
+Product, Kronecker and BlockDiag trees they go through ``torch_matmat``, a differentiable tensor-op
+restatement of the operator tree's matvec, which only runs in backward passes.
 """
 from __future__ import annotations
 
@@ -96,10 +97,48 @@ def torch_matmat(A: O.LinearOperator, X: torch.Tensor, sub: dict | None = None) 
     raise NotImplementedError(f"no differentiable matvec for {type(A).__name__}")
 
 
+def _vjp_params_device(A, tensors, X, dual):
+    """The same gradients from the library's VJP kernels (colagb_matmat_vjp: Dense / Sparse / Diagonal
+    leaves in the compute type under Sum / ScalarMul / Identity), or None where the tree needs the
+    tensor-op restatement."""
+    import ctypes as C
+    from .. import _capi
+    from ..lowering import lower
+    try:
+        low = lower(A)
+    except NotImplementedError:
+        return None
+    dt = low.compute_dtype
+    want = {id(p): p for p in tensors}
+    grads = {}
+    ptrs = (C.c_void_p * len(low.nodes))()
+    for node, t in low.leaf_tensors.items():
+        if id(t) in want:
+            if t.dtype != dt or not t.is_cuda:
+                return None
+            if id(t) not in grads:
+                grads[id(t)] = torch.zeros(t.shape, dtype=dt, device=t.device)
+            ptrs[node] = grads[id(t)].data_ptr()
+    Xc = X.detach().to(dt).contiguous()
+    Gc = dual.detach().to(dt).contiguous()
+    k = Xc.shape[1]
+    st = _capi.load().colagb_matmat_vjp(low.handle, Xc.data_ptr(), k, Gc.data_ptr(), k, k, 1.0, ptrs,
+                                        _capi.stream_ptr(Xc.device))
+    if st == _capi.ERR_UNSUPPORTED:
+        return None
+    _capi.check(st, "matmat vjp")
+    return [grads.get(id(p)) if id(p) in grads else torch.zeros_like(p) for p in tensors]
+
+
 def _vjp_params(A, tensors, X, dual):
-    """Gradients of sum(dual * (A(theta) @ X)) with respect to `tensors`."""
+    """Gradients of sum(dual * (A(theta) @ X)) with respect to `tensors`: on the device by the library's
+    VJP kernels where the operator tree allows, else through the tensor-op restatement."""
     if not tensors:
         return []
+    if X.is_cuda:
+        g = _vjp_params_device(A, tensors, X, dual)
+        if g is not None:
+            return [gi.to(p.dtype) for gi, p in zip(g, tensors)]
     with torch.enable_grad():
         copies = [p.detach().requires_grad_(True) for p in tensors]
         sub = {id(p): c for p, c in zip(tensors, copies)}

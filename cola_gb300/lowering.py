@@ -22,6 +22,7 @@ class Lowered:
 
     def __init__(self, op: O.LinearOperator):
         self.nodes: list[_capi.OpNode] = []
+        self.leaf_tensors: dict[int, torch.Tensor] = {}  # node index -> the operator tensor it reads
         self._keep: list = []
         self.device: torch.device | None = None
         self.any64 = False
@@ -83,11 +84,13 @@ class Lowered:
                 A = A.contiguous()
             self._keep.append(A)
             self._dev(A)
+            self.leaf_tensors[len(self.nodes)] = op.A
             return self._add(kind=_capi.OP_DENSE, dtype=self._leaf_dtype(A), rows=rows, cols=cols, data=A.data_ptr(),
                              ld=A.stride(0) if A.shape[0] > 0 else cols)
         if isinstance(op, O.Sparse):
             self._keep += [op.indptr, op.indices, op.values]
             self._dev(op.values)
+            self.leaf_tensors[len(self.nodes)] = op.values
             return self._add(kind=_capi.OP_CSR, dtype=self._leaf_dtype(op.values), rows=rows, cols=cols,
                              data=op.values.data_ptr(), indptr=op.indptr.data_ptr(), indices=op.indices.data_ptr(),
                              nnz=op.nnz)
@@ -95,6 +98,7 @@ class Lowered:
             d = op.diag.contiguous()
             self._keep.append(d)
             self._dev(d)
+            self.leaf_tensors[len(self.nodes)] = op.diag
             return self._add(kind=_capi.OP_DIAG, dtype=self._leaf_dtype(d), rows=rows, cols=cols, data=d.data_ptr())
         if isinstance(op, O.ScalarMul):
             return self._add(kind=_capi.OP_SCALAR, rows=rows, cols=cols, scalar=float(op.c))

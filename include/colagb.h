@@ -110,6 +110,16 @@ int colagb_matmat_workspace_bytes(const colagb_op* op, int64_t k, size_t* bytes)
 int colagb_matmat(const colagb_op* op, const void* X, int64_t ldx, void* Y, int64_t ldy, int64_t k,
                   double alpha, double beta, void* workspace, size_t workspace_bytes, void* stream);
 
+/* Gradients with respect to the operator's own arrays: for Y = op(theta) X and a cotangent G
+ * (rows x k, compute type), node_grads[i] += alpha * d<G, op(theta) X>/d data_i for every node i whose
+ * node_grads entry (a HOST array of num_nodes device pointers, NULL = skip) is set: Dense (rows x cols,
+ * contiguous), Sparse (nnz values) and Diagonal (rows) leaves stored in the compute type, through Sum /
+ * ScalarMul / Identity compositions.  Product, Kronecker and BlockDiag trees: COLAGB_ERR_UNSUPPORTED.
+ * Replaces the autograd of _matmat that cg_bwd and slq_bwd rely on (cola/linalg/inverse/cg.py:72-86,
+ * cola/linalg/tbd/slq.py:10-31). */
+int colagb_matmat_vjp(const colagb_op* op, const void* X, int64_t ldx, const void* G, int64_t ldg, int64_t k,
+                      double alpha, void* const* node_grads, void* stream);
+
 /* ======================================================================== *
  *  Conjugate gradients                                                     *
  *  Replaces cg() / run_batched_cg() / take_cg_step()                       *
