@@ -690,7 +690,7 @@ static BatchedWs carve_batched(Bump& ws, const colagb_batched_csr& A, const cola
     w.onchip_bytes = 0;
     w.v16 = nullptr;
     w.dg16 = nullptr;
-    const size_t bb = block_workspace_bytes(A.n, A.num_systems, num_sms() * 2);
+    const size_t bb = block_workspace_bytes(A.n, A.num_systems, num_sms() * 4);
     w.block = ws.take<char>(bb);
     w.block_bytes = bb;
     return w;

@@ -107,7 +107,9 @@ __device__ __forceinline__ void grid_totals_d(const double* pd, int nb, int64_t 
   }
 }
 
-__global__ void __launch_bounds__(kBT) k_block_ir(const BlockArgs a) {
+// Four CTAs per SM (64 registers, no spills): the SpMM phase is latency-bound on index -> p-row
+// gathers, and at two CTAs per SM (124 registers) only a quarter of the warp slots were occupied.
+__global__ void __launch_bounds__(kBT, 4) k_block_ir(const BlockArgs a) {
   __shared__ float4 red[kBT];
   __shared__ double tmpd[kBT];
   __shared__ float tmpf[kBT];
@@ -391,7 +393,7 @@ int block_grid_blocks() {
     cudaGetLastError();
     return 0;
   }
-  return num_sms() * (occ < 2 ? occ : 2);
+  return num_sms() * (occ < 4 ? occ : 4);
 }
 
 // One shared-matrix block of up to kBMaxK right-hand sides (B, X: (S, n) FP64).
