@@ -562,7 +562,15 @@ def reference_package():
         if pth not in sys.path:
             sys.path.insert(0, pth)
     import importlib.util
-    if importlib.util.find_spec("tqdm") is None:
+
+    def _have(name):
+        if name in sys.modules:  # includes the stand-in below, registered by an earlier call
+            return True
+        try:
+            return importlib.util.find_spec(name) is not None
+        except (ImportError, ValueError):
+            return False
+    if not _have("tqdm"):
         import types
 
         class _Bar:
