@@ -115,6 +115,7 @@ SIGNATURES = {
                                  _vp]),
     "colagb_basis_combine": (C.c_int, [_vp, _i64, _i64, _i32, _vp, _i64, _vp, _i32, _vp]),
     "colagb_tridiag_eig_f64": (C.c_int, [_vp, _vp, _i64, _i64, _vp, _vp, _vp, _vp, _vp]),
+    "colagb_tridiag_eig_f32": (C.c_int, [_vp, _vp, _i64, _i64, _vp, _vp, _vp, _vp, _vp]),
     "colagb_grid5_stencil": (C.c_int, [_vp, _vp, _vp, _i64, _i64, _i64, _vp, _vp, _vp]),
     "colagb_fsai_features": (C.c_int, [_vp, _i64, _i64, _vp, _vp]),
     "colagb_fsai_assemble": (C.c_int, [_vp, _vp, _i64, _i64, _vp, _vp]),

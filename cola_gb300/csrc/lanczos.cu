@@ -1,4 +1,4 @@
-// Lanczos with full reorthogonalisation and the FP64 tridiagonal eigensolver.
+// Lanczos with full reorthogonalisation and the tridiagonal eigensolver (FP64, or FP32 for FP32 recurrences).
 //
 // Reference (cola/linalg/decompositions/lanczos.py):
 //   init_lanczos :275-284   V[..., 1] = rhs / |rhs|, i = 1
@@ -435,40 +435,99 @@ __global__ void k_basis_combine(const T* basis, int64_t n, int64_t bs, int m, co
 }
 
 // ---------------------------------------------------------------------------------------------
-// FP64 symmetric tridiagonal eigensolver: implicit QL with Wilkinson shifts, one CTA per matrix.
-// Thread 0 runs the scalar recurrence; each QL sweep's Givens rotations are recorded in shared
-// memory and then applied by all threads to their own rows of the eigenvector matrix (rows are
+// Symmetric tridiagonal eigensolver (batched): implicit QL with Wilkinson shifts, one CTA per
+// matrix, in R = double or float.  The matrix is first scaled by a power of two (exact) so that its
+// largest entry lies in [0.5, 1): the sweep below forms squares without overflow checks in either
+// precision.  Thread 0 runs the scalar recurrence; each QL sweep's Givens rotations are recorded in
+// shared memory and then applied by all threads to their own rows of the eigenvector matrix (rows are
 // independent under column rotations).  Row 0 alone (Gauss weights) is tracked by thread 0.
 // `rec` (optional, with evecs == nullptr): every Givens rotation (c, s) on columns (i, i+1) is
 // appended in generation order to rec[sys * cap ...] / rec_i, the count to rec_n[sys] (-1 when cap
 // was exceeded), and the sorting permutation to rec_perm[sys * m ...]; k_tridiag_apply replays them.
-__global__ void k_tridiag_ql(const double* A, const double* Bv, int64_t m, double* evals, double* first_row,
-                             double* evecs, int32_t* status, double2* rec = nullptr, int32_t* rec_i = nullptr,
+template <class R> struct TriTraits;
+template <> struct TriTraits<double> {
+  using R2 = double2;
+  static constexpr double eps = 2.220446049250313e-16;
+  __device__ static double rsq(double x) { return rsqrt(x); }
+  __device__ static double hyp(double a, double b) { return hypot(a, b); }
+  __device__ static double2 pack(double c, double s) { return make_double2(c, s); }
+  __device__ static double ab(double x) { return fabs(x); }
+  __device__ static double mx(double x, double y) { return fmax(x, y); }
+  __device__ static double fm(double x, double y, double z) { return fma(x, y, z); }
+  __device__ static double fr(double x, int* ex) { return frexp(x, ex); }
+  __device__ static double ld(double x, int ex) { return ldexp(x, ex); }
+};
+template <> struct TriTraits<float> {
+  using R2 = float2;
+  static constexpr float eps = 1.1920928955078125e-7f;
+  __device__ static float rsq(float x) { return rsqrtf(x); }
+  __device__ static float hyp(float a, float b) { return hypotf(a, b); }
+  __device__ static float2 pack(float c, float s) { return make_float2(c, s); }
+  __device__ static float ab(float x) { return fabsf(x); }
+  __device__ static float mx(float x, float y) { return fmaxf(x, y); }
+  __device__ static float fm(float x, float y, float z) { return fmaf(x, y, z); }
+  __device__ static float fr(float x, int* ex) { return frexpf(x, ex); }
+  __device__ static float ld(float x, int ex) { return ldexpf(x, ex); }
+};
+
+// Strict total order for the eigenvalue sort: ascending, NaN last, ties by index.
+template <class R>
+__device__ inline bool tri_before(R x, int64_t i, R y, int64_t j) {
+  const bool nx = isnan(x), ny = isnan(y);
+  if (nx != ny) return ny;
+  if (!nx && x != y) return x < y;
+  return i < j;
+}
+
+template <class R>
+__global__ void k_tridiag_ql(const R* A, const R* Bv, int64_t m, R* evals, R* first_row, R* evecs,
+                             int32_t* status, typename TriTraits<R>::R2* rec = nullptr, int32_t* rec_i = nullptr,
                              int32_t* rec_n = nullptr, int32_t* rec_perm = nullptr, int64_t cap = 0) {
-  extern __shared__ double sm[];
-  double* d = sm;              // m
-  double* e = d + m;           // m
-  double* z0 = e + m;          // m (row 0 of Z)
-  double* rc = z0 + m;         // m rotation cosines
-  double* rs = rc + m;         // m rotation sines
+  using TT = TriTraits<R>;
+  extern __shared__ __align__(16) unsigned char tri_smem[];
+  R* d = reinterpret_cast<R*>(tri_smem);  // m
+  R* e = d + m;                           // m
+  R* z0 = e + m;                          // m (row 0 of Z)
+  R* rc = z0 + m;                         // m rotation cosines
+  R* rs = rc + m;                         // m rotation sines
   int* perm = reinterpret_cast<int*>(rs + m);  // m
   __shared__ int s_cmd, s_lo, s_hi, s_fail;
+  __shared__ R s_amax[32];
   const int64_t sys = blockIdx.x;
-  const double* a = A + sys * m;
-  const double* b = Bv + sys * m;
-  double* Z = evecs ? evecs + sys * m * m : nullptr;
+  const R* a = A + sys * m;
+  const R* b = Bv + sys * m;
+  R* Z = evecs ? evecs + sys * m * m : nullptr;
+  R amax = R(0);
   for (int64_t i = threadIdx.x; i < m; i += blockDim.x) {
-    d[i] = a[i];
-    e[i] = (i + 1 < m) ? b[i] : 0.0;
-    z0[i] = (i == 0) ? 1.0 : 0.0;
+    const R ai = a[i], bi = (i + 1 < m) ? b[i] : R(0);
+    amax = TT::mx(amax, TT::mx(TT::ab(ai), TT::ab(bi)));
+  }
+  for (int o = 16; o > 0; o >>= 1) amax = TT::mx(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+  if ((threadIdx.x & 31) == 0) s_amax[threadIdx.x >> 5] = amax;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    R t = R(0);
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t = TT::mx(t, s_amax[w]);
+    s_amax[0] = t;
+    s_fail = 0;
+  }
+  __syncthreads();
+  // 2^-e with amax = f * 2^e, f in [0.5, 1): exact scaling, undone on the eigenvalues
+  int ex = 0;
+  const R amx = s_amax[0];
+  if (amx > R(0) && isfinite(amx)) TT::fr(amx, &ex);
+  const R scale = TT::ld(R(1), -ex), unscale = TT::ld(R(1), ex);
+  for (int64_t i = threadIdx.x; i < m; i += blockDim.x) {
+    d[i] = a[i] * scale;
+    e[i] = (i + 1 < m) ? b[i] * scale : R(0);
+    z0[i] = (i == 0) ? R(1) : R(0);
   }
   if (Z)
-    for (int64_t u = threadIdx.x; u < m * m; u += blockDim.x) Z[u] = (u / m == u % m) ? 1.0 : 0.0;
-  if (threadIdx.x == 0) s_fail = 0;
+    for (int64_t u = threadIdx.x; u < m * m; u += blockDim.x) Z[u] = (u / m == u % m) ? R(1) : R(0);
   __syncthreads();
   int l = 0, iter = 0;
   int64_t nrec = 0;
-  double2* my_rec = rec ? rec + sys * cap : nullptr;
+  typename TT::R2* my_rec = rec ? rec + sys * cap : nullptr;
   int32_t* my_rec_i = rec ? rec_i + sys * cap : nullptr;
   while (true) {
     // thread 0: one QL sweep (or decide to move on)
@@ -477,41 +536,41 @@ __global__ void k_tridiag_ql(const double* A, const double* Bv, int64_t m, doubl
       while (l < m) {
         int mm = l;
         for (; mm < m - 1; ++mm) {
-          const double dd = fabs(d[mm]) + fabs(d[mm + 1]);
-          if (fabs(e[mm]) <= 2.220446049250313e-16 * dd) break;
+          const R dd = TT::ab(d[mm]) + TT::ab(d[mm + 1]);
+          if (TT::ab(e[mm]) <= TT::eps * dd) break;
         }
         if (mm == l) { ++l; iter = 0; continue; }
         if (iter++ >= 60) { s_fail = 1; ++l; iter = 0; continue; }
-        double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
-        double r = hypot(g, 1.0);
-        g = d[mm] - d[l] + e[l] / (g + (g >= 0.0 ? fabs(r) : -fabs(r)));
-        double s = 1.0, c = 1.0, p = 0.0;
+        R g = (d[l + 1] - d[l]) / (R(2) * e[l]);
+        R r = TT::hyp(g, R(1));
+        g = d[mm] - d[l] + e[l] / (g + (g >= R(0) ? TT::ab(r) : -TT::ab(r)));
+        R s = R(1), c = R(1), p = R(0);
         int i = mm - 1;
         bool underflow = false;
         // The sweep is one dependent chain on this thread: the operands of step i - 1 (e[i-1], d[i-1],
         // z0[i-1]), which step i does not modify, are loaded ahead, d[i] / z0[i] are carried in
         // registers, and each rotation takes one reciprocal square root instead of a hypot and two
-        // divisions (|f|, |g| stay far inside the FP64 range here).
-        double ei = e[i], di1 = d[i + 1], di = d[i], zi1 = z0[i + 1];
+        // divisions (|f|, |g| are bounded by a small multiple of the scaled matrix's norm).
+        R ei = e[i], di1 = d[i + 1], di = d[i], zi1 = z0[i + 1];
         for (; i >= l; --i) {
-          const double e_nx = i > l ? e[i - 1] : 0.0;
-          const double d_nx = i > l ? d[i - 1] : 0.0;
-          const double zi = z0[i];
-          const double f = s * ei, bb = c * ei;
-          const double q = fma(f, f, g * g);
-          if (q == 0.0) {
-            e[i + 1] = 0.0;
+          const R e_nx = i > l ? e[i - 1] : R(0);
+          const R d_nx = i > l ? d[i - 1] : R(0);
+          const R zi = z0[i];
+          const R f = s * ei, bb = c * ei;
+          const R q = TT::fm(f, f, g * g);
+          if (q == R(0)) {
+            e[i + 1] = R(0);
             d[i + 1] = di1 - p;
-            e[mm] = 0.0;
+            e[mm] = R(0);
             underflow = true;
             break;
           }
-          const double ri = rsqrt(q);
+          const R ri = TT::rsq(q);
           e[i + 1] = q * ri;
           s = f * ri;
           c = g * ri;
           g = di1 - p;
-          r = (di - g) * s + 2.0 * c * bb;
+          r = (di - g) * s + R(2) * c * bb;
           p = s * r;
           d[i + 1] = g + p;
           g = c * r - bb;
@@ -519,13 +578,13 @@ __global__ void k_tridiag_ql(const double* A, const double* Bv, int64_t m, doubl
           rs[i] = s;
           if (my_rec) {
             if (nrec < cap) {
-              my_rec[nrec] = make_double2(c, s);
+              my_rec[nrec] = TT::pack(c, s);
               my_rec_i[nrec] = i;
             }
             ++nrec;
           }
           z0[i + 1] = s * zi + c * zi1;
-          const double zi_new = c * zi - s * zi1;
+          const R zi_new = c * zi - s * zi1;
           z0[i] = zi_new;
           ei = e_nx;
           di1 = di;
@@ -538,7 +597,7 @@ __global__ void k_tridiag_ql(const double* A, const double* Bv, int64_t m, doubl
         } else {
           d[l] -= p;
           e[l] = g;
-          e[mm] = 0.0;
+          e[mm] = R(0);
           s_lo = l;
           s_hi = mm;
         }
@@ -553,10 +612,10 @@ __global__ void k_tridiag_ql(const double* A, const double* Bv, int64_t m, doubl
       // rotations were generated for i = hi-1 down to lo, apply in that order
       const int lo = s_lo, hi = s_hi;
       for (int64_t row = threadIdx.x; row < m; row += blockDim.x) {
-        double* zr = Z + row * m;
+        R* zr = Z + row * m;
         for (int i = hi - 1; i >= lo; --i) {
-          const double c = rc[i], s = rs[i];
-          const double f = zr[i + 1];
+          const R c = rc[i], s = rs[i];
+          const R f = zr[i + 1];
           zr[i + 1] = s * zr[i] + c * f;
           zr[i] = c * zr[i] - s * f;
         }
@@ -566,28 +625,23 @@ __global__ void k_tridiag_ql(const double* A, const double* Bv, int64_t m, doubl
     if (cmd == 2) break;
     if (cmd == 0) break;
   }
-  // sort ascending (selection by thread 0), then permute outputs
-  if (threadIdx.x == 0) {
-    for (int i = 0; i < m; ++i) perm[i] = i;
-    for (int i = 0; i < m; ++i) {
-      int k = i;
-      for (int j = i + 1; j < m; ++j)
-        if (d[perm[j]] < d[perm[k]]) k = j;
-      const int t = perm[i];
-      perm[i] = perm[k];
-      perm[k] = t;
-    }
+  // ascending order by rank (ties by index): every thread ranks its own entries, O(m) each
+  for (int64_t j = threadIdx.x; j < m; j += blockDim.x) {
+    const R dj = d[j];
+    int rank = 0;
+    for (int64_t i = 0; i < m; ++i) rank += tri_before(d[i], i, dj, j);
+    perm[rank] = (int)j;
   }
   __syncthreads();
   for (int64_t j = threadIdx.x; j < m; j += blockDim.x) {
-    evals[sys * m + j] = d[perm[j]];
+    evals[sys * m + j] = d[perm[j]] * unscale;
     if (first_row) first_row[sys * m + j] = Z ? Z[perm[j]] : z0[perm[j]];
     if (rec_perm) rec_perm[sys * m + j] = perm[j];
   }
   if (rec && threadIdx.x == 0) rec_n[sys] = nrec <= cap ? (int32_t)nrec : -1;
   __syncthreads();
   if (Z) {
-    double* tmp = rc;  // reuse as a row buffer
+    R* tmp = rc;  // reuse as a row buffer
     for (int64_t row = 0; row < m; ++row) {
       for (int64_t j = threadIdx.x; j < m; j += blockDim.x) tmp[j] = Z[row * m + perm[j]];
       __syncthreads();
@@ -602,27 +656,30 @@ __global__ void k_tridiag_ql(const double* A, const double* Bv, int64_t m, doubl
 // owns one row (rows are independent), held in shared memory as zs[col][lane] (conflict-free);
 // every rotation acts on columns (i, i+1).  Output columns follow the sorted eigenvalues.
 constexpr int kRotRows = 32;
-__global__ void __launch_bounds__(kRotRows) k_tridiag_apply(const double2* rec, const int32_t* rec_i,
-                                                            const int32_t* rec_n, const int32_t* rec_perm, int64_t m,
-                                                            int64_t cap, double* evecs) {
-  extern __shared__ double zs[];  // m x kRotRows
+template <class R>
+__global__ void __launch_bounds__(kRotRows) k_tridiag_apply(const typename TriTraits<R>::R2* rec,
+                                                            const int32_t* rec_i, const int32_t* rec_n,
+                                                            const int32_t* rec_perm, int64_t m, int64_t cap,
+                                                            R* evecs) {
+  extern __shared__ __align__(16) unsigned char rot_smem[];
+  R* zs = reinterpret_cast<R*>(rot_smem);  // m x kRotRows
   const int64_t sys = blockIdx.y;
   const int t = threadIdx.x;
   const int64_t row = (int64_t)blockIdx.x * kRotRows + t;
   const int32_t nr = rec_n[sys];
   if (nr < 0) return;  // the recording overflowed: the in-kernel path produced Z
-  for (int64_t i = 0; i < m; ++i) zs[i * kRotRows + t] = (row == i) ? 1.0 : 0.0;
-  const double2* r = rec + sys * cap;
+  for (int64_t i = 0; i < m; ++i) zs[i * kRotRows + t] = (row == i) ? R(1) : R(0);
+  const typename TriTraits<R>::R2* r = rec + sys * cap;
   const int32_t* ri = rec_i + sys * cap;
   for (int32_t q = 0; q < nr; ++q) {
-    const double2 cs = r[q];
+    const auto cs = r[q];
     const int i = ri[q];
-    const double zi = zs[i * kRotRows + t], f = zs[(i + 1) * kRotRows + t];
+    const R zi = zs[i * kRotRows + t], f = zs[(i + 1) * kRotRows + t];
     zs[(i + 1) * kRotRows + t] = cs.y * zi + cs.x * f;
     zs[i * kRotRows + t] = cs.x * zi - cs.y * f;
   }
   if (row < m) {
-    double* out = evecs + sys * m * m + row * m;
+    R* out = evecs + sys * m * m + row * m;
     const int32_t* perm = rec_perm + sys * m;
     for (int64_t j = 0; j < m; ++j) out[j] = zs[perm[j] * kRotRows + t];
   }
@@ -914,36 +971,36 @@ extern "C" int colagb_basis_combine(const void* basis, int64_t n, int64_t bs, in
   return COLAGB_OK;
 }
 
-extern "C" int colagb_tridiag_eig_f64(const double* a, const double* b, int64_t m, int64_t batch, double* evals,
-                                      double* first_row, double* evecs, int32_t* status, void* stream) {
-  if (m < 0 || batch < 0 || (m * batch > 0 && (!a || !b || !evals)))
-    return fail(COLAGB_ERR_INVALID, "colagb_tridiag_eig_f64: bad arguments");
+template <class R>
+static int tridiag_eig(const R* a, const R* b, int64_t m, int64_t batch, R* evals, R* first_row, R* evecs,
+                       int32_t* status, cudaStream_t st, const char* name) {
+  using R2 = typename TriTraits<R>::R2;
+  if (m < 0 || batch < 0 || (m * batch > 0 && (!a || !b || !evals))) return fail(COLAGB_ERR_INVALID, name);
   if (m * batch == 0) return COLAGB_OK;
-  const size_t smem = (size_t)m * (5 * sizeof(double) + sizeof(int));
-  if (smem > 200 * 1024) return fail(COLAGB_ERR_INVALID, "colagb_tridiag_eig_f64: m too large (max 4000)");
+  const size_t smem = (size_t)m * (5 * sizeof(R) + sizeof(int));
+  if (smem > 200 * 1024) return fail(COLAGB_ERR_INVALID, "tridiagonal eigensolver: m too large");
   if (smem > 48 * 1024)
-    COLAGB_CUDA(cudaFuncSetAttribute(k_tridiag_ql, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  cudaStream_t st = as_stream(stream);
-  const size_t smem_rot = (size_t)m * kRotRows * sizeof(double);
+    COLAGB_CUDA(cudaFuncSetAttribute(k_tridiag_ql<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const size_t smem_rot = (size_t)m * kRotRows * sizeof(R);
   if (evecs && smem_rot <= 200 * 1024) {
     // eigenvectors: QL records its rotations (one thread generates them serially), then many CTAs
     // replay them on the rows of Z in shared memory; applying them to Z in global memory from the
     // same CTA, row per thread, cost ~95 % of the solve
     const int64_t cap = 6 * m * m + 64;
     void* buf = nullptr;
-    const size_t bytes = (size_t)batch * cap * (sizeof(double2) + sizeof(int32_t)) +
+    const size_t bytes = (size_t)batch * cap * (sizeof(R2) + sizeof(int32_t)) +
                          (size_t)batch * (m + 1) * sizeof(int32_t);
     COLAGB_CUDA(cudaMallocAsync(&buf, bytes, st));
-    double2* rec = static_cast<double2*>(buf);
+    R2* rec = static_cast<R2*>(buf);
     int32_t* rec_i = reinterpret_cast<int32_t*>(rec + batch * cap);
     int32_t* rec_n = rec_i + batch * cap;
     int32_t* rec_perm = rec_n + batch;
-    k_tridiag_ql<<<(unsigned)batch, 128, smem, st>>>(a, b, m, evals, first_row, nullptr, status, rec, rec_i, rec_n,
-                                                     rec_perm, cap);
+    k_tridiag_ql<R><<<(unsigned)batch, 128, smem, st>>>(a, b, m, evals, first_row, nullptr, status, rec, rec_i,
+                                                        rec_n, rec_perm, cap);
     COLAGB_CUDA(cudaGetLastError());
     if (smem_rot > 48 * 1024)
-      COLAGB_CUDA(cudaFuncSetAttribute(k_tridiag_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_rot));
-    k_tridiag_apply<<<dim3((unsigned)ceil_div(m, (int64_t)kRotRows), (unsigned)batch), kRotRows, smem_rot, st>>>(
+      COLAGB_CUDA(cudaFuncSetAttribute(k_tridiag_apply<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_rot));
+    k_tridiag_apply<R><<<dim3((unsigned)ceil_div(m, (int64_t)kRotRows), (unsigned)batch), kRotRows, smem_rot, st>>>(
         rec, rec_i, rec_n, rec_perm, m, cap, evecs);
     COLAGB_CUDA(cudaGetLastError());
     std::vector<int32_t> hn(batch);
@@ -955,9 +1012,21 @@ extern "C" int colagb_tridiag_eig_f64(const double* a, const double* b, int64_t 
     if (!overflow) return COLAGB_OK;
     // rare: more rotations than recorded -- recompute with Z updated inside the QL kernel
   }
-  k_tridiag_ql<<<(unsigned)batch, 128, smem, st>>>(a, b, m, evals, first_row, evecs, status);
+  k_tridiag_ql<R><<<(unsigned)batch, 128, smem, st>>>(a, b, m, evals, first_row, evecs, status);
   COLAGB_CUDA(cudaGetLastError());
   return COLAGB_OK;
+}
+
+extern "C" int colagb_tridiag_eig_f64(const double* a, const double* b, int64_t m, int64_t batch, double* evals,
+                                      double* first_row, double* evecs, int32_t* status, void* stream) {
+  return tridiag_eig<double>(a, b, m, batch, evals, first_row, evecs, status, as_stream(stream),
+                             "colagb_tridiag_eig_f64: bad arguments");
+}
+
+extern "C" int colagb_tridiag_eig_f32(const float* a, const float* b, int64_t m, int64_t batch, float* evals,
+                                      float* first_row, float* evecs, int32_t* status, void* stream) {
+  return tridiag_eig<float>(a, b, m, batch, evals, first_row, evecs, status, as_stream(stream),
+                            "colagb_tridiag_eig_f32: bad arguments");
 }
 
 extern "C" int colagb_arnoldi_workspace_bytes(const colagb_op* A, int64_t bs, int32_t max_iters, size_t* bytes) {

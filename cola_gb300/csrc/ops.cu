@@ -177,6 +177,119 @@ __global__ void __launch_bounds__(256) csr_spmv_kernel(const int32_t* __restrict
   if (row < rows && sub == 0) Y[row * ldy] = combine(acc, alpha, beta, Y + row * ldy);
 }
 
+// CSR, one column, short rows ("CSR-stream"): one warp per group of 32 consecutive rows.  The group's
+// nonzeros are one contiguous span [beg, end) of the index and value arrays: the warp streams it with
+// 128-bit loads (4 entries per lane per pass, two passes in flight), gathers the four x entries of
+// each load independently, and parks the products in shared memory; lane r then sums row r's
+// products in entry order.  A group whose span exceeds the buffer is done row by row, lanes striding
+// over the row.  On a graph with unordered columns the x gathers are scattered L2 sectors; this keeps
+// ~8 of them in flight per lane instead of one dependent index -> x chain per entry.
+constexpr int kStreamWarps = 8;
+template <class T> struct StreamCap { static constexpr int value = 4096 / (int)sizeof(T); };
+
+template <class T, class S> struct Load4;
+template <class T> struct Load4<T, float> {
+  __device__ static void run(const float* p, T v[4]) {
+    const float4 q = __ldg(reinterpret_cast<const float4*>(p));
+    v[0] = T(q.x); v[1] = T(q.y); v[2] = T(q.z); v[3] = T(q.w);
+  }
+};
+template <class T> struct Load4<T, double> {
+  __device__ static void run(const double* p, T v[4]) {
+    const double2 a = __ldg(reinterpret_cast<const double2*>(p)), b = __ldg(reinterpret_cast<const double2*>(p) + 1);
+    v[0] = T(a.x); v[1] = T(a.y); v[2] = T(b.x); v[3] = T(b.y);
+  }
+};
+template <class T> struct Load4<T, __nv_bfloat16> {
+  __device__ static void run(const __nv_bfloat16* p, T v[4]) {
+    const uint2 q = __ldg(reinterpret_cast<const uint2*>(p));
+    const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&q.x));
+    const float2 b = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&q.y));
+    v[0] = T(a.x); v[1] = T(a.y); v[2] = T(b.x); v[3] = T(b.y);
+  }
+};
+
+// entries base .. base+3 (those inside [beg, end)) -> their products val * x[col]; others 0
+template <class T, class S, bool VEC>
+__device__ __forceinline__ void stream_pass(const int32_t* __restrict__ indices, const S* __restrict__ vals,
+                                            int64_t nnz, int32_t beg, int32_t end, int64_t base,
+                                            const T* __restrict__ X, int64_t ldx, T pr[4]) {
+  int32_t id[4];
+  T v[4];
+  if (base >= end) {
+#pragma unroll
+    for (int c = 0; c < 4; ++c) pr[c] = T(0);
+    return;
+  }
+  if (VEC && base + 3 < nnz) {
+    const int4 q = __ldg(reinterpret_cast<const int4*>(indices + base));
+    id[0] = q.x; id[1] = q.y; id[2] = q.z; id[3] = q.w;
+    Load4<T, S>::run(vals + base, v);
+  } else {
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const int64_t e = base + c;
+      const bool ok = e >= beg && e < end;
+      id[c] = ok ? indices[e] : 0;
+      v[c] = ok ? cvt<T>(vals[e]) : T(0);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const int64_t e = base + c;
+    pr[c] = (e >= beg && e < end) ? v[c] * X[(int64_t)id[c] * ldx] : T(0);
+  }
+}
+
+template <class T, class S, bool VEC>
+__global__ void __launch_bounds__(kStreamWarps * 32, sizeof(T) == 4 ? 6 : 4) csr_stream_kernel(
+    const int32_t* __restrict__ indptr, const int32_t* __restrict__ indices, const S* __restrict__ vals,
+    int64_t rows, int64_t nnz, const T* __restrict__ X, int64_t ldx, int64_t bsx, T* __restrict__ Y, int64_t ldy,
+    int64_t bsy, T alpha, T beta, const int* skip) {
+  constexpr int CAP = StreamCap<T>::value;
+  __shared__ T prod[kStreamWarps][CAP];
+  if (skip && *skip) return;
+  const int64_t b = blockIdx.y;
+  X += b * bsx;
+  Y += b * bsy;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t r0 = ((int64_t)blockIdx.x * kStreamWarps + w) * 32;
+  if (r0 >= rows) return;  // the whole warp leaves; nothing below synchronises beyond the warp
+  const int nr = (int)(rows - r0 < 32 ? rows - r0 : 32);
+  const int32_t my_lo = indptr[r0 + (lane < nr ? lane : nr)];
+  const int32_t my_hi = lane < nr ? indptr[r0 + lane + 1] : my_lo;
+  const int32_t beg = __shfl_sync(0xffffffffu, my_lo, 0);
+  const int32_t end = __shfl_sync(0xffffffffu, my_hi, nr - 1);
+  T acc = T(0);
+  if (end - beg <= CAP) {
+    T* pw = prod[w];
+    const int64_t abeg = VEC ? (beg & ~3) : beg;
+    for (int64_t base = abeg + lane * 4; base < end; base += 256) {
+      T p0[4], p1[4];
+      stream_pass<T, S, VEC>(indices, vals, nnz, beg, end, base, X, ldx, p0);
+      stream_pass<T, S, VEC>(indices, vals, nnz, beg, end, base + 128, X, ldx, p1);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const int64_t e0 = base + c, e1 = base + 128 + c;
+        if (e0 >= beg && e0 < end) pw[e0 - beg] = p0[c];
+        if (e1 >= beg && e1 < end) pw[e1 - beg] = p1[c];
+      }
+    }
+    __syncwarp();
+    for (int32_t j = my_lo - beg; j < my_hi - beg; ++j) acc += pw[j];
+  } else {
+    for (int rr = 0; rr < nr; ++rr) {
+      const int32_t lo = __shfl_sync(0xffffffffu, my_lo, rr), hi = __shfl_sync(0xffffffffu, my_hi, rr);
+      T sum = T(0);
+      for (int32_t j = lo + lane; j < hi; j += 32) sum += cvt<T>(vals[j]) * X[(int64_t)indices[j] * ldx];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+      if (lane == rr) acc = sum;
+    }
+  }
+  if (lane < nr) Y[(r0 + lane) * ldy] = combine(acc, alpha, beta, Y + (r0 + lane) * ldy);
+}
+
 // CSR, k columns: one warp per row, lanes over 32-column chunks; each entry reads a contiguous
 // row segment of X (coalesced).
 template <class T, class S>
@@ -289,8 +402,29 @@ static int launch_csr(const colagb_op_node& nd, const T* X, int64_t ldx, int64_t
                       int64_t bsy, int64_t k, int64_t batch, T alpha, T beta, const int* skip, cudaStream_t st) {
   const S* v = static_cast<const S*>(nd.data);
   if (nd.rows == 0 || k == 0) return COLAGB_OK;
-  if (k == 1) {
-    const double avg = nd.rows > 0 ? (double)nd.nnz / (double)nd.rows : 0.0;
+  const double avg = nd.rows > 0 ? (double)nd.nnz / (double)nd.rows : 0.0;
+  if (k == 1 && avg <= StreamCap<T>::value / 48.0) {
+    // short rows: the streaming kernel (most 32-row groups fit its per-warp buffer)
+    const bool vec = (reinterpret_cast<uintptr_t>(nd.indices) % 16 == 0) &&
+                     (reinterpret_cast<uintptr_t>(v) % (sizeof(S) * 4 < 16 ? sizeof(S) * 4 : 16) == 0);
+    dim3 grid((unsigned)ceil_div(nd.rows, (int64_t)kStreamWarps * 32), (unsigned)batch);
+    // the whole L1 as shared memory (L1 hits are rare here): the 32 KB per CTA then limits
+    // residency no more than the registers do
+    static const bool carved = [] {
+      cudaFuncSetAttribute(csr_stream_kernel<T, S, true>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                           (int)cudaSharedmemCarveoutMaxShared);
+      cudaFuncSetAttribute(csr_stream_kernel<T, S, false>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                           (int)cudaSharedmemCarveoutMaxShared);
+      return true;
+    }();
+    (void)carved;
+    if (vec)
+      csr_stream_kernel<T, S, true><<<grid, kStreamWarps * 32, 0, st>>>(nd.indptr, nd.indices, v, nd.rows, nd.nnz, X,
+                                                                         ldx, bsx, Y, ldy, bsy, alpha, beta, skip);
+    else
+      csr_stream_kernel<T, S, false><<<grid, kStreamWarps * 32, 0, st>>>(nd.indptr, nd.indices, v, nd.rows, nd.nnz,
+                                                                          X, ldx, bsx, Y, ldy, bsy, alpha, beta, skip);
+  } else if (k == 1) {
     int tpr = 1;
     while (tpr < 32 && tpr * 2 <= avg) tpr *= 2;
     dim3 grid((unsigned)ceil_div(nd.rows * tpr, 256), (unsigned)batch);

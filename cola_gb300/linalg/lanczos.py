@@ -1,8 +1,8 @@
 """Lanczos, Lanczos eigensolver, eig (cola/linalg/decompositions/lanczos.py:34-61, 185-232,
-cola/linalg/eig/eigs.py:76-111) and the FP64 tridiagonal eigensolver.
+cola/linalg/eig/eigs.py:76-111) and the tridiagonal eigensolver.
 
 The Lanczos loop (with full CGS2 reorthogonalisation) runs in libcolagb (colagb_lanczos); the
-tridiagonal eigenproblems are solved in FP64 on the GPU (colagb_tridiag_eig_f64) where the
+tridiagonal eigenproblems are solved on the GPU (colagb_tridiag_eig_f64 / _f32) where the
 reference calls eigh in the operator dtype.
 """
 from __future__ import annotations
@@ -114,25 +114,29 @@ def lanczos(A: O.LinearOperator, start_vector=None, max_iters=100, tol=1e-7, pba
 
 
 def tridiag_eigh(beta: torch.Tensor, alpha: torch.Tensor, want_vectors: bool = True):
-    """Eigen-decomposition of symmetric tridiagonals in FP64 on the GPU.
+    """Eigen-decomposition of symmetric tridiagonals on the GPU, in the precision of the recurrence
+    that produced them: FP32 tridiagonals (from FP32 / BF16 operators) are solved in FP32, like the
+    reference's eigh of the FP32 T (lanczos.py:57, unary.py:52), everything else in FP64.
 
     beta: (batch, m) diagonals, alpha: (batch, m-1) off-diagonals.  Returns (evals (batch, m)
-    ascending, evecs (batch, m, m) or first-row weights (batch, m))."""
+    ascending, evecs (batch, m, m) or first-row weights (batch, m), status)."""
     lib = _capi.load()
     dev = beta.device
     _capi.require_cuda(beta)
     bsz, m = beta.shape
-    a = beta.to(torch.float64).contiguous()
-    b = torch.zeros((bsz, m), dtype=torch.float64, device=dev)
+    dt = torch.float32 if beta.dtype in (torch.float32, torch.bfloat16, torch.float16) else torch.float64
+    a = beta.to(dt).contiguous()
+    b = torch.zeros((bsz, m), dtype=dt, device=dev)
     if m > 1:
-        b[:, : m - 1] = alpha.to(torch.float64)
-    evals = torch.empty((bsz, m), dtype=torch.float64, device=dev)
-    first = torch.empty((bsz, m), dtype=torch.float64, device=dev)
-    evecs = torch.empty((bsz, m, m), dtype=torch.float64, device=dev) if want_vectors else None
+        b[:, : m - 1] = alpha.to(dt)
+    evals = torch.empty((bsz, m), dtype=dt, device=dev)
+    first = torch.empty((bsz, m), dtype=dt, device=dev)
+    evecs = torch.empty((bsz, m, m), dtype=dt, device=dev) if want_vectors else None
     status = torch.zeros(bsz, dtype=torch.int32, device=dev)
-    _capi.check(lib.colagb_tridiag_eig_f64(a.data_ptr(), b.data_ptr(), m, bsz, evals.data_ptr(), first.data_ptr(),
-                                           evecs.data_ptr() if evecs is not None else None, status.data_ptr(),
-                                           _capi.stream_ptr(dev)), "tridiagonal eigensolver")
+    fn = lib.colagb_tridiag_eig_f32 if dt == torch.float32 else lib.colagb_tridiag_eig_f64
+    _capi.check(fn(a.data_ptr(), b.data_ptr(), m, bsz, evals.data_ptr(), first.data_ptr(),
+                   evecs.data_ptr() if evecs is not None else None, status.data_ptr(), _capi.stream_ptr(dev)),
+                "tridiagonal eigensolver")
     return evals, (evecs if want_vectors else first), status
 
 

@@ -338,21 +338,26 @@ int colagb_basis_combine(const void* basis, int64_t n, int64_t bs, int32_t m, co
                          void* out, int32_t dtype, void* stream);
 
 /* ======================================================================== *
- *  FP64 symmetric tridiagonal eigensolver (batched), implicit QL with      *
- *  Wilkinson shifts.  Replaces xnp.eigh(T) in lanczos_eigs (lanczos.py:57), *
- *  LanczosUnary (unary.py:52) and slq_fwd (tbd/slq.py:44).                 *
+ *  Symmetric tridiagonal eigensolver (batched), implicit QL with Wilkinson *
+ *  shifts, in FP64 or FP32.  Replaces xnp.eigh(T) in lanczos_eigs         *
+ *  (lanczos.py:57), LanczosUnary (unary.py:52) and slq_fwd (tbd/slq.py:44),*
+ *  which solve T in the precision of the recurrence that produced it.     *
  *  a: batch x m diagonal, b: batch x m off-diagonal (b[i] couples i, i+1;  *
- *  b[m-1] ignored).  evals: batch x m ascending.  first_row: batch x m,    *
- *  row 0 of the eigenvector matrix (Gauss quadrature weights), may be NULL. *
- *  evecs: batch x m x m (row-major, column j = eigenvector j), may be NULL. *
- *  status: batch ints, 0 = converged, 1 = iteration limit hit.            *
+ *  b[m-1] ignored).  evals: batch x m ascending (NaN last).  first_row:    *
+ *  batch x m, row 0 of the eigenvector matrix (Gauss quadrature weights),  *
+ *  may be NULL.  evecs: batch x m x m (row-major, column j = eigenvector   *
+ *  j), may be NULL.  status: batch ints, 0 = converged, 1 = iteration      *
+ *  limit hit.  Each matrix is scaled by a power of two before the sweeps   *
+ *  (exact), so any finite input is handled without overflow.              *
  * ======================================================================== */
 /* With evecs, the rotations of the QL sweeps are recorded and replayed on the rows of the eigenvector
  * matrix by a second kernel; the record lives in a stream-ordered temporary (cudaMallocAsync /
- * cudaFreeAsync on `stream`) of batch * (6 m^2 + 64) * 20 bytes -- the one entry point that allocates
- * device memory itself. */
+ * cudaFreeAsync on `stream`) of batch * (6 m^2 + 64) * (2 s + 4) bytes (s = 8 or 4) -- the one entry
+ * point that allocates device memory itself. */
 int colagb_tridiag_eig_f64(const double* a, const double* b, int64_t m, int64_t batch, double* evals,
                            double* first_row, double* evecs, int32_t* status, void* stream);
+int colagb_tridiag_eig_f32(const float* a, const float* b, int64_t m, int64_t batch, float* evals,
+                           float* first_row, float* evecs, int32_t* status, void* stream);
 
 /* ======================================================================== *
  *  Learned FSAI preconditioner for 5-point operators on an m x m grid     *

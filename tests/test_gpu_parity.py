@@ -60,6 +60,48 @@ def test_csr_matmat(k, dtype, tol):
     assert rel(op @ X, dense @ X.double()) < tol
 
 
+def _irregular_csr(n, seed, long_rows=(), long_len=300):
+    """Row lengths 0..20 (with empty rows), a few rows of long_len entries, unsorted-in-space columns."""
+    rng = np.random.default_rng(seed)
+    lens = rng.integers(0, 21, n)
+    lens[rng.random(n) < 0.1] = 0
+    for r in long_rows:
+        lens[r] = long_len
+    ip = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    ix = np.concatenate([np.sort(rng.choice(n, size=int(c), replace=False)) for c in lens]).astype(np.int32)
+    v = rng.standard_normal(int(ip[-1]))
+    return ip, ix, v
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64, torch.bfloat16])
+@pytest.mark.parametrize("misalign", [False, True])
+def test_csr_spmv_irregular_rows(dtype, misalign):
+    """Single-column CSR products on ragged rows: empty rows, 32-row groups whose nonzeros overflow the
+    streaming kernel's buffer (rows of 300), a row count that is not a multiple of 32, and index /
+    value arrays that are not 16-byte aligned (the scalar-load variant)."""
+    n = 2000 + 17
+    ip, ix, v = _irregular_csr(n, seed=11, long_rows=(5, 6, 7, 40, 1999))
+    cdt = torch.float64 if dtype == torch.float64 else torch.float32
+    vals = torch.as_tensor(v).to(dtype)
+    idx = torch.as_tensor(ix)
+    if misalign:  # same data one element into a larger buffer
+        vals = torch.cat([vals[:1], vals])[1:]
+        idx = torch.cat([idx[:1], idx])[1:]
+    op = cola.ops.Sparse.from_csr(torch.as_tensor(ip).to(DEV), idx.to(DEV), vals.to(DEV), (n, n))
+    x = torch.randn(n, device=DEV, dtype=cdt)
+    dense = torch.zeros(n, n, dtype=torch.float64)
+    rows = np.repeat(np.arange(n), np.diff(ip))
+    dense[torch.as_tensor(rows), torch.as_tensor(ix).long()] = vals.double()
+    ref = dense.to(DEV) @ x.double()
+    y = op @ x
+    assert y.dtype == cdt
+    tol = 1e-12 if dtype == torch.float64 else 1e-5
+    assert rel(y, ref) < tol
+    # Sum of two leaves: the second product accumulates into the first (beta = 1)
+    y2 = (op + op) @ x
+    assert rel(y2, 2 * ref) < tol
+
+
 def test_sparse_known_answer(golden):
     g = golden("ops_sparse_known")
     S = cola.ops.Sparse(T(g["data"]), T(g["rows"]), T(g["cols"]), (3, 4))
@@ -325,6 +367,50 @@ def test_tridiag_eigh(m):
         Pm = P[i].cpu().numpy()
         np.testing.assert_allclose(Tm @ Pm, Pm * w[None, :], atol=1e-9)
         np.testing.assert_allclose(np.abs(first[i].cpu().numpy()), np.abs(V[0]), atol=1e-9)
+
+
+@pytest.mark.parametrize("m", [1, 2, 33, 100, 256])
+def test_tridiag_eigh_fp32(m):
+    """FP32 tridiagonals (from FP32 recurrences) are solved in FP32, as the reference's eigh of the FP32
+    T: eigenvalues within a few FP32 ulps of the norm, eigenvectors orthonormal and satisfying
+    T P = P diag(w) to FP32 accuracy."""
+    rng = np.random.default_rng(100 + m)
+    bsz = 3
+    a = rng.standard_normal((bsz, m)).astype(np.float32)
+    b = rng.standard_normal((bsz, max(m - 1, 0))).astype(np.float32)
+    ev, P, status = cola.linalg.tridiag_eigh(T(a, torch.float32), T(b, torch.float32), want_vectors=True)
+    ev2, first, _ = cola.linalg.tridiag_eigh(T(a, torch.float32), T(b, torch.float32), want_vectors=False)
+    assert ev.dtype == torch.float32 and P.dtype == torch.float32
+    assert int(status.sum()) == 0
+    for i in range(bsz):
+        Tm = np.diag(a[i].astype(np.float64))
+        if m > 1:
+            Tm += np.diag(b[i].astype(np.float64), -1) + np.diag(b[i].astype(np.float64), 1)
+        w, V = np.linalg.eigh(Tm)
+        nrm = max(np.abs(w).max(), 1e-30)
+        assert np.abs(ev[i].cpu().numpy() - w).max() <= 64 * 1.2e-7 * nrm
+        assert np.abs(ev2[i].cpu().numpy() - w).max() <= 64 * 1.2e-7 * nrm
+        Pm = P[i].cpu().double().numpy()
+        # orthogonality and residual to O(m eps) of FP32, as for any backward-stable QL
+        assert np.abs(Pm.T @ Pm - np.eye(m)).max() < 8 * m * 1.2e-7 + 1e-6
+        assert np.abs(Tm @ Pm - Pm * w[None, :]).max() < (8 * m * 1.2e-7 + 1e-6) * nrm
+
+
+@pytest.mark.parametrize("dtype,scale", [(torch.float32, 1e25), (torch.float32, 1e-25), (torch.float64, 1e200),
+                                         (torch.float64, 1e-200)])
+def test_tridiag_eigh_scaled(dtype, scale):
+    """Entries far from 1 (whose squares would overflow or underflow) give the scaled eigenvalues: each
+    matrix is scaled by a power of two before the sweeps."""
+    rng = np.random.default_rng(7)
+    a = rng.standard_normal((2, 40))
+    b = rng.standard_normal((2, 39))
+    ev, _, st = cola.linalg.tridiag_eigh(T(a * scale, dtype), T(b * scale, dtype), want_vectors=False)
+    ev1, _, _ = cola.linalg.tridiag_eigh(T(a, dtype), T(b, dtype), want_vectors=False)
+    assert int(st.sum()) == 0
+    got = ev.double().cpu().numpy() / scale
+    ref = ev1.double().cpu().numpy()
+    tol = 1e-5 if dtype == torch.float32 else 1e-12
+    assert np.abs(got - ref).max() <= tol * np.abs(ref).max()
 
 
 # ---------------------------------------------------------------------------------------------
