@@ -31,6 +31,7 @@ KRON_PRECISION = {"auto": 0, "fp32": 1, "bf16": 2, "bf16x3": 3}
 PREC_NONE, PREC_JACOBI, PREC_FSAI = 0, 1, 2
 IR_RELIABLE, IR_RESTART = 0, 1
 MATVEC_FP32, MATVEC_BF16 = 0, 1
+SPARE_OFF, SPARE_AUTO, SPARE_ONLY = 0, 1, 2
 
 SYS_RUNNING, SYS_CONVERGED, SYS_MAX_ITERS, SYS_BREAKDOWN, SYS_NAN, SYS_FALLBACK = range(6)
 SYS_STATUS_NAMES = {0: "running", 1: "converged", 2: "max_iters", 3: "breakdown", 4: "nan", 5: "fallback"}
@@ -72,7 +73,7 @@ class IrParams(C.Structure):
     _fields_ = [("tol", C.c_double), ("inner_tol", C.c_double), ("max_sweeps", C.c_int32),
                 ("max_inner_iters", C.c_int32), ("preconditioner", C.c_int32), ("fallback", C.c_int32),
                 ("spin_limit", C.c_int64), ("mode", C.c_int32), ("schedule", C.c_int32), ("no_wait", C.c_int32),
-                ("matvec", C.c_int32)]
+                ("matvec", C.c_int32), ("spare", C.c_int32)]
 
 
 class IrResult(C.Structure):

@@ -1,6 +1,6 @@
 """One batched solve of the 2-D diffusion family, for profiling and latency measurements.
 
-    python -m cola_gb300.cases --systems 8 --m 512 --precond jacobi --schedule onchip --repeat 2
+    python -m cola_gb300.cases --systems 8 --m 512 --precond jacobi --schedule onchip --repeat 2 [--spare off]
 
 Runs ``--repeat`` identical solves (the first one also pays for workspace allocation) and prints one
 JSON line per solve: wall time, solves/s, mean / max CG steps, FP64 relative residual, and the time
@@ -26,6 +26,8 @@ def main(argv=None):
     ap.add_argument("--schedule", default="auto", choices=["auto", "grid", "cluster8", "cluster16", "onchip"])
     ap.add_argument("--repeat", type=int, default=2)
     ap.add_argument("--tol", type=float, default=1e-8)
+    ap.add_argument("--spare", default="off", choices=["auto", "off", "only"],
+                    help="on-chip schedule: the companion CTAs on the SMs the clusters leave free")
     args = ap.parse_args(argv)
 
     import cola_gb300 as cola
@@ -56,11 +58,12 @@ def main(argv=None):
         torch.cuda.synchronize()
         t = time.perf_counter()
         X, info = cola.linalg.solve_batched(fam, B, precond="fsai" if pat is not None else args.precond,
-                                            tol=args.tol, fsai=fsai, schedule=args.schedule)
+                                            tol=args.tol, fsai=fsai, schedule=args.schedule, spare=args.spare)
         torch.cuda.synchronize()
         t = time.perf_counter() - t
         it = info["iterations"].double()
-        print(json.dumps({"repeat": rep, "schedule": args.schedule, "precond": args.precond, "systems": args.systems,
+        print(json.dumps({"repeat": rep, "schedule": args.schedule, "spare": args.spare, "precond": args.precond,
+                          "systems": args.systems,
                           "n": fam.n, "seconds": t, "build_seconds": tb, "solves_per_s": args.systems / t,
                           "mean_iters": float(it.mean()), "max_iters": int(it.max()),
                           "us_per_step_slowest": 1e6 * t / max(1, int(it.max())),

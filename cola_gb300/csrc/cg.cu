@@ -37,7 +37,7 @@ namespace colagb {
 using PfnCtxGetCurrent = CUresult (*)(CUcontext*);
 using PfnCtxGetId = CUresult (*)(CUcontext, unsigned long long*);
 
-static unsigned long long current_context_id() {
+unsigned long long current_context_id() {
   static PfnCtxGetCurrent get_cur = nullptr;
   static PfnCtxGetId get_id = nullptr;
   static std::once_flag once;

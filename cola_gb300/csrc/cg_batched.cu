@@ -648,7 +648,7 @@ struct BatchedWs {
   size_t block_bytes;
 };
 
-size_t onchip_workspace_floats(int64_t n, bool fsai);
+size_t onchip_workspace_floats(int64_t n, bool fsai, bool spare);
 size_t block_workspace_bytes(int64_t n, int64_t S, int nb_max);
 int block_grid_blocks();
 int block_pcg_solve(const colagb_batched_csr* A, const double* B, double* X, const colagb_ir_params* prm,
@@ -698,7 +698,7 @@ static BatchedWs carve_batched(Bump& ws, const colagb_batched_csr& A, const cola
   w.block = nullptr;
   w.block_bytes = 0;
   const bool onchip = !bf && (prm.schedule == COLAGB_SCHED_AUTO || prm.schedule == COLAGB_SCHED_ONCHIP);
-  const size_t nf = onchip ? onchip_workspace_floats(A.n, fsai) : 0;
+  const size_t nf = onchip ? onchip_workspace_floats(A.n, fsai, prm.spare != COLAGB_SPARE_OFF) : 0;
   w.onchip = nf ? ws.take<float>(nf) : nullptr;
   w.onchip_bytes = nf * sizeof(float);
   const int64_t sets = A.shared_values ? 1 : S;

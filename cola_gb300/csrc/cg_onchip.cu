@@ -23,6 +23,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <mutex>
 #include <string>
 #include <type_traits>
 #include <vector>
@@ -704,6 +705,539 @@ __global__ void __launch_bounds__(kOT, 1) k_onchip_pcg(const __grid_constant__ O
   }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Companion schedule on the SMs the clusters leave free.  The on-chip clusters hold 16 SMs each
+// (7 clusters = 112 of the 152 SMs at 224 KB of shared memory per CTA); on each remaining SM one
+// 512-thread CTA solves whole systems alone, with the same algorithm and stop rule, its vectors in
+// global memory.  It claims systems from the on-chip kernel's counter while more than `reserve`
+// remain unclaimed, so that the clusters (about ten times faster per system) finish the tail.
+//
+// Layout per CTA: the system's rows padded to np (a multiple of 4 * kST * kRowBatch) in the strip
+// layout of the on-chip schedule with the CTA as the whole "cluster" (S = np / 4 float4 groups), so
+// every operand of a diagonal product is one aligned 128-bit load; p and r carry a halo of H float4s
+// on each side whose components are copies of the adjacent strips' rows, written by the owner of
+// each row as it stores it (put4 / put1).  Per step and row the CTA streams the matrix diagonals (A
+// in FP32, the FSAI operator M in bfloat16) and ~9 FP32 vector words; the next batches of each
+// stream are prefetched into L2 with bulk prefetches so that DRAM latency is hidden without
+// registers.  Reductions are block-wide in a fixed order.
+constexpr int kST = 512;  // threads per spare-SM CTA
+constexpr int kSU = 4;    // float4 groups per thread per batch (loads in flight per stream)
+constexpr int64_t kSpareRowAlign = 4 * kST * kRowBatch;  // 16384
+constexpr int kSpareRatio = 28;  // cluster solves per companion solve (measured: ~14 ms vs ~380 ms per 512 x 512 system)
+
+struct SpareArgs {
+  float* base;       // per-CTA regions of per_cta floats
+  int64_t per_cta;
+  int64_t np;        // rows padded to kSpareRowAlign
+  int H;             // halo float4s on each side (multiple of 4 rows, <= np / 4)
+  int reserve;       // claim only while more than this many systems are unclaimed
+};
+
+// floats of one spare CTA's region for n rows: A diagonals, 1/diag, G diagonals, M (bfloat16, in
+// float-sized space), p and r with halos of up to np / 4 float4s, A p, z, d.
+static int64_t spare_rows(int64_t n) { return (n + kSpareRowAlign - 1) / kSpareRowAlign * kSpareRowAlign; }
+static int64_t spare_cta_floats(int64_t n, bool fsai) {
+  const int64_t np = spare_rows(n);
+  const int64_t mat = (kMaxDiagA + 1) * np + (fsai ? kMaxDiagG * np + (kMaxDiagM * np + 1) / 2 : 0);
+  return mat + 2 * (3 * np) + 3 * np + 64;
+}
+
+// The companion CTAs' streams carry an L2 evict-first policy: their working sets (~20 MB per system)
+// pass through L2 once per step and must not displace the clusters' diagonal slots, which L2 serves
+// every ~14 us.
+__device__ __forceinline__ uint64_t evict_first_policy() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+__device__ __forceinline__ void l2_prefetch(const void* p, uint32_t bytes, uint64_t pol) {
+  asm volatile("cp.async.bulk.prefetch.L2.global.L2::cache_hint [%0], %1, %2;" ::"l"(p), "r"(bytes), "l"(pol)
+               : "memory");
+}
+__device__ __forceinline__ float4 ld4_ef(const float* p, uint64_t pol) {
+  float4 v;
+  asm volatile("ld.global.L1::no_allocate.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ void st4_ef(float* p, float4 v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.v4.f32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(p), "f"(v.x), "f"(v.y), "f"(v.z),
+               "f"(v.w), "l"(pol)
+               : "memory");
+}
+template <typename T> struct SpareDiag;
+template <> struct SpareDiag<float> {
+  using Reg = float4;
+  static __device__ __forceinline__ Reg load(const float* p, uint64_t pol) { return ld4_ef(p, pol); }
+};
+template <> struct SpareDiag<__nv_bfloat16> {
+  using Reg = uint2;
+  static __device__ __forceinline__ Reg load(const __nv_bfloat16* p, uint64_t pol) {
+    uint2 v;
+    asm volatile("ld.global.L1::no_allocate.L2::cache_hint.v2.u32 {%0, %1}, [%2], %3;"
+                 : "=r"(v.x), "=r"(v.y)
+                 : "l"(p), "l"(pol));
+    return v;
+  }
+};
+
+// Strip-layout store of float4 group q of a vector with halos (H float4s each side): the halo
+// components that copy q's rows are written too (components 1..3 of the left halo float4 q - S and
+// 0..2 of the right halo float4 q + S; the others stay zero from the setup).
+__device__ __forceinline__ void put4(float* v, int q, int S, int H, float4 x, uint64_t pol) {
+  st4_ef(v + 4 * (int64_t)q, x, pol);
+  if (q >= S - H) {
+    float* h = v + 4 * (q - S);
+    h[1] = x.x;
+    h[2] = x.y;
+    h[3] = x.z;
+  }
+  if (q < H) {
+    float* h = v + 4 * (q + S);
+    h[0] = x.y;
+    h[1] = x.z;
+    h[2] = x.w;
+  }
+}
+// The same for one row l (float index sidx(l, S)).
+__device__ __forceinline__ void put1(float* v, int l, int S, int H, float x) {
+  const int q = l % S, c = l / S;
+  v[4 * q + c] = x;
+  if (q >= S - H && c <= 2) v[4 * (q - S) + c + 1] = x;
+  if (q < H && c >= 1) v[4 * (q + S) + c - 1] = x;
+}
+
+// Block-wide sums of NQ values in a fixed order (every thread gets the totals).
+template <int NQ, class T>
+__device__ __forceinline__ void spare_sum(T (&v)[NQ], T* red) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) v[q] = warp_sum(v[q]);
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) red[q * (kST / 32) + w] = v[q];
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    T s = T(0);
+    for (int u = 0; u < kST / 32; ++u) s += red[q * (kST / 32) + u];
+    v[q] = s;
+  }
+  __syncthreads();
+}
+
+// out[q] = sum_k D[k][q] * v[q + off[k]] over this thread's groups (main diagonal last); returns the
+// thread's part of <v, D v>.  While a batch is consumed, the batch two ahead of every stream is
+// prefetched into L2 (thread k < nk: diagonal k; thread nk: v).
+template <typename T>
+__device__ __forceinline__ float spare_product(const T* D, const int* off, int nk, int64_t np, const float* v,
+                                               float* out, int S, int H, int tid, uint64_t pol) {
+  using DL = Diag4<T>;
+  using SL = SpareDiag<T>;
+  constexpr int kBatch = kSU * kST;  // float4 groups per batch
+  float dot = 0.f;
+#pragma unroll 1
+  for (int g0 = 0; g0 < S; g0 += kBatch) {
+    const int gp = g0 + 2 * kBatch;
+    if (gp < S) {
+      if (tid < nk) l2_prefetch(D + tid * np + 4 * (int64_t)gp, (uint32_t)(kBatch * 4 * sizeof(T)), pol);
+      else if (tid == nk) {
+        const int lo = gp - H, hi = gp + kBatch + H < S + H ? gp + kBatch + H : S + H;
+        l2_prefetch(v + 4 * (int64_t)lo, (uint32_t)((hi - lo) * 16), pol);
+      }
+    }
+    float4 acc[kSU], own[kSU];
+#pragma unroll
+    for (int u = 0; u < kSU; ++u) acc[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll 1
+    for (int k = 0; k < nk; ++k) {
+      const T* Dk = D + k * np;
+      const int o = off[k];
+      typename DL::Reg dv[kSU];
+      float4 pv[kSU];
+#pragma unroll
+      for (int u = 0; u < kSU; ++u) {
+        const int q = g0 + tid + u * kST;
+        dv[u] = SL::load(Dk + 4 * (int64_t)q, pol);
+        pv[u] = ld4_ef(v + 4 * (int64_t)(q + o), pol);
+      }
+#pragma unroll
+      for (int u = 0; u < kSU; ++u) {
+        const float4 av = DL::wide(dv[u]);
+        acc[u].x = fmaf(av.x, pv[u].x, acc[u].x);
+        acc[u].y = fmaf(av.y, pv[u].y, acc[u].y);
+        acc[u].z = fmaf(av.z, pv[u].z, acc[u].z);
+        acc[u].w = fmaf(av.w, pv[u].w, acc[u].w);
+        if (o == 0) own[u] = pv[u];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kSU; ++u) {
+      const int q = g0 + tid + u * kST;
+      if (off[nk - 1] != 0) own[u] = ld4_ef(v + 4 * (int64_t)q, pol);
+      st4_ef(out + 4 * (int64_t)q, acc[u], pol);
+      dot += dot4(own[u], acc[u]);
+    }
+  }
+  return dot;
+}
+
+// Data written inside this kernel by other threads of the CTA is read after a __syncthreads.
+__global__ void __launch_bounds__(kST, 1) k_spare_pcg(const __grid_constant__ OnchipArgs a,
+                                                      const __grid_constant__ SpareArgs sp) {
+  __shared__ double dred[4 * (kST / 32)];
+  __shared__ float fred[4 * (kST / 32)];
+  __shared__ unsigned int s_sys;
+  const int tid = threadIdx.x;
+  const int64_t n = a.n, np = sp.np;
+  const int S = (int)(np / 4), H = sp.H;
+  constexpr int kBatch = kSU * kST;
+  float* base = sp.base + (int64_t)blockIdx.x * sp.per_cta;
+  float* A = base;
+  float* Dv = A + kMaxDiagA * np;
+  float* Gd = a.gdia ? Dv + np : nullptr;
+  __nv_bfloat16* M = a.mdia ? reinterpret_cast<__nv_bfloat16*>(Dv + np + kMaxDiagG * np) : nullptr;
+  float* vec = Dv + np + (a.gdia ? kMaxDiagG * np + (kMaxDiagM * np + 1) / 2 : 0);
+  vec = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(vec) + 15) & ~uintptr_t(15));
+  float* ps = vec + 4 * (int64_t)H;             // p: float4 indices [-H, S + H)
+  float* rs = ps + 4 * ((int64_t)S + 2 * H);    // r: float4 indices [-H, S + H)
+  float* aps = rs + 4 * ((int64_t)S + H);       // A p: [0, S)
+  float* zs = aps + np;                         // z (FSAI): [0, S)
+  float* ds = zs + np;                          // d: [0, S)
+  const uint64_t pol = evict_first_policy();
+
+  while (true) {
+    if (tid == 0) {
+      unsigned int c = *reinterpret_cast<volatile unsigned int*>(a.next);
+      unsigned int got = (unsigned int)a.S;
+#pragma unroll 1
+      for (int tries = 0; tries < (1 << 20); ++tries) {  // every failed exchange saw a newer claim
+        if ((int64_t)c + sp.reserve >= a.S) break;
+        const unsigned int prev = atomicCAS(a.next, c, c + 1);
+        if (prev == c) {
+          got = c;
+          break;
+        }
+        c = prev;
+      }
+      s_sys = got;
+    }
+    __syncthreads();
+    const int64_t s = s_sys;
+    __syncthreads();
+    if (s >= a.S) break;
+
+    const float* vals = a.vals + s * a.vstride;
+    const double* B = a.B + s * n;
+    double* X = a.X + s * n;
+    int prec = a.prec_kind;
+
+    // ---- setup: diagonal storage, x = 0, vectors and halos zero, |b|^2 ----
+    double v1[1] = {0.0};
+#pragma unroll 1
+    for (int64_t l = tid; l < np; l += kST) {
+      const bool live = l < n;
+      const int64_t si = sidx((int)l, S);
+      csr_row_to_diagonals(a.indptr, a.indices, vals, l, live, a.off, a.nd, A + si, np);
+      Dv[si] = a.center >= 0 && A[a.center * np + si] != 0.f ? 1.f / A[a.center * np + si] : 1.f;
+      if (Gd) csr_row_to_diagonals(a.g_indptr, a.g_indices, a.g_vals + s * a.g_nnz, l, live, a.goff, a.ng, Gd + l, np);
+      ps[l] = 0.f;
+      rs[l] = 0.f;
+      ds[l] = 0.f;
+      if (l < 4 * H) {
+        ps[l - 4 * H] = 0.f;
+        ps[np + l] = 0.f;
+        rs[l - 4 * H] = 0.f;
+        rs[np + l] = 0.f;
+      }
+      if (live) {
+        const double bv = B[l];
+        v1[0] += bv * bv;
+        X[l] = 0.0;
+      }
+    }
+    spare_sum<1>(v1, dred);  // also publishes G's diagonals and x = 0 to the CTA
+    if (M) {  // M = G^T G (same construction as the clusters', CTA = whole system)
+#pragma unroll 1
+      for (int l0 = tid; l0 < np; l0 += kRowBatch * kST) {
+        float asum[kRowBatch], ctr[kRowBatch];
+#pragma unroll
+        for (int u = 0; u < kRowBatch; ++u) asum[u] = ctr[u] = 0.f;
+        int mc = 0;
+#pragma unroll 1
+        for (int m = 0; m < a.nm; ++m) {
+          float v[kRowBatch];
+#pragma unroll
+          for (int u = 0; u < kRowBatch; ++u) v[u] = 0.f;
+#pragma unroll 1
+          for (int q = a.pstart[m]; q < a.pstart[m + 1]; ++q) {
+            const float* ga = Gd + a.pa[q] * np;
+            const float* gb = Gd + a.pb[q] * np;
+            const int go = a.goff[a.pa[q]];
+#pragma unroll
+            for (int u = 0; u < kRowBatch; ++u) {
+              const int64_t i = l0 + u * kST;
+              const int64_t k = i - go;
+              if (i < n && k < n) v[u] += ga[k] * gb[k];
+            }
+          }
+#pragma unroll
+          for (int u = 0; u < kRowBatch; ++u) asum[u] += fabsf(v[u]);
+          if (a.moff[m] == 0) {
+            mc = m;
+#pragma unroll
+            for (int u = 0; u < kRowBatch; ++u) ctr[u] = v[u];
+          } else {
+#pragma unroll
+            for (int u = 0; u < kRowBatch; ++u) M[m * np + sidx(l0 + u * kST, S)] = __float2bfloat16_rn(v[u]);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < kRowBatch; ++u)
+          M[mc * np + sidx(l0 + u * kST, S)] = __float2bfloat16_rn(ctr[u] + kMBoost * asum[u]);
+      }
+    }
+    const double bnorm = sqrt(v1[0]);
+    int status = COLAGB_SYS_RUNNING;
+    double relres = bnorm > 0.0 ? 1.0 : 0.0;
+    if (!(bnorm > 0.0)) status = bnorm == 0.0 ? COLAGB_SYS_CONVERGED : COLAGB_SYS_NAN;
+    const double binv = bnorm > 0.0 ? 1.0 / bnorm : 1.0;
+
+    // r = b/|b| - A x in FP64 (eight rows' loads in flight per diagonal), |r|^2; r's halos too
+    auto residual = [&](double& rr) {
+      rr = 0.0;
+#pragma unroll 1
+      for (int l0 = tid; l0 < np; l0 += kRowBatch * kST) {
+        double ax[kRowBatch];
+#pragma unroll
+        for (int u = 0; u < kRowBatch; ++u) ax[u] = 0.0;
+#pragma unroll 1
+        for (int k = 0; k < a.nd; ++k) {
+          const float* Ak = A + k * np;
+          const int o = a.off[k];
+#pragma unroll
+          for (int u = 0; u < kRowBatch; ++u) {
+            const int l = l0 + u * kST;
+            const int64_t c = (int64_t)l + o;
+            const float av = Ak[sidx(l, S)];
+            const double xv = c >= 0 && c < n ? X[c] : 0.0;
+            ax[u] += (double)av * xv;
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < kRowBatch; ++u) {
+          const int l = l0 + u * kST;
+          if (l < n) {
+            const double rv = B[l] * binv - ax[u];
+            put1(rs, l, S, H, (float)rv);
+            rr += rv * rv;
+          }
+        }
+      }
+    };
+    // z (preconditioned r) into dst with its halos when dst is p, into zs (FSAI) otherwise; <r, z>
+    auto precondition = [&](float* dst) -> float {
+      float rz = 0.f;
+      if (prec == COLAGB_PREC_FSAI) {
+        rz = spare_product<__nv_bfloat16>(M, a.moff, a.nm, np, rs, zs, S, H, tid, pol);
+        if (dst == ps) {
+          __syncthreads();
+#pragma unroll 1
+          for (int q = tid; q < S; q += kST) put4(ps, q, S, H, ld4_ef(zs + 4 * (int64_t)q, pol), pol);
+        }
+        return rz;
+      }
+#pragma unroll 1
+      for (int q = tid; q < S; q += kST) {
+        const float4 r = ld4_ef(rs + 4 * (int64_t)q, pol);
+        float4 z = r;
+        if (prec == COLAGB_PREC_JACOBI) {
+          const float4 d = ld4_ef(Dv + 4 * (int64_t)q, pol);
+          z = make_float4(d.x * r.x, d.y * r.y, d.z * r.z, d.w * r.w);
+        }
+        rz += dot4(r, z);
+        if (dst == ps) put4(ps, q, S, H, z, pol);
+      }
+      return rz;
+    };
+
+    double q2[1];
+    residual(q2[0]);
+    spare_sum<1>(q2, dred);  // r and its halos complete
+    float rn = (float)sqrt(q2[0]);
+    float rmax = rn;
+    double relres_prev = relres;
+    float q1[1] = {precondition(ps)};
+    spare_sum<1>(q1, fred);  // p and its halos complete
+    float gamma = q1[0];
+    if (status == COLAGB_SYS_RUNNING && rn <= (float)a.tol) status = COLAGB_SYS_CONVERGED;
+
+    int it = 0, nrep = 0, it_rep = 0;
+    const float delta = (float)a.inner_tol;
+    while (status == COLAGB_SYS_RUNNING) {
+      // A: A p ; <p, A p>
+      float qa[1] = {spare_product<float>(A, a.off, a.nd, np, ps, aps, S, H, tid, pol)};
+      spare_sum<1>(qa, fred);
+      const float pap = qa[0];
+      if (!(pap > 0.f)) {
+        status = (pap == pap) ? COLAGB_SYS_BREAKDOWN : COLAGB_SYS_NAN;
+        break;
+      }
+      const float alpha = gamma / pap;
+      // B: r -= alpha A p ; |r|^2 ; <r, z> (Jacobi / none here, FSAI after r is complete)
+      float rrf = 0.f, rzf = 0.f;
+#pragma unroll 1
+      for (int g0 = 0; g0 < S; g0 += kBatch) {
+        float4 rv[kSU], av[kSU], dv[kSU];
+#pragma unroll
+        for (int u = 0; u < kSU; ++u) {
+          const int64_t q = g0 + tid + u * kST;
+          rv[u] = ld4_ef(rs + 4 * q, pol);
+          av[u] = ld4_ef(aps + 4 * q, pol);
+          dv[u] = prec == COLAGB_PREC_JACOBI ? ld4_ef(Dv + 4 * q, pol) : make_float4(1.f, 1.f, 1.f, 1.f);
+        }
+#pragma unroll
+        for (int u = 0; u < kSU; ++u) {
+          const int q = g0 + tid + u * kST;
+          rv[u].x -= alpha * av[u].x;
+          rv[u].y -= alpha * av[u].y;
+          rv[u].z -= alpha * av[u].z;
+          rv[u].w -= alpha * av[u].w;
+          rrf += dot4(rv[u], rv[u]);
+          if (prec != COLAGB_PREC_FSAI) {
+            const float4 zv = prec == COLAGB_PREC_JACOBI
+                                  ? make_float4(dv[u].x * rv[u].x, dv[u].y * rv[u].y, dv[u].z * rv[u].z,
+                                                dv[u].w * rv[u].w)
+                                  : rv[u];
+            rzf += dot4(rv[u], zv);
+          }
+          put4(rs, q, S, H, rv[u], pol);
+        }
+      }
+      float qb[2] = {rrf, rzf};
+      if (prec == COLAGB_PREC_FSAI) {
+        __syncthreads();  // r and its halos complete
+        qb[1] = precondition(zs);
+      }
+      spare_sum<2>(qb, fred);
+      ++it;
+      rn = sqrtf(qb[0]);
+      float gamma_new = qb[1];
+      bool restart = false, dpend = true;
+      if (!(rn == rn)) {
+#pragma unroll 1
+        for (int64_t l = tid; l < np; l += kST) ds[l] += alpha * ps[l];
+        status = COLAGB_SYS_NAN;
+        break;
+      }
+      if (rn <= delta * rmax || rn <= (float)a.tol || it >= a.max_inner ||
+          (a.fallback && prec == COLAGB_PREC_FSAI && it - it_rep >= kJudgeSteps)) {
+        // FP64 replacement: x += d + alpha p, d = 0 ; r = b/|b| - A x
+#pragma unroll 1
+        for (int l0 = tid; l0 < np; l0 += kRowBatch * kST) {
+          double xv[kRowBatch];
+#pragma unroll
+          for (int u = 0; u < kRowBatch; ++u) {
+            const int64_t i = l0 + u * kST;
+            xv[u] = i < n ? X[i] : 0.0;
+          }
+#pragma unroll
+          for (int u = 0; u < kRowBatch; ++u) {
+            const int l = l0 + u * kST;
+            const int sl = sidx(l, S);
+            const float dn = ds[sl] + alpha * ps[sl];
+            if (l < n) X[l] = xv[u] + (double)dn;
+            ds[sl] = 0.f;
+          }
+        }
+        dpend = false;
+        it_rep = it;
+        __syncthreads();  // x complete before any thread reads its neighbours' rows
+        residual(q2[0]);
+        spare_sum<1>(q2, dred);
+        ++nrep;
+        const double rr = sqrt(q2[0]);
+        relres = rr;
+        if (!(rr == rr)) { status = COLAGB_SYS_NAN; break; }
+        if (rr <= a.tol) { status = COLAGB_SYS_CONVERGED; break; }
+        if (it >= a.max_inner || nrep >= a.max_sweeps) { status = COLAGB_SYS_MAX_ITERS; break; }
+        if (a.fallback && prec == COLAGB_PREC_FSAI && rr > 0.5 * relres_prev) {
+          prec = COLAGB_PREC_JACOBI;
+          restart = true;
+        }
+        if (a.mode == COLAGB_IR_RESTART) restart = true;
+        relres_prev = rr;
+        rn = (float)rr;
+        rmax = rn;
+        q1[0] = precondition(zs);
+        spare_sum<1>(q1, fred);
+        gamma_new = q1[0];
+      }
+      const float beta = restart || gamma == 0.f ? 0.f : gamma_new / gamma;
+      gamma = gamma_new;
+      // C: d += alpha p (unless flushed) ; p = z + beta p, with p's halos
+#pragma unroll 1
+      for (int g0 = 0; g0 < S; g0 += kBatch) {
+        float4 po[kSU], dd[kSU], zv[kSU];
+#pragma unroll
+        for (int u = 0; u < kSU; ++u) {
+          const int64_t q = g0 + tid + u * kST;
+          po[u] = ld4_ef(ps + 4 * q, pol);
+          dd[u] = ld4_ef(ds + 4 * q, pol);
+          if (prec == COLAGB_PREC_FSAI) {
+            zv[u] = ld4_ef(zs + 4 * q, pol);
+          } else {
+            const float4 r = ld4_ef(rs + 4 * q, pol);
+            if (prec == COLAGB_PREC_JACOBI) {
+              const float4 d = ld4_ef(Dv + 4 * q, pol);
+              zv[u] = make_float4(d.x * r.x, d.y * r.y, d.z * r.z, d.w * r.w);
+            } else {
+              zv[u] = r;
+            }
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < kSU; ++u) {
+          const int q = g0 + tid + u * kST;
+          if (dpend)
+            st4_ef(ds + 4 * (int64_t)q, make_float4(dd[u].x + alpha * po[u].x, dd[u].y + alpha * po[u].y,
+                                                    dd[u].z + alpha * po[u].z, dd[u].w + alpha * po[u].w), pol);
+          put4(ps, q, S, H, make_float4(zv[u].x + beta * po[u].x, zv[u].y + beta * po[u].y,
+                                        zv[u].z + beta * po[u].z, zv[u].w + beta * po[u].w), pol);
+        }
+      }
+      __syncthreads();  // p and its halos complete
+    }
+    __syncthreads();
+    // finish: x += d, scale by |b|
+#pragma unroll 1
+    for (int l0 = tid; l0 < np; l0 += kRowBatch * kST) {
+      double xv[kRowBatch];
+#pragma unroll
+      for (int u = 0; u < kRowBatch; ++u) {
+        const int64_t i = l0 + u * kST;
+        xv[u] = i < n ? X[i] : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < kRowBatch; ++u) {
+        const int l = l0 + u * kST;
+        if (l < n) X[l] = (xv[u] + (double)ds[sidx(l, S)]) * (bnorm > 0.0 ? bnorm : 1.0);
+      }
+    }
+    if (tid == 0) {
+      int st = status == COLAGB_SYS_RUNNING ? COLAGB_SYS_MAX_ITERS : status;
+      if (st == COLAGB_SYS_CONVERGED && a.prec_kind == COLAGB_PREC_FSAI && prec != COLAGB_PREC_FSAI)
+        st = COLAGB_SYS_FALLBACK;
+      if (a.out_status) a.out_status[s] = st;
+      if (a.out_iters) a.out_iters[s] = it;
+      if (a.out_relres) a.out_relres[s] = relres;
+      if (a.out_nrep) a.out_nrep[s] = nrep;
+    }
+    __syncthreads();
+  }
+}
+
 // ---- pattern analysis: the set of diagonals (column - row) a CSR pattern occupies ----
 __global__ void k_offset_bitmap(const int32_t* __restrict__ indptr, const int32_t* __restrict__ indices, int64_t n,
                                 unsigned int* bits) {
@@ -784,14 +1318,66 @@ static int onchip_cluster(int64_t n, int* rows_per_cta, int* groups) {
 
 static int onchip_slots(int cl) { return (num_sms() + cl - 1) / cl; }
 
-// Workspace of the on-chip schedule (diagonal slots + pattern scratch); 0 when not applicable.
-size_t onchip_workspace_floats(int64_t n, bool fsai) {
+template <int CL, int G>
+static int onchip_active_clusters(size_t smem, int* nclusters);
+
+// CTAs of the companion schedule: the SMs that the clusters leave free at the largest shared-memory
+// footprint (the fewest resident clusters), 0 when none.
+static int spare_ctas(int64_t n) {
+  int R = 0, G = 0;
+  const int CL = onchip_cluster(n, &R, &G);
+  if (CL == 0) return 0;
+  int nc = 0;
+  if (CL == 8)
+    G == 8 ? onchip_active_clusters<8, 8>(kOnchipSmemMax, &nc)
+           : G == 16 ? onchip_active_clusters<8, 16>(kOnchipSmemMax, &nc) : onchip_active_clusters<8, 32>(kOnchipSmemMax, &nc);
+  else
+    G == 8 ? onchip_active_clusters<16, 8>(kOnchipSmemMax, &nc)
+           : G == 16 ? onchip_active_clusters<16, 16>(kOnchipSmemMax, &nc) : onchip_active_clusters<16, 32>(kOnchipSmemMax, &nc);
+  if (nc < 1) return 0;
+  const int free_sms = num_sms() - CL * std::min(nc, onchip_slots(CL));
+  return free_sms > 0 ? free_sms : 0;
+}
+
+// Workspace of the on-chip schedule (diagonal slots + pattern scratch, then the companion CTAs'
+// regions); 0 when not applicable.
+size_t onchip_workspace_floats(int64_t n, bool fsai, bool spare) {
   int R = 0;
   const int cl = onchip_cluster(n, &R, nullptr);
   if (cl == 0) return 0;
   const int64_t np = (int64_t)cl * R;
   const int64_t per = kMaxDiagA + 1 + (fsai ? kMaxDiagG + kMaxDiagM : 0);
-  return (size_t)onchip_slots(cl) * per * np + (size_t)(2 * n + 31) / 32 + 64 + 64;
+  const size_t core = (size_t)onchip_slots(cl) * per * np + (size_t)(2 * n + 31) / 32 + 64 + 64;
+  return spare ? core + 64 + (size_t)spare_ctas(n) * spare_cta_floats(n, fsai) : core;
+}
+
+// A private non-blocking stream and two events per CUDA context for the companion launch (forked
+// from and joined back into the caller's stream).
+struct SpareStreams {
+  unsigned long long ctx = 0;
+  cudaStream_t st = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+};
+static const SpareStreams* spare_streams() {
+  static std::mutex mu;
+  static std::vector<SpareStreams> all;
+  const unsigned long long id = current_context_id();
+  if (id == 0) return nullptr;
+  std::lock_guard<std::mutex> lk(mu);
+  for (const auto& e : all)
+    if (e.ctx == id) return &e;
+  SpareStreams e;
+  e.ctx = id;
+  if (cudaStreamCreateWithFlags(&e.st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&e.fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&e.join, cudaEventDisableTiming) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  all.reserve(64);
+  if (all.size() >= 64) return nullptr;  // keeps the returned pointers stable
+  all.push_back(e);
+  return &all.back();
 }
 
 template <int CL, int G>
@@ -858,8 +1444,10 @@ int onchip_pcg_solve(const colagb_batched_csr* Acsr, const double* B, double* X,
   int R = 0, G = 0;
   const int CL = onchip_cluster(n, &R, &G);
   if (CL == 0 || n < 1) return COLAGB_OK;
-  const size_t need = onchip_workspace_floats(n, fsai) * sizeof(float);
+  const bool want_spare = prm->spare != COLAGB_SPARE_OFF;
+  const size_t need = onchip_workspace_floats(n, fsai, want_spare) * sizeof(float);
   if (ws_bytes < need || ws == nullptr) return COLAGB_OK;
+  const int nspare = want_spare ? spare_ctas(n) : 0;
   const int64_t np = (int64_t)CL * R;
   const int64_t per = kMaxDiagA + 1 + (fsai ? kMaxDiagG + kMaxDiagM : 0);
   float* base = static_cast<float*>(ws);
@@ -955,13 +1543,53 @@ int onchip_pcg_solve(const colagb_batched_csr* Acsr, const double* B, double* X,
   a.fallback = prm->fallback;
   a.mode = prm->mode;
   COLAGB_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned int), st));
-  int rc;
-  if (CL == 8)
+  // companion CTAs on the free SMs (prm->spare: AUTO, OFF, or ONLY for tests)
+  const int spare_mode = prm->spare;
+  const int64_t nps = spare_rows(n);
+  const SpareStreams* ss = nullptr;
+  int nsp = 0;
+  if (spare_mode != COLAGB_SPARE_OFF && nspare > 0 && H <= nps / 4) {
+    ss = spare_streams();
+    if (ss) nsp = nspare;
+  }
+  if (spare_mode == COLAGB_SPARE_ONLY && nsp == 0) return COLAGB_OK;  // not available: the caller falls back
+  SpareArgs sp = {};
+  if (nsp > 0) {
+    sp.base = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(counter + 16) + 255) & ~uintptr_t(255));
+    sp.per_cta = spare_cta_floats(n, fsai);
+    sp.np = nps;
+    sp.H = H;
+    // a cluster solves a system ~kSpareRatio times faster than one CTA does: leave the clusters that many
+    // systems each at the end, so that no companion solve outlasts the clusters' last one
+    int nc = 0;
+    if (CL == 8)
+      G == 8 ? onchip_active_clusters<8, 8>(smem, &nc)
+             : G == 16 ? onchip_active_clusters<8, 16>(smem, &nc) : onchip_active_clusters<8, 32>(smem, &nc);
+    else
+      G == 8 ? onchip_active_clusters<16, 8>(smem, &nc)
+             : G == 16 ? onchip_active_clusters<16, 16>(smem, &nc) : onchip_active_clusters<16, 32>(smem, &nc);
+    nsp = std::min<int64_t>(std::max(0, num_sms() - CL * std::min(nc, onchip_slots(CL))), nspare);
+    sp.reserve = spare_mode == COLAGB_SPARE_ONLY ? 0 : (int)std::min<int64_t>((int64_t)kSpareRatio * nc, 1 << 30);
+    if (spare_mode != COLAGB_SPARE_ONLY && (nsp == 0 || a.S <= sp.reserve)) nsp = 0;
+    if (spare_mode == COLAGB_SPARE_ONLY && nsp == 0) nsp = nspare;
+  }
+  if (nsp > 0) COLAGB_CUDA(cudaEventRecord(ss->fork, st));
+  int rc = COLAGB_OK;
+  if (spare_mode == COLAGB_SPARE_ONLY) {
+    // no clusters: the companion CTAs take every system
+  } else if (CL == 8)
     rc = G == 8 ? launch_onchip<8, 8>(a, smem, st)
                 : G == 16 ? launch_onchip<8, 16>(a, smem, st) : launch_onchip<8, 32>(a, smem, st);
   else
     rc = G == 8 ? launch_onchip<16, 8>(a, smem, st)
                 : G == 16 ? launch_onchip<16, 16>(a, smem, st) : launch_onchip<16, 32>(a, smem, st);
+  if (rc == COLAGB_OK && nsp > 0) {
+    COLAGB_CUDA(cudaStreamWaitEvent(ss->st, ss->fork, 0));
+    k_spare_pcg<<<(unsigned)nsp, kST, 0, ss->st>>>(a, sp);
+    COLAGB_CUDA(cudaGetLastError());
+    COLAGB_CUDA(cudaEventRecord(ss->join, ss->st));
+    COLAGB_CUDA(cudaStreamWaitEvent(st, ss->join, 0));
+  }
   if (rc == COLAGB_OK) *used = true;
   return rc == COLAGB_ERR_UNSUPPORTED ? COLAGB_OK : rc;
 }

@@ -31,6 +31,7 @@ int check_cuda(cudaError_t e, const char* what);
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
 int num_sms();                 // SM count of the current device (cached per device)
+unsigned long long current_context_id();  // unique id of the calling thread's current CUDA context, 0 if none
 __host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 inline size_t align_up(size_t v, size_t a = 256) { return (v + a - 1) / a * a; }
 

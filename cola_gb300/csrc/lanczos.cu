@@ -971,6 +971,31 @@ extern "C" int colagb_basis_combine(const void* basis, int64_t n, int64_t bs, in
   return COLAGB_OK;
 }
 
+// Rayleigh quotients of the computed eigenvectors in FP64: evals[j] = s_j^T T s_j / s_j^T s_j.  After an
+// FP32 QL the eigenvalues carry the sweeps' accumulated rounding (a few FP32 ulps of |T|); the quotient
+// of the FP32 eigenvector is off by the square of the vector's error, so this returns each eigenvalue
+// to within FP32 rounding.  One thread per eigenvector; consecutive threads read consecutive columns.
+template <class R>
+__global__ void k_tridiag_rq(const R* A, const R* Bv, int64_t m, const R* evecs, R* evals) {
+  const int64_t sys = blockIdx.y;
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= m) return;
+  const R* a = A + sys * m;
+  const R* b = Bv + sys * m;
+  const R* Z = evecs + sys * m * m;
+  double num = 0.0, den = 0.0, sp = 0.0, si = (double)Z[j];
+  for (int64_t i = 0; i < m; ++i) {
+    const double sn = i + 1 < m ? (double)Z[(i + 1) * m + j] : 0.0;
+    double t = (double)a[i] * si + (i > 0 ? (double)b[i - 1] * sp : 0.0);
+    if (i + 1 < m) t += (double)b[i] * sn;
+    num += si * t;
+    den += si * si;
+    sp = si;
+    si = sn;
+  }
+  if (den > 0.0) evals[sys * m + j] = (R)(num / den);
+}
+
 template <class R>
 static int tridiag_eig(const R* a, const R* b, int64_t m, int64_t batch, R* evals, R* first_row, R* evecs,
                        int32_t* status, cudaStream_t st, const char* name) {
@@ -1009,11 +1034,21 @@ static int tridiag_eig(const R* a, const R* b, int64_t m, int64_t batch, R* eval
     bool overflow = false;
     for (int64_t q = 0; q < batch; ++q) overflow |= hn[q] < 0;
     COLAGB_CUDA(cudaFreeAsync(buf, st));
-    if (!overflow) return COLAGB_OK;
+    if (!overflow) {
+      if (std::is_same<R, float>::value) {
+        k_tridiag_rq<R><<<dim3((unsigned)ceil_div(m, (int64_t)128), (unsigned)batch), 128, 0, st>>>(a, b, m, evecs, evals);
+        COLAGB_CUDA(cudaGetLastError());
+      }
+      return COLAGB_OK;
+    }
     // rare: more rotations than recorded -- recompute with Z updated inside the QL kernel
   }
   k_tridiag_ql<R><<<(unsigned)batch, 128, smem, st>>>(a, b, m, evals, first_row, evecs, status);
   COLAGB_CUDA(cudaGetLastError());
+  if (evecs && std::is_same<R, float>::value) {
+    k_tridiag_rq<R><<<dim3((unsigned)ceil_div(m, (int64_t)128), (unsigned)batch), 128, 0, st>>>(a, b, m, evecs, evals);
+    COLAGB_CUDA(cudaGetLastError());
+  }
   return COLAGB_OK;
 }
 

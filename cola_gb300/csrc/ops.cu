@@ -242,7 +242,7 @@ __device__ __forceinline__ void stream_pass(const int32_t* __restrict__ indices,
 }
 
 template <class T, class S, bool VEC>
-__global__ void __launch_bounds__(kStreamWarps * 32, sizeof(T) == 4 ? 6 : 4) csr_stream_kernel(
+__global__ void __launch_bounds__(kStreamWarps * 32) csr_stream_kernel(
     const int32_t* __restrict__ indptr, const int32_t* __restrict__ indices, const S* __restrict__ vals,
     int64_t rows, int64_t nnz, const T* __restrict__ X, int64_t ldx, int64_t bsx, T* __restrict__ Y, int64_t ldy,
     int64_t bsy, T alpha, T beta, const int* skip) {
@@ -408,16 +408,6 @@ static int launch_csr(const colagb_op_node& nd, const T* X, int64_t ldx, int64_t
     const bool vec = (reinterpret_cast<uintptr_t>(nd.indices) % 16 == 0) &&
                      (reinterpret_cast<uintptr_t>(v) % (sizeof(S) * 4 < 16 ? sizeof(S) * 4 : 16) == 0);
     dim3 grid((unsigned)ceil_div(nd.rows, (int64_t)kStreamWarps * 32), (unsigned)batch);
-    // the whole L1 as shared memory (L1 hits are rare here): the 32 KB per CTA then limits
-    // residency no more than the registers do
-    static const bool carved = [] {
-      cudaFuncSetAttribute(csr_stream_kernel<T, S, true>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                           (int)cudaSharedmemCarveoutMaxShared);
-      cudaFuncSetAttribute(csr_stream_kernel<T, S, false>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                           (int)cudaSharedmemCarveoutMaxShared);
-      return true;
-    }();
-    (void)carved;
     if (vec)
       csr_stream_kernel<T, S, true><<<grid, kStreamWarps * 32, 0, st>>>(nd.indptr, nd.indices, v, nd.rows, nd.nnz, X,
                                                                          ldx, bsx, Y, ldy, bsy, alpha, beta, skip);

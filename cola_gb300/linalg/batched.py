@@ -191,7 +191,8 @@ def onchip_schedule_info(n: int, halo: int) -> dict:
 def solve_batched(A: BatchedCSR, B: torch.Tensor, precond: str = "jacobi", tol: float = 1e-8,
                   inner_tol: float | None = None, max_sweeps: int = 200, max_inner_iters: int = 50000,
                   fsai: tuple | None = None, fallback: bool = True, mode: str = "reliable",
-                  schedule: str = "auto", wait: bool = True, spin_limit: int = 0, matvec: str = "fp32"):
+                  schedule: str = "auto", wait: bool = True, spin_limit: int = 0, matvec: str = "fp32",
+                  spare: str = "off"):
     """Solve A_s x_s = b_s for every system s to |b_s - A_s x_s| / |b_s| <= tol (FP64 residual).
 
     Args:
@@ -223,6 +224,10 @@ def solve_batched(A: BatchedCSR, B: torch.Tensor, precond: str = "jacobi", tol: 
             values with an FP32 diagonal made consistent with them (within 2^-9 of A in the energy norm
             for weighted-Laplacian-type operators), on the cluster schedules; the FP64 residual
             replacements always use the FP32 values.
+        spare: the on-chip schedule's use of the SMs its clusters leave free (40 of 152 for 512 x 512):
+            "auto" -- one CTA per free SM also solves whole systems (same algorithm and stop rule,
+            vectors in global memory) while more than ~28 systems per cluster remain, so the clusters
+            finish the tail; "off" (default) -- clusters only; "only" -- every system on those CTAs.
     Returns (X (S, n) float64, info) with per-system iterations, status and FP64 relative residuals.
     """
     _capi.require_cuda(A.values, B)
@@ -265,7 +270,8 @@ def solve_batched(A: BatchedCSR, B: torch.Tensor, precond: str = "jacobi", tol: 
                          max_inner_iters=int(max_inner_iters), preconditioner=pk, fallback=1 if fallback else 0,
                          spin_limit=int(spin_limit), mode=_capi.IR_RELIABLE if mode == "reliable" else _capi.IR_RESTART,
                          schedule=_SCHED[schedule], no_wait=0 if wait else 1,
-                         matvec={"fp32": _capi.MATVEC_FP32, "bf16": _capi.MATVEC_BF16}[matvec])
+                         matvec={"fp32": _capi.MATVEC_FP32, "bf16": _capi.MATVEC_BF16}[matvec],
+                         spare={"auto": _capi.SPARE_AUTO, "off": _capi.SPARE_OFF, "only": _capi.SPARE_ONLY}[spare])
     iters = torch.zeros(S, dtype=torch.int32, device=dev)
     status = torch.zeros(S, dtype=torch.int32, device=dev)
     relres = torch.zeros(S, dtype=torch.float64, device=dev)

@@ -225,7 +225,20 @@ typedef struct colagb_ir_params {
                             = -1); 0: wait and report the largest replacement count.  The grid
                             schedule always waits (it reads its barrier-timeout flag). */
   int32_t matvec;        /* COLAGB_MATVEC_*: storage of A in the inner FP32 CG's matvec */
+  int32_t spare;         /* COLAGB_SPARE_*: the on-chip schedule's use of the SMs its clusters leave free */
 } colagb_ir_params;
+
+/* The on-chip schedule's clusters occupy 16 SMs each (7 clusters = 112 of 152 SMs at 224 KB of shared
+ * memory per CTA).  AUTO: one 512-thread CTA on each remaining SM also solves whole systems, with the
+ * same algorithm, stop rule and outputs, its vectors in global memory (L2 evict-first, so that the
+ * clusters' diagonal slots stay in L2); it claims systems from the same counter while more than ~28
+ * per resident cluster remain unclaimed, so that the clusters (that much faster per system) finish the
+ * tail.  Which kernel solved a system depends on timing, so the FP32 rounding of its iterates (not its
+ * stop rule) can differ between runs.  OFF (0, the default): clusters only.  ONLY: every system on
+ * those CTAs (a test and measurement mode). */
+#define COLAGB_SPARE_OFF 0
+#define COLAGB_SPARE_AUTO 1
+#define COLAGB_SPARE_ONLY 2
 
 /* Inner matvec storage.  FP32: the CSR values as given.  BF16 (cluster schedules only; AUTO then
  * picks the cluster schedule): off-diagonal values rounded to BF16 and a separate FP32 diagonal
@@ -348,7 +361,9 @@ int colagb_basis_combine(const void* basis, int64_t n, int64_t bs, int32_t m, co
  *  may be NULL.  evecs: batch x m x m (row-major, column j = eigenvector   *
  *  j), may be NULL.  status: batch ints, 0 = converged, 1 = iteration      *
  *  limit hit.  Each matrix is scaled by a power of two before the sweeps   *
- *  (exact), so any finite input is handled without overflow.              *
+ *  (exact), so any finite input is handled without overflow.  FP32 with   *
+ *  evecs: each eigenvalue is then replaced by the FP64 Rayleigh quotient  *
+ *  of its eigenvector (rounded to FP32), removing the sweeps' rounding.   *
  * ======================================================================== */
 /* With evecs, the rotations of the QL sweeps are recorded and replayed on the rows of the eigenvector
  * matrix by a second kernel; the record lives in a stream-ordered temporary (cudaMallocAsync /
