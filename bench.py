@@ -206,14 +206,15 @@ KERNEL_OF = {"onchip": "k_onchip_pcg", "cluster8": "k_cluster_pcg", "cluster16":
              "grid": "k_batched_ir"}
 
 
-def launches_per_solve(schedule, method, systems):
+def launches_per_solve(schedule, method, systems, spare="off"):
     """This library's kernels per timed step: the preconditioner build, then per chunk of <= 1024
     systems the on-chip schedule runs the pattern analysis (bitmap + collect, for A and, with FSAI,
-    for G) and the solve kernel; the other schedules one solve kernel."""
+    for G) and the solve kernel (plus the companion kernel with spare="auto"); the other schedules
+    one solve kernel."""
     chunks = (systems + 1023) // 1024
     build = BUILD_LAUNCHES_PER_64.get(method, 0) * ((systems + 63) // 64)
     if schedule == "onchip":
-        return build + chunks * (1 + 2 * (2 if PRECOND[method] == "fsai" else 1))
+        return build + chunks * (1 + 2 * (2 if PRECOND[method] == "fsai" else 1) + (1 if spare == "auto" else 0))
     return build + chunks
 
 
@@ -317,7 +318,8 @@ def run_ours(args, world, rank, local):
         method = "jacobi"
         build = preconditioner_builder(method, fam, dev)
     prec = PRECOND[method]
-    kw = dict(precond=prec, tol=1e-8, inner_tol=args.inner_tol, mode=args.mode, schedule=args.schedule)
+    kw = dict(precond=prec, tol=1e-8, inner_tol=args.inner_tol, mode=args.mode, schedule=args.schedule,
+              spare=args.spare)
     st = torch.cuda.current_stream(dev)
 
     side = torch.cuda.Stream(dev)  # the next step's preconditioner build
@@ -507,13 +509,13 @@ def run_ours(args, world, rank, local):
         "vs_baseline": None, "dtype": "f32-inner/f64-refinement", "data": "synthetic",
         "config": {"workload": WORKLOAD, "systems_per_gpu": args.systems, "grid": f"{args.m}x{args.m}", "n": n,
                    "nnz": nnz, "method": method, "tol": 1e-8, "refinement": args.mode, "inner_tol": args.inner_tol,
-                   "schedule": sched_ran,
+                   "schedule": sched_ran, "spare_sms": args.spare,
                    "l2": "inputs larger than L2 (CSR values + right-hand sides > 1.5 GB per step)",
                    "parallelism": f"replicas{world}"},
         "quality": quality,
         "e2e": e2e,
         "roofline": roof,
-        "gpu_launches": args.steps * launches_per_solve(sched_ran, method, args.systems),
+        "gpu_launches": args.steps * launches_per_solve(sched_ran, method, args.systems, args.spare),
         "wall_s_timed": wall,
     }
     clk_s = clk.summary()
@@ -711,6 +713,8 @@ def main():
     ap.add_argument("--inner-tol", type=float, default=None)
     ap.add_argument("--mode", default="reliable", choices=["reliable", "restart"])
     ap.add_argument("--schedule", default="auto", choices=["auto", "grid", "cluster8", "cluster16", "onchip"])
+    ap.add_argument("--spare", default="auto", choices=["off", "auto"],
+                    help="on-chip schedule: also solve systems on the SMs its clusters leave free")
     ap.add_argument("--cpu-baseline", type=int, default=1)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-seconds", type=float, default=20.0)

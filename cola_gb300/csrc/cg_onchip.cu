@@ -847,7 +847,7 @@ __device__ __forceinline__ float spare_product(const T* D, const int* off, int n
         l2_prefetch(v + 4 * (int64_t)lo, (uint32_t)((hi - lo) * 16), pol);
       }
     }
-    float4 acc[kSU], own[kSU];
+    float4 acc[kSU];
 #pragma unroll
     for (int u = 0; u < kSU; ++u) acc[u] = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll 1
@@ -869,15 +869,15 @@ __device__ __forceinline__ float spare_product(const T* D, const int* off, int n
         acc[u].y = fmaf(av.y, pv[u].y, acc[u].y);
         acc[u].z = fmaf(av.z, pv[u].z, acc[u].z);
         acc[u].w = fmaf(av.w, pv[u].w, acc[u].w);
-        if (o == 0) own[u] = pv[u];
+        // the main diagonal comes last: its operand is v's own rows and acc is complete
+        if (o == 0 && k == nk - 1) dot += dot4(pv[u], acc[u]);
       }
     }
 #pragma unroll
     for (int u = 0; u < kSU; ++u) {
       const int q = g0 + tid + u * kST;
-      if (off[nk - 1] != 0) own[u] = ld4_ef(v + 4 * (int64_t)q, pol);
+      if (off[nk - 1] != 0) dot += dot4(ld4_ef(v + 4 * (int64_t)q, pol), acc[u]);
       st4_ef(out + 4 * (int64_t)q, acc[u], pol);
-      dot += dot4(own[u], acc[u]);
     }
   }
   return dot;

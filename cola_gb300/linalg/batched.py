@@ -192,7 +192,7 @@ def solve_batched(A: BatchedCSR, B: torch.Tensor, precond: str = "jacobi", tol: 
                   inner_tol: float | None = None, max_sweeps: int = 200, max_inner_iters: int = 50000,
                   fsai: tuple | None = None, fallback: bool = True, mode: str = "reliable",
                   schedule: str = "auto", wait: bool = True, spin_limit: int = 0, matvec: str = "fp32",
-                  spare: str = "off"):
+                  spare: str = "auto"):
     """Solve A_s x_s = b_s for every system s to |b_s - A_s x_s| / |b_s| <= tol (FP64 residual).
 
     Args:
@@ -227,7 +227,8 @@ def solve_batched(A: BatchedCSR, B: torch.Tensor, precond: str = "jacobi", tol: 
         spare: the on-chip schedule's use of the SMs its clusters leave free (40 of 152 for 512 x 512):
             "auto" -- one CTA per free SM also solves whole systems (same algorithm and stop rule,
             vectors in global memory) while more than ~28 systems per cluster remain, so the clusters
-            finish the tail; "off" (default) -- clusters only; "only" -- every system on those CTAs.
+            finish the tail (default; on the 256-system 512 x 512 batch: 482 -> 454 ms per solve call);
+            "off" -- clusters only, bit-reproducible run to run; "only" -- every system on those CTAs.
     Returns (X (S, n) float64, info) with per-system iterations, status and FP64 relative residuals.
     """
     _capi.require_cuda(A.values, B)

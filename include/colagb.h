@@ -234,8 +234,9 @@ typedef struct colagb_ir_params {
  * clusters' diagonal slots stay in L2); it claims systems from the same counter while more than ~28
  * per resident cluster remain unclaimed, so that the clusters (that much faster per system) finish the
  * tail.  Which kernel solved a system depends on timing, so the FP32 rounding of its iterates (not its
- * stop rule) can differ between runs.  OFF (0, the default): clusters only.  ONLY: every system on
- * those CTAs (a test and measurement mode). */
+ * stop rule) can differ between runs.  OFF (0, the zero-initialised value): clusters only, the same
+ * bits run to run.  ONLY: every system on those CTAs (a test and measurement mode).  The Python layer's
+ * solve_batched asks for AUTO unless told otherwise. */
 #define COLAGB_SPARE_OFF 0
 #define COLAGB_SPARE_AUTO 1
 #define COLAGB_SPARE_ONLY 2

@@ -290,6 +290,36 @@ def test_lanczos_known_answers(golden, case):
     np.testing.assert_allclose(Tm.alpha[:, :, 0].cpu().numpy(), g["alpha"], rtol=1e-5, atol=1e-6)
 
 
+@pytest.mark.parametrize("m", [120, 450])
+def test_lanczos_fp32_fused_reorthogonalisation(m):
+    """Single-vector FP32 Lanczos fuses the first CGS pass's subtraction with the second pass's
+    projection up to step 400 (beyond it the two run apart): the basis stays orthonormal to FP32
+    accuracy and the five isolated top Ritz values equal the FP64 run's."""
+    from cola_gb300.workloads import diffusion_family_2d
+    fam, _, _, _ = diffusion_family_2d([3], m=128, device=DEV)
+    n = fam.n
+    ip, ix, v = fam.indptr, fam.indices, fam.values[0]
+    start = torch.randn(n, 1, generator=torch.Generator().manual_seed(1), dtype=torch.float64)
+    from cola_gb300.linalg.lanczos import run_lanczos
+    Qs, ev = {}, {}
+    spikes = torch.zeros(n, dtype=torch.float64)
+    spikes[torch.randperm(n, generator=torch.Generator().manual_seed(2))[:5]] = torch.tensor([300., 250, 200, 150, 100])
+    for dt in (torch.float32, torch.float64):
+        A = cola.ops.Sparse.from_csr(ip, ix, v.to(dt), (n, n)) + cola.ops.Diagonal(spikes.to(DEV, dt))
+        r = run_lanczos(A, start.to(DEV, dt), m, 1e-12)
+        alpha, beta, Q = r.alpha_beta_q()  # alpha (1, k-1), beta (1, k), Q (k, n, 1)
+        Qs[dt] = Q[:, :, 0].double()
+        T = np.diag(beta[0].double().cpu().numpy())
+        if alpha.shape[1] > 0:
+            off = alpha[0].double().cpu().numpy()
+            T += np.diag(off, 1) + np.diag(off, -1)
+        ev[dt] = np.sort(np.linalg.eigvalsh(T))[-5:]
+    Q32 = Qs[torch.float32]
+    G = Q32 @ Q32.T
+    assert float((G - torch.eye(G.shape[0], device=DEV, dtype=torch.float64)).abs().max()) < 1e-4
+    assert np.max(np.abs(ev[torch.float32] - ev[torch.float64]) / np.abs(ev[torch.float64])) < 1e-5
+
+
 def test_eig_lanczos_golden(golden):
     g = golden("eig_lanczos")
     op = cola.SelfAdjoint(cola.ops.Dense(T(g["A"])))
