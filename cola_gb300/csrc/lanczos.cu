@@ -248,124 +248,6 @@ __global__ void __launch_bounds__(256) k_lz_project1(const float* __restrict__ b
   }
 }
 
-// The middle of CGS2 fused (bs == 1, FP32): the first pass's subtraction w <- w - V h1 and the second
-// pass's projection h2 = V^T w, reading each filled slot's rows once instead of twice.  Block blk owns
-// the same rows as k_lz_project1; it walks them in sub-chunks of kSubRows rows whose slot rows are
-// staged in shared memory (16-byte cp.async, double-buffered, so the next sub-chunk streams in while
-// this one is used).  Per sub-chunk: thread (g, js) sums slots js + 1, js + 17, ... of row group g,
-// the 16 partial float4s are added in a fixed order and subtracted from w; then half-warp hw forms
-// the dot of slots hw + 1, hw + 17, ... with the new rows and accumulates it in shared memory.  The
-// per-block partials go to hpart as k_lz_project1's do.
-constexpr int kSubRows = 64;        // rows per sub-chunk (16 float4 groups)
-constexpr int kFusedMaxSlots = 400;  // staged slots: 2 x 400 x 256 B = 200 KB of shared memory
-
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
-
-static size_t subproj1_smem(int imax) {
-  return (size_t)2 * imax * 16 * sizeof(float4) + 256 * sizeof(float4) + 16 * sizeof(float4) +
-         (size_t)(imax + 1) * sizeof(float);
-}
-
-__global__ void __launch_bounds__(256) k_lz_subproj1(const float* __restrict__ basis, float* __restrict__ w,
-                                                     int64_t n, int64_t chunk, int64_t slots, int imax,
-                                                     LzState<float> s) {
-  if (*s.done) return;
-  const int i = *s.step;  // <= imax (the host's bound on the step)
-  extern __shared__ float4 fsm[];
-  float4* stage = fsm;                              // [2][imax][16]
-  float4* red = stage + 2 * (int64_t)imax * 16;     // [16][16]
-  float4* w1 = red + 256;                           // [16]
-  float* acc = reinterpret_cast<float*>(w1 + 16);   // [imax + 1]
-  const int t = threadIdx.x;
-  const int64_t r0 = (int64_t)blockIdx.x * chunk;
-  const int64_t r1 = r0 + chunk < n ? r0 + chunk : n;
-  if (r0 >= r1) return;
-  const int nsub = (int)((r1 - r0 + kSubRows - 1) / kSubRows);
-  for (int j = t; j <= i; j += 256) acc[j] = 0.f;
-  auto groups = [&](int k) {  // valid float4 groups of sub-chunk k (r1 - r0 is a multiple of 4)
-    const int64_t left = (r1 - r0 - (int64_t)k * kSubRows) / 4;
-    return (int)(left < 16 ? left : 16);
-  };
-  auto stage_load = [&](int k) {
-    float4* buf = stage + (int64_t)(k & 1) * imax * 16;
-    const int64_t rs = r0 + (int64_t)k * kSubRows;
-    const int gl = groups(k);
-    for (int e = t; e < i * 16; e += 256) {
-      const int j = 1 + (e >> 4), g = e & 15;
-      if (g < gl) cp_async16(buf + (int64_t)(j - 1) * 16 + g, basis + (int64_t)j * n + rs + 4 * g);
-    }
-    cp_async_commit();
-  };
-  stage_load(0);
-  const int g = t & 15, js = t >> 4;  // step 1: row group, slot set
-  const int rounds = (i + 15) / 16;   // step 2: slots per half-warp (uniform across the warp)
-  for (int k = 0; k < nsub; ++k) {
-    if (k + 1 < nsub) stage_load(k + 1);
-    else cp_async_commit();  // an empty group keeps the wait count uniform
-    cp_async_wait<1>();
-    __syncthreads();  // sub-chunk k staged for every thread
-    const float4* buf = stage + (int64_t)(k & 1) * imax * 16;
-    const int64_t rs = r0 + (int64_t)k * kSubRows;
-    const int gl = groups(k);
-    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (g < gl)
-      for (int j = 1 + js; j <= i; j += 16) {
-        const float4 v = buf[(int64_t)(j - 1) * 16 + g];
-        const float h = s.hbuf[j];
-        p.x += v.x * h;
-        p.y += v.y * h;
-        p.z += v.z * h;
-        p.w += v.w * h;
-      }
-    red[js * 16 + g] = p;
-    __syncthreads();
-    if (t < gl) {
-      float4 sum = make_float4(0.f, 0.f, 0.f, 0.f);
-      for (int q = 0; q < 16; ++q) {
-        const float4 r = red[q * 16 + t];
-        sum.x += r.x;
-        sum.y += r.y;
-        sum.z += r.z;
-        sum.w += r.w;
-      }
-      float4 wv = *reinterpret_cast<const float4*>(w + rs + 4 * t);
-      wv.x -= sum.x;
-      wv.y -= sum.y;
-      wv.z -= sum.z;
-      wv.w -= sum.w;
-      w1[t] = wv;
-      *reinterpret_cast<float4*>(w + rs + 4 * t) = wv;
-    }
-    __syncthreads();
-    const int hw = t >> 4, l = t & 15;
-    for (int rd = 0; rd < rounds; ++rd) {
-      const int j = 1 + hw + 16 * rd;
-      float d = 0.f;
-      if (j <= i && l < gl) {
-        const float4 v = buf[(int64_t)(j - 1) * 16 + l], x = w1[l];
-        d = v.x * x.x + v.y * x.y + v.z * x.z + v.w * x.w;
-      }
-      d += __shfl_xor_sync(0xffffffffu, d, 8);
-      d += __shfl_xor_sync(0xffffffffu, d, 4);
-      d += __shfl_xor_sync(0xffffffffu, d, 2);
-      d += __shfl_xor_sync(0xffffffffu, d, 1);
-      if (l == 0 && j <= i) acc[j] += d;
-    }
-    __syncthreads();  // buffer k & 1, red and w1 free again
-  }
-  cp_async_wait<0>();
-  float* out = s.hpart + (int64_t)blockIdx.x * slots;
-  for (int j = 1 + t; j <= i; j += 256) out[j] = acc[j];
-}
-
 // Block form (bs in {4, 8, 16, 32, 64, 128}, FP32): block blk owns rows [blk * chunk, ...), i.e. one
 // contiguous run of chunk * bs floats per slot.  w's run is staged in shared memory; warp q takes
 // slots j = 1 + q, 1 + q + nwarps, ...; a warp step covers 128 consecutive floats, so lane l always
@@ -881,13 +763,6 @@ static int lanczos_t(const colagb_op* A, const T* V0, int64_t ldv0, int64_t bs, 
       }
     }
   }
-  // steps up to fused_imax fuse the first pass's subtraction with the second pass's projection
-  int fused_imax = 0;
-  if (p1) {
-    fused_imax = std::min(m, kFusedMaxSlots);
-    COLAGB_CUDA(cudaFuncSetAttribute(k_lz_subproj1, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)subproj1_smem(fused_imax)));
-  }
   int host_step = 1;  // the step index the next launch group starts at (upper bound)
   int hdone = 0;
   while (true) {
@@ -902,17 +777,7 @@ static int lanczos_t(const colagb_op* A, const T* V0, int64_t ldv0, int64_t bs, 
       COLAGB_TRY(op_apply<T>(A, A->root, vi, bs, 0, w, bs, 0, bs, 1, T(1), T(0), ow, s.done, st));
       k_lz_alpha<T><<<nb, 256, 0, st>>>(w, vi, n, bs, diag, m, s);
       k_lz_three_term<T><<<eg, 256, 0, st>>>(w, vi, vim1, n, bs, diag, subdiag, m, s);
-      const bool fused = p1 && i <= fused_imax;
       for (int pass = 0; pass < 2; ++pass) {
-        if (fused && pass == 1) {
-          // pass 0's subtraction and pass 1's projection in one sweep over the basis (k_lz_subproj1)
-          if constexpr (std::is_same<T, float>::value)
-            k_lz_subproj1<<<nb1, 256, subproj1_smem(fused_imax), st>>>(basis, w, n, chunk, slots, fused_imax, s);
-          k_lz_reduce_h<T><<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div((int64_t)(i + 1) * bs, 8), 4096)),
-                             256, 0, st>>>(nb1, bs, slots, s);
-          k_lz_subtract<T><<<eg, 256, 0, st>>>(basis, w, n, bs, s);
-          break;
-        }
         if constexpr (std::is_same<T, float>::value) {
           if (p1)
             k_lz_project1<<<nb1, 256, chunk * sizeof(float), st>>>(basis, w, n, chunk, slots, s);
@@ -925,7 +790,7 @@ static int lanczos_t(const colagb_op* A, const T* V0, int64_t ldv0, int64_t bs, 
         }
         k_lz_reduce_h<T><<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div((int64_t)(i + 1) * bs, 8), 4096)),
                            256, 0, st>>>((p1 || pq) ? nb1 : nb, bs, slots, s);
-        if (!(fused && pass == 0)) k_lz_subtract<T><<<eg, 256, 0, st>>>(basis, w, n, bs, s);
+        k_lz_subtract<T><<<eg, 256, 0, st>>>(basis, w, n, bs, s);
       }
       k_lz_finish<T><<<nb, 256, 0, st>>>(w, n, bs, subdiag, m, prm.tol, s);
       COLAGB_CUDA(cudaGetLastError());
