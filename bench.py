@@ -218,6 +218,21 @@ def launches_per_solve(schedule, method, systems, spare="off"):
     return build + chunks
 
 
+def companion_roofline(systems, mean_steps, n, nd, nm, solve_s, hbm_peak):
+    """The on-chip schedule's companion CTAs (one per SM the clusters leave free) stream each system
+    they solve from global memory: per CG step and row the matrix (nd FP32 + nm bfloat16 diagonals)
+    and 48 B of FP32 vector traffic (A p: p read, A p written; r update: r r/w, A p read; M r: r read,
+    z written; p / d update: z read, p r/w, d r/w).  `systems` is what they solved in the waited
+    warm-up step of the same batch (the split between the two kernels varies a little run to run)."""
+    if systems is None:
+        return None
+    per_row = nd * 4 + nm * 2 + 48
+    nbytes = systems * mean_steps * per_row * n
+    return {"systems_per_step": systems, "bytes_per_row_step": per_row, "dram_bytes_est": nbytes,
+            "dram_gbs_est": nbytes / solve_s / 1e9, "dram_frac_est": nbytes / solve_s / 1e9 / hbm_peak,
+            "note": "the companions' DRAM traffic is not in `traffic` (an ncu capture of the clusters alone)"}
+
+
 def read_bandwidth(dev, nbytes: int, reps=(2, 12), tries: int = 3) -> float:
     """Read bandwidth in GB/s of this library's streaming probe over an nbytes buffer: the time of
     reps[1] - reps[0] extra passes (CUDA events on the launching stream, best of `tries`).  A buffer
@@ -360,6 +375,7 @@ def run_ours(args, world, rank, local):
 
     X, infos = run_steps(max(1, args.warmup), wait_first=True)
     sweeps_max = infos[0]["sweeps"]  # the timed steps solve the same systems
+    companion_systems = infos[0].get("companion_systems")
     torch.cuda.synchronize()
     b0, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     b0.record(st)
@@ -496,6 +512,8 @@ def run_ours(args, world, rank, local):
                        "HBM streaming of the CSR values and Krylov vectors",
             "kernel": KERNEL_OF.get(sched_ran, "k_cluster_pcg"), "schedule": sched_ran,
             "alg_bytes_per_launch": alg_bytes_step,
+            "companions": companion_roofline(companion_systems, iters_total / args.steps / args.systems,
+                                             n, nd, nm, solve_s, hbm_peak) if onchip else None,
             "solve_ms_per_step": 1e3 * solve_s,
             "build_ms_alone": build_ms,
             "build_overlap": "step i + 1's build runs beside step i's solve on a second stream"}

@@ -78,7 +78,7 @@ class IrParams(C.Structure):
 
 class IrResult(C.Structure):
     _fields_ = [("sweeps", C.c_int32), ("total_inner_iters", C.c_int32), ("status", C.c_int32),
-                ("schedule", C.c_int32)]
+                ("schedule", C.c_int32), ("companion_systems", C.c_int32)]
 
 
 class LanczosParams(C.Structure):

@@ -664,7 +664,7 @@ static bool use_block(const colagb_batched_csr& A, const colagb_ir_params& prm) 
 }
 int onchip_pcg_solve(const colagb_batched_csr* A, const double* B, double* X, const colagb_ir_params* prm,
                      int32_t* iters, int32_t* status, double* relres, int* nrep, void* ws, size_t ws_bytes,
-                     bool* used, cudaStream_t st);
+                     bool* used, unsigned int** companion_solved, cudaStream_t st);
 
 static BatchedWs carve_batched(Bump& ws, const colagb_batched_csr& A, const colagb_ir_params& prm) {
   const int64_t S = A.num_systems < kMaxBatch ? A.num_systems : kMaxBatch;
@@ -777,6 +777,7 @@ extern "C" int colagb_cg_batched_csr_solve(const colagb_batched_csr* A, const do
   result->total_inner_iters = 0;
   result->status = COLAGB_OK;
   result->schedule = params->schedule;
+  result->companion_systems = 0;
   if (S_all == 0 || A->n == 0) return COLAGB_OK;
   if (!B || !X) return fail(COLAGB_ERR_INVALID, "batched CG: null B/X");
   if (A->n % 4 != 0 || (uintptr_t)B % 16 != 0 || (uintptr_t)X % 16 != 0)
@@ -804,11 +805,12 @@ extern "C" int colagb_cg_batched_csr_solve(const colagb_batched_csr* A, const do
     sub.values = A->values + (A->shared_values ? 0 : s0 * A->nnz);
     sub.g_values = A->g_values ? A->g_values + s0 * A->g_nnz : nullptr;
     bool used = false;
+    unsigned int* comp = nullptr;
     if (try_onchip)
       COLAGB_TRY(onchip_pcg_solve(&sub, B + s0 * A->n, X + s0 * A->n, params,
                                   per_system_iters ? per_system_iters + s0 : nullptr,
                                   per_system_status ? per_system_status + s0 : nullptr, relres ? relres + s0 : nullptr,
-                                  w.nrep, w.onchip, w.onchip_bytes, &used, st));
+                                  w.nrep, w.onchip, w.onchip_bytes, &used, &comp, st));
     if (!used && params->schedule == COLAGB_SCHED_ONCHIP)
       return fail(COLAGB_ERR_UNSUPPORTED,
                   "batched CG: the on-chip schedule needs a pattern of at most 9 diagonals (FSAI: G lower "
@@ -825,12 +827,17 @@ extern "C" int colagb_cg_batched_csr_solve(const colagb_batched_csr* A, const do
                                      csize, w.v16, w.dg16, st));
       if (params->no_wait) {
         result->sweeps = -1;
+        result->companion_systems = -1;
         continue;
       }
       int mx[2] = {0, 0};
       std::vector<int> hrep(S);
+      unsigned int hcomp = 0;
       COLAGB_CUDA(cudaMemcpyAsync(hrep.data(), w.nrep, S * sizeof(int), cudaMemcpyDeviceToHost, st));
+      if (used && comp)
+        COLAGB_CUDA(cudaMemcpyAsync(&hcomp, comp, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
       COLAGB_CUDA(cudaStreamSynchronize(st));
+      result->companion_systems += (int32_t)hcomp;
       for (int64_t q = 0; q < S; ++q) mx[0] = hrep[q] > mx[0] ? hrep[q] : mx[0];
       result->sweeps = mx[0] > result->sweeps ? mx[0] : result->sweeps;
       continue;

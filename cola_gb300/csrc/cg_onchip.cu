@@ -731,6 +731,7 @@ struct SpareArgs {
   int64_t np;        // rows padded to kSpareRowAlign
   int H;             // halo float4s on each side (multiple of 4 rows, <= np / 4)
   int reserve;       // claim only while more than this many systems are unclaimed
+  unsigned int* solved;  // systems these CTAs solved
 };
 
 // floats of one spare CTA's region for n rows: A diagonals, 1/diag, G diagonals, M (bfloat16, in
@@ -1233,6 +1234,7 @@ __global__ void __launch_bounds__(kST, 1) k_spare_pcg(const __grid_constant__ On
       if (a.out_iters) a.out_iters[s] = it;
       if (a.out_relres) a.out_relres[s] = relres;
       if (a.out_nrep) a.out_nrep[s] = nrep;
+      atomicAdd(sp.solved, 1u);
     }
     __syncthreads();
   }
@@ -1437,8 +1439,9 @@ static int onchip_active_clusters(size_t smem, int* nclusters) {
 // caller whether it ran.
 int onchip_pcg_solve(const colagb_batched_csr* Acsr, const double* B, double* X, const colagb_ir_params* prm,
                      int32_t* iters, int32_t* status, double* relres, int* nrep, void* ws, size_t ws_bytes,
-                     bool* used, cudaStream_t st) {
+                     bool* used, unsigned int** companion_solved, cudaStream_t st) {
   *used = false;
+  *companion_solved = nullptr;
   const int64_t n = Acsr->n;
   const bool fsai = prm->preconditioner == COLAGB_PREC_FSAI;
   int R = 0, G = 0;
@@ -1542,7 +1545,8 @@ int onchip_pcg_solve(const colagb_batched_csr* Acsr, const double* B, double* X,
   a.prec_kind = prm->preconditioner;
   a.fallback = prm->fallback;
   a.mode = prm->mode;
-  COLAGB_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned int), st));
+  COLAGB_CUDA(cudaMemsetAsync(counter, 0, 2 * sizeof(unsigned int), st));  // system counter, companion count
+  *companion_solved = counter + 1;
   // companion CTAs on the free SMs (prm->spare: AUTO, OFF, or ONLY for tests)
   const int spare_mode = prm->spare;
   const int64_t nps = spare_rows(n);
@@ -1559,6 +1563,7 @@ int onchip_pcg_solve(const colagb_batched_csr* Acsr, const double* B, double* X,
     sp.per_cta = spare_cta_floats(n, fsai);
     sp.np = nps;
     sp.H = H;
+    sp.solved = counter + 1;
     // a cluster solves a system ~kSpareRatio times faster than one CTA does: leave the clusters that many
     // systems each at the end, so that no companion solve outlasts the clusters' last one
     int nc = 0;

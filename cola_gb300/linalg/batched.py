@@ -286,5 +286,6 @@ def solve_batched(A: BatchedCSR, B: torch.Tensor, precond: str = "jacobi", tol: 
     swp = int(res.sweeps) if res.sweeps >= 0 else None
     info = {"iterations": iters, "status": status, "relres": relres, "replacements": swp,
             "sweeps": swp, "max_iterations": int(res.total_inner_iters),
-            "schedule": _SCHED_NAME.get(int(res.schedule), "auto")}
+            "schedule": _SCHED_NAME.get(int(res.schedule), "auto"),
+            "companion_systems": int(res.companion_systems) if res.companion_systems >= 0 else None}
     return X, info

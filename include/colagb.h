@@ -276,6 +276,8 @@ typedef struct colagb_ir_result {
   int32_t total_inner_iters;   /* sum over sweeps of the max inner iterations */
   int32_t status;              /* COLAGB_OK or COLAGB_ERR_TIMEOUT */
   int32_t schedule;            /* the COLAGB_SCHED_* that ran (AUTO resolved) */
+  int32_t companion_systems;   /* systems solved by the on-chip schedule's companion CTAs (0 without
+                                  them, -1 with no_wait) */
 } colagb_ir_result;
 
 /* B: num_systems x n FP64 right-hand sides; X: num_systems x n FP64 solutions (out).
