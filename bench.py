@@ -223,7 +223,7 @@ def companion_roofline(systems, mean_steps, n, nd, nm, solve_s, hbm_peak):
     they solve from global memory: per CG step and row the matrix (nd FP32 + nm bfloat16 diagonals)
     and 48 B of FP32 vector traffic (A p: p read, A p written; r update: r r/w, A p read; M r: r read,
     z written; p / d update: z read, p r/w, d r/w).  `systems` is what they solved in the waited
-    warm-up step of the same batch (the split between the two kernels varies a little run to run)."""
+    last warm-up step of the same batch (the split between the two kernels varies a little run to run)."""
     if systems is None:
         return None
     per_row = nd * 4 + nm * 2 + 48
@@ -349,7 +349,7 @@ def run_ours(args, world, rank, local):
             ready.record(side)
         return fs, ready
 
-    def run_steps(k, marks=None, wait_first=False):
+    def run_steps(k, marks=None, wait_last=False):
         """k steps on the resident family.  Step i's solve runs on the main stream; step i + 1's
         preconditioner is built on the side stream meanwhile, on the SMs that the solve's persistent
         clusters leave free (112 of the 152 hold the on-chip schedule).  Each step still builds its
@@ -363,7 +363,7 @@ def run_ours(args, world, rank, local):
             st.wait_event(ready)
             if marks:
                 marks[i][0].record(st)
-            X, info = solve_batched(fam, B, fsai=fs, wait=wait_first and i == 0, **kw)
+            X, info = solve_batched(fam, B, fsai=fs, wait=wait_last and i == k - 1, **kw)
             if marks:
                 marks[i][1].record(st)
             if fs is not None:
@@ -373,9 +373,9 @@ def run_ours(args, world, rank, local):
                 fs, ready = build_on_side(fam)
         return X, infos
 
-    X, infos = run_steps(max(1, args.warmup), wait_first=True)
-    sweeps_max = infos[0]["sweeps"]  # the timed steps solve the same systems
-    companion_systems = infos[0].get("companion_systems")
+    X, infos = run_steps(max(1, args.warmup), wait_last=True)
+    sweeps_max = infos[-1]["sweeps"]  # the timed steps solve the same systems
+    companion_systems = infos[-1].get("companion_systems")
     torch.cuda.synchronize()
     b0, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     b0.record(st)

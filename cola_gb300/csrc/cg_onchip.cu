@@ -1370,7 +1370,11 @@ static const SpareStreams* spare_streams() {
     if (e.ctx == id) return &e;
   SpareStreams e;
   e.ctx = id;
-  if (cudaStreamCreateWithFlags(&e.st, cudaStreamNonBlocking) != cudaSuccess ||
+  // load the companion kernel now: with lazy module loading its first launch would otherwise load it
+  // then, which waits for the clusters' kernel already running, and the companions would start late
+  cudaFuncAttributes fa;
+  if (cudaFuncGetAttributes(&fa, k_spare_pcg) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&e.st, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&e.fork, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&e.join, cudaEventDisableTiming) != cudaSuccess) {
     cudaGetLastError();
