@@ -689,6 +689,132 @@ def cpu_baseline(args, fam, B, sample_s=15.0):
             "seconds": t_used}
 
 
+def _reference_csr(cola_ref, indptr, indices, vals, n):
+    """The reference's Sparse operator for a CSR matrix; where its construction reorders the values
+    (an unstable argsort, operators.py:64-76), the same CSR product (Sparse._matmat, operators.py:77-78)
+    in the reference's LinearOperator base class.  Returns (operator, description)."""
+    indptr, indices = indptr.long(), indices.long()
+    rows = torch.repeat_interleave(torch.arange(n), indptr[1:] - indptr[:-1])
+    Acsr = torch.sparse_csr_tensor(indptr, indices, vals, (n, n))
+    A0 = cola_ref.ops.Sparse(vals, rows, indices, (n, n))
+    probe = torch.randn(n, dtype=vals.dtype, generator=torch.Generator().manual_seed(0))
+    if torch.allclose(A0 @ probe, Acsr @ probe, rtol=1e-5, atol=1e-6):
+        return A0, "Sparse"
+
+    class _CSR(cola_ref.ops.LinearOperator):
+        def __init__(self, M):
+            super().__init__(dtype=M.dtype, shape=M.shape)
+            self.M = M
+
+        def _matmat(self, X):
+            return self.M @ X
+    return _CSR(Acsr), "LinearOperator(CSR @ X)"
+
+
+def _reference_lanczos_step_seconds(cola_ref, op, rhs, m, k_steps=3):
+    """Seconds per step of the reference's own Lanczos (lanczos_fact's body, lanczos.py:238-253) on the
+    operator and start block, with the (bs, n, m + 2) basis of an m-step run: its loop driver is
+    replaced for the duration by one that runs k_steps of the body (after one untimed step) and stops.
+    The reference reorthogonalises against all m + 2 columns at every step (lanczos.py:287-296), so every
+    step costs the same and a run costs m of them."""
+    from cola.linalg.decompositions import lanczos as ref_lanczos
+    xnp = op.xnp
+    timing = {}
+    original = xnp.while_loop_winfo
+
+    def bounded(error, tol, max_iters, pbar=False, **kw):
+        def while_fn(cond_fun, body_fun, state):
+            state = body_fun(state)
+            t0 = time.perf_counter()
+            for _ in range(k_steps):
+                state = body_fun(state)
+            timing["t"] = (time.perf_counter() - t0) / k_steps
+            return state
+        return while_fn, {}
+    xnp.while_loop_winfo = bounded
+    try:
+        init = ref_lanczos.init_lanczos(xnp, rhs, m, op.dtype)
+        ref_lanczos.lanczos_fact(op, init, max_iters=m, tol=0.0)
+    finally:
+        xnp.while_loop_winfo = original
+    return timing["t"]
+
+
+def config_reference_cpu(config):
+    """The reference package on the host cores (all threads) for a benchmark configuration, on a bounded
+    sample of the workload (stated in `sample`), same inputs as the GPU line.  None without the package."""
+    cola_ref = reference_package()
+    if cola_ref is None:
+        return {"unavailable": "the reference package is not installed in baseline/_ref"}
+    threads = os.cpu_count() or 1
+    torch.set_num_threads(threads)
+    from cola_gb300 import workloads as W
+    out = {"kind": "reference", "cores": threads}
+    if config == "c1":
+        A, b, _ = W.dense_spd(2048, seed=0, lo=1e-2, hi=1e2, dtype=torch.float32)
+        t0 = time.perf_counter()
+        Ainv = cola_ref.linalg.inv(cola_ref.PSD(cola_ref.ops.Dense(A)), cola_ref.linalg.CG(tol=1e-6, max_iters=2000))
+        x = Ainv @ b
+        t = time.perf_counter() - t0
+        out.update(value=1.0 / t, unit="solves/s", seconds=t,
+                   sample=f"one full FP32 solve, {int(Ainv.info['iterations'])} CG iterations")
+    elif config == "c2":
+        ip, ix, v = W.diffusion_3d(m=128, device="cpu")
+        n = ip.numel() - 1
+        A, kind = _reference_csr(cola_ref, ip, ix, v, n)
+        rows = torch.repeat_interleave(torch.arange(n), (ip[1:] - ip[:-1]).long())
+        dg = torch.zeros(n).index_add_(0, rows, torch.where(rows == ix.long(), v, torch.zeros_like(v)))
+        Bm = torch.randn(n, 32, generator=torch.Generator().manual_seed(2))
+        its = 50
+        alg = cola_ref.linalg.CG(tol=1e-30, max_iters=its, P=cola_ref.ops.Diagonal(1.0 / dg))
+        t0 = time.perf_counter()
+        X = cola_ref.linalg.inv(cola_ref.PSD(A), alg) @ Bm
+        t = time.perf_counter() - t0
+        steps = 427  # Jacobi-PCG steps to a 1e-8 FP64 residual on this operator (the GPU line's count)
+        out.update(value=32.0 / (t / its * steps), unit="rhs/s", seconds=t,
+                   sample=f"{its} Jacobi-PCG iterations of all 32 right-hand sides on the reference's {kind} "
+                          f"(FP32), extrapolated to the {steps} iterations a 1e-8 residual takes")
+    elif config == "c3a":
+        mats, rhs, meta = W.rbf_systems(num=256, seed=3, device="cpu")
+        done, t = 0, 0.0
+        for A, b in zip(mats, rhs):
+            t0 = time.perf_counter()
+            cola_ref.linalg.inv(cola_ref.PSD(cola_ref.ops.Dense(A)), cola_ref.linalg.CG(tol=1e-6, max_iters=2000)) @ b
+            t += time.perf_counter() - t0
+            done += 1
+            if t > 20.0:
+                break
+        out.update(value=done / t, unit="systems/s", seconds=t,
+                   sample=f"the first {done} of the 256 systems, one reference CG call each (FP32)")
+    elif config == "c3b":
+        Ks, _ = W.kron_rbf(seed=4, device="cpu")
+        K = cola_ref.ops.Kronecker(*[cola_ref.ops.Dense(k) for k in Ks])
+        op = cola_ref.PSD(K + 0.01 * cola_ref.ops.I_like(K))
+        bs, steps = 8, 100
+        from cola_gb300.linalg.prng import randn as keyed_randn
+        Z = torch.sign(keyed_randn(op.shape[0], 64, dtype=torch.float32, key=5))[:, :bs].contiguous()
+        t = _reference_lanczos_step_seconds(cola_ref, op, Z, steps)
+        total = t * steps * (64 / bs)
+        out.update(value=1.0 / total, unit="logdets/s", seconds=t,
+                   sample=f"3 steps of the reference's own Lanczos on {bs} of the 64 probes with the 102-column "
+                          f"basis (per step {t:.2f} s), times {steps} steps and 64/{bs}")
+    elif config == "c5":
+        A1, _, _ = W.dense_spd(1024, seed=6, lo=1e-2, hi=1e1, dtype=torch.float32)
+        A2, _, _ = W.dense_spd(1024, seed=61, lo=1e-2, hi=1e1, dtype=torch.float32)
+        n = 1 << 20
+        ip, ix, v = W.rgg_laplacian(n, 0.002, seed=7, device="cpu")
+        L, kind = _reference_csr(cola_ref, ip, ix, v, n)
+        op = cola_ref.SelfAdjoint(cola_ref.ops.Kronecker(cola_ref.ops.Dense(A1), cola_ref.ops.Dense(A2)) + L)
+        steps = 256
+        from cola_gb300.linalg.prng import PRNGKey, randn as keyed_randn
+        start = keyed_randn(n, dtype=torch.float32, key=PRNGKey(42))[:, None]
+        t = _reference_lanczos_step_seconds(cola_ref, op, start, steps)
+        out.update(value=1.0 / (t * steps), unit="eigensolves/s", seconds=t,
+                   sample=f"3 steps of the reference's own Lanczos (Kronecker + {kind}, 258-column basis; per step "
+                          f"{t:.2f} s), times {steps} steps")
+    return out
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return None
@@ -743,7 +869,10 @@ def main():
         from cola_gb300 import _capi, configs
         _capi.load()
         if rank == 0:
-            print(json.dumps(configs.RUNNERS[args.config]()))
+            line = configs.RUNNERS[args.config]()
+            if args.cpu_baseline:
+                line["cpu_reference"] = config_reference_cpu(args.config)
+            print(json.dumps(line))
         return
     if args.impl == "reference":
         out = run_reference(args, world, rank)
