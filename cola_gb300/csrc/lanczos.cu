@@ -71,6 +71,94 @@ __device__ __forceinline__ void lz_partials(int64_t n, int64_t bs, F f, T* out, 
   }
 }
 
+// The same per-column sums of a[r][b] * c[r][b] for FP32 blocks with bs a multiple of 4 (bs <= 1024):
+// thread t takes column quad t % (bs / 4) and rows t / (bs / 4), t / (bs / 4) + rpp, ... with 128-bit
+// loads, four rows per round on independent accumulators (a thread per column and row with scalar
+// loads waited on one load at a time: ~0.6 TB/s on 64-column blocks).  Row slots are then summed in a
+// fixed tree as in lz_partials.
+__device__ __forceinline__ void lz_partials4(int64_t n, int64_t bs, const float* __restrict__ a,
+                                             const float* __restrict__ c, float4* out4, float4* smem4) {
+  const int t = threadIdx.x;
+  const int qd = (int)(bs / 4);
+  const int rpp = (int)blockDim.x / qd;
+  const int my_q = t % qd, my_r = t / qd;
+  float4 acc[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) acc[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (my_r < rpp) {
+    const int64_t stride = (int64_t)rpp * gridDim.x;
+    int64_t r = (int64_t)blockIdx.x * rpp + my_r;
+    for (; r + 3 * stride < n; r += 4 * stride) {
+      float4 x[4], y[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int64_t o = (r + u * stride) * bs + 4 * my_q;
+        x[u] = __ldg(reinterpret_cast<const float4*>(a + o));
+        y[u] = __ldg(reinterpret_cast<const float4*>(c + o));
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        acc[u].x += x[u].x * y[u].x;
+        acc[u].y += x[u].y * y[u].y;
+        acc[u].z += x[u].z * y[u].z;
+        acc[u].w += x[u].w * y[u].w;
+      }
+    }
+    for (; r < n; r += stride) {
+      const int64_t o = r * bs + 4 * my_q;
+      const float4 x = __ldg(reinterpret_cast<const float4*>(a + o)), y = __ldg(reinterpret_cast<const float4*>(c + o));
+      acc[0].x += x.x * y.x;
+      acc[0].y += x.y * y.y;
+      acc[0].z += x.z * y.z;
+      acc[0].w += x.w * y.w;
+    }
+  }
+  float4 tot;
+  tot.x = (acc[0].x + acc[1].x) + (acc[2].x + acc[3].x);
+  tot.y = (acc[0].y + acc[1].y) + (acc[2].y + acc[3].y);
+  tot.z = (acc[0].z + acc[1].z) + (acc[2].z + acc[3].z);
+  tot.w = (acc[0].w + acc[1].w) + (acc[2].w + acc[3].w);
+  smem4[t] = tot;
+  __syncthreads();
+  for (int w = rpp; w > 1;) {
+    const int h = (w + 1) >> 1;
+    if (my_r < w - h) {
+      const float4 o = smem4[t + h * qd];
+      smem4[t].x += o.x;
+      smem4[t].y += o.y;
+      smem4[t].z += o.z;
+      smem4[t].w += o.w;
+    }
+    __syncthreads();
+    w = h;
+  }
+  if (t < qd) out4[t] = smem4[t];
+  __syncthreads();
+}
+
+// Column sums of a .* c into this CTA's partials: the 128-bit path for FP32 blocks of 4..1024 columns
+// and for single FP32 columns with n % 4 == 0 (16-byte aligned), the generic one otherwise.
+template <class T>
+__device__ __forceinline__ void lz_colsum(int64_t n, int64_t bs, const T* a, const T* c, T* out, T* smem) {
+  if constexpr (std::is_same<T, float>::value) {
+    const bool al = (reinterpret_cast<uintptr_t>(a) % 16) == 0 && (reinterpret_cast<uintptr_t>(c) % 16) == 0;
+    if (al && bs % 4 == 0 && bs <= 1024) {
+      __shared__ float4 smem4[256];
+      lz_partials4(n, bs, a, c, reinterpret_cast<float4*>(out), smem4);
+      return;
+    }
+    if (al && bs == 1 && n % 4 == 0) {  // one column: four consecutive rows per 128-bit load
+      __shared__ float4 smem4b[256];
+      __shared__ float4 quad;
+      lz_partials4(n / 4, 4, a, c, &quad, smem4b);
+      if (threadIdx.x == 0) out[0] = (quad.x + quad.y) + (quad.z + quad.w);
+      __syncthreads();
+      return;
+    }
+  }
+  lz_partials<T>(n, bs, [&](int64_t r, int64_t b) { return a[r * bs + b] * c[r * bs + b]; }, out, smem);
+}
+
 // Sum over the nb per-CTA partials of column b, formed by the whole block (all threads get it).
 template <class T>
 __device__ __forceinline__ T lz_block_total(const T* part, int nb, int64_t bs, int64_t b, T* red) {
@@ -83,8 +171,26 @@ __device__ __forceinline__ T lz_block_total(const T* part, int nb, int64_t bs, i
 // (serial sum only beyond kLzStage columns).
 constexpr int kLzStage = 64;
 template <class T>
-__device__ __forceinline__ void lz_stage(const T* part, int nb, int64_t bs, T* tot, T* red) {
+__device__ __forceinline__ void lz_stage(const T* part, int nb, int64_t bs, T* tot, T* red, T* scratch) {
   const int64_t kk = bs < kLzStage ? bs : kLzStage;
+  if (kk >= 8 && blockDim.x % kk == 0) {
+    // all columns at once: thread (b, g) sums partials g, g + G, ... of column b (consecutive threads,
+    // consecutive columns), then the G group sums of each column are added in order
+    const int G = (int)(blockDim.x / kk);
+    const int b = (int)(threadIdx.x % kk), g = (int)(threadIdx.x / kk);
+    T acc = T(0);
+#pragma unroll 4
+    for (int q = g; q < nb; q += G) acc += __ldcg(part + (int64_t)q * bs + b);
+    scratch[threadIdx.x] = acc;
+    __syncthreads();
+    if (threadIdx.x < kk) {
+      T sum = T(0);
+      for (int gg = 0; gg < G; ++gg) sum += scratch[gg * kk + threadIdx.x];
+      tot[threadIdx.x] = sum;
+    }
+    __syncthreads();
+    return;
+  }
   for (int64_t b = 0; b < kk; ++b) {
     const T v = lz_block_total(part, nb, bs, b, red);
     if (threadIdx.x == 0) tot[b] = v;
@@ -109,11 +215,10 @@ template <class T>
 __global__ void __launch_bounds__(256) k_lz_norm(const T* v, int64_t n, int64_t bs, LzState<T> s) {
   if (*s.done) return;
   __shared__ T smem[256];
-  lz_partials<T>(n, bs, [&](int64_t r, int64_t b) { const T x = v[r * bs + b]; return x * x; },
-                 s.npart + (int64_t)blockIdx.x * bs, smem);
+  lz_colsum<T>(n, bs, v, v, s.npart + (int64_t)blockIdx.x * bs, smem);
   if (lz_last_block(s.counters + 0)) {
     __shared__ T tot[kLzStage], red[32];
-    lz_stage(s.npart, gridDim.x, bs, tot, red);
+    lz_stage(s.npart, gridDim.x, bs, tot, red, smem);
     for (int64_t b = threadIdx.x; b < bs; b += blockDim.x) s.nrm[b] = sqrt(lz_total(s.npart, gridDim.x, bs, b, tot));
     if (threadIdx.x == 0) s.counters[0] = 0;
   }
@@ -132,11 +237,10 @@ __global__ void __launch_bounds__(256) k_lz_alpha(const T* w, const T* vi, int64
                                                   int max_iters, LzState<T> s) {
   if (*s.done) return;
   __shared__ T smem[256];
-  lz_partials<T>(n, bs, [&](int64_t r, int64_t b) { return w[r * bs + b] * vi[r * bs + b]; },
-                 s.npart + (int64_t)blockIdx.x * bs, smem);
+  lz_colsum<T>(n, bs, w, vi, s.npart + (int64_t)blockIdx.x * bs, smem);
   if (lz_last_block(s.counters + 1)) {
     __shared__ T tot[kLzStage], red[32];
-    lz_stage(s.npart, gridDim.x, bs, tot, red);
+    lz_stage(s.npart, gridDim.x, bs, tot, red, smem);
     const int i = *s.step;
     for (int64_t b = threadIdx.x; b < bs; b += blockDim.x)
       diag[b * max_iters + (i - 1)] = lz_total(s.npart, gridDim.x, bs, b, tot);
@@ -253,7 +357,7 @@ __global__ void __launch_bounds__(256) k_lz_project1(const float* __restrict__ b
 // slots j = 1 + q, 1 + q + nwarps, ...; a warp step covers 128 consecutive floats, so lane l always
 // holds column quad l % (bs / 4) and accumulates it in a float4; a shuffle tree over the lanes of
 // the same quad finishes the slot.  128-bit streams, no block-wide barrier per slot.
-__global__ void __launch_bounds__(256) k_lz_projectq(const float* __restrict__ basis, const float* __restrict__ w,
+__global__ void __launch_bounds__(512) k_lz_projectq(const float* __restrict__ basis, const float* __restrict__ w,
                                                      int64_t n, int64_t bs, int64_t chunk, int64_t slots,
                                                      LzState<float> s) {
   if (*s.done) return;
@@ -381,12 +485,11 @@ __global__ void __launch_bounds__(256) k_lz_finish(const T* w, int64_t n, int64_
                                                    double tol, LzState<T> s) {
   if (*s.done) return;
   __shared__ T smem[256];
-  lz_partials<T>(n, bs, [&](int64_t r, int64_t b) { const T x = w[r * bs + b]; return x * x; },
-                 s.npart + (int64_t)blockIdx.x * bs, smem);
+  lz_colsum<T>(n, bs, w, w, s.npart + (int64_t)blockIdx.x * bs, smem);
   if (lz_last_block(s.counters + 2)) {
     __shared__ int s_any;
     __shared__ T tot[kLzStage], red[32];
-    lz_stage(s.npart, gridDim.x, bs, tot, red);
+    lz_stage(s.npart, gridDim.x, bs, tot, red, smem);
     const int i = *s.step;
     if (threadIdx.x == 0) s_any = 0;
     __syncthreads();
@@ -782,7 +885,7 @@ static int lanczos_t(const colagb_op* A, const T* V0, int64_t ldv0, int64_t bs, 
           if (p1)
             k_lz_project1<<<nb1, 256, chunk * sizeof(float), st>>>(basis, w, n, chunk, slots, s);
           else if (pq)
-            k_lz_projectq<<<nb1, 256, chunk * bs * sizeof(float), st>>>(basis, w, n, bs, chunk, slots, s);
+            k_lz_projectq<<<nb1, 512, chunk * bs * sizeof(float), st>>>(basis, w, n, bs, chunk, slots, s);
           else
             k_lz_project<T><<<nb, 256, 0, st>>>(basis, w, n, bs, slots, s);
         } else {
