@@ -242,6 +242,27 @@ def test_bench_byte_model_and_launch_count():
     assert bench.launches_per_solve("onchip", "learned", 256) == 4 * 2 + (1 + 2 * 2)
     assert bench.launches_per_solve("onchip", "plain", 256) == 1 + 2
     assert bench.launches_per_solve("cluster8", "jacobi", 2048) == 2
+    assert bench.launches_per_solve("onchip", "learned", 256, "auto") == 4 * 2 + (1 + 2 * 2) + 1
+    comp = bench.companion_roofline(40, 1000.0, n, 5, 7, 0.5, 6754.8)
+    assert comp["bytes_per_row_step"] == 5 * 4 + 7 * 2 + 48
+    assert comp["dram_bytes_est"] == 40 * 1000.0 * 82 * n
+    assert bench.companion_roofline(None, 1000.0, n, 5, 7, 0.5, 6754.8) is None
+
+
+def test_reference_lanczos_step_timer_runs_the_reference_body():
+    """The per-configuration CPU timing drives the reference's own Lanczos body for a few steps with
+    the basis of a full run, and puts its loop driver back afterwards."""
+    import sys
+    sys.path.insert(0, str(ROOT))
+    import bench
+    cola_ref = bench.reference_package()
+    if cola_ref is None:
+        pytest.skip("the reference package is not installed in baseline/_ref")
+    A = torch.randn(64, 64, dtype=torch.float64, generator=torch.Generator().manual_seed(0))
+    op = cola_ref.PSD(cola_ref.ops.Dense(A @ A.T + 64 * torch.eye(64, dtype=torch.float64)))
+    before = op.xnp.while_loop_winfo
+    t = bench._reference_lanczos_step_seconds(cola_ref, op, torch.randn(64, 2, dtype=torch.float64), 20, k_steps=2)
+    assert t > 0 and op.xnp.while_loop_winfo is before
 
 
 def test_c_program_links_and_calls_the_abi(tmp_path):
