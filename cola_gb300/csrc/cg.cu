@@ -537,6 +537,123 @@ __device__ __forceinline__ bool phase_sync(const GridBarrier& gb) {
   }
 }
 
+// Cluster-wide sums of NQ values for the one-cluster fused kernel with a single right-hand side:
+// warp shuffles, one block barrier, then lane r of warp 0 stores the CTA's sums into CTA r's shared
+// memory (slot [q][rank]); after the cluster barrier (release / acquire) every CTA adds the 16 slots
+// in rank order, so all CTAs hold the same totals and nothing is loaded from global memory or a peer
+// on the critical path.  Two slot buffers alternate: a CTA can be at most one reduction ahead of
+// another, because each reduction ends in a cluster barrier.
+constexpr int kK1MaxCtas = 16;
+template <int NQ, class T>
+__device__ __forceinline__ void k1_cluster_sum(T (&v)[NQ], T* wsum, T* slots, int& buf) {
+  namespace cgx = cooperative_groups;
+  cgx::cluster_group cl = cgx::this_cluster();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int ncta = (int)cl.num_blocks(), rank = (int)cl.block_rank();
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) v[q] = warp_sum(v[q]);
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) wsum[q * 32 + warp] = v[q];
+  __syncthreads();
+  T* sl = slots + buf * NQ * kK1MaxCtas;
+  if (warp == 0) {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      T x = lane < nw ? wsum[q * 32 + lane] : T(0);
+      v[q] = warp_sum(x);
+    }
+    if (lane < ncta)
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) *cl.map_shared_rank(sl + q * kK1MaxCtas + rank, lane) = v[q];
+  }
+  cl.sync();
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    T tot = T(0);
+    for (int r = 0; r < ncta; ++r) tot += sl[q * kK1MaxCtas + r];
+    v[q] = tot;
+  }
+  buf ^= 1;
+}
+
+// The fused CG for one right-hand side on one thread-block cluster (<= 16 CTAs): the same algorithm,
+// stop rule and history as the general body of k_cg_fused below (cg.py:94-178), with every inner
+// product reduced by k1_cluster_sum -- two of them per step, <p, Ap> and (<r, z>, |r|^2) -- instead of
+// per-CTA partials in global memory read back after the barrier.
+template <class T, class S, int PK>
+__device__ __forceinline__ void cg_fused_k1(const FusedArgs<T, S>& a, int64_t r0, int64_t r1) {
+  __shared__ T wsum[2 * 32];
+  __shared__ T slots[2 * 2 * kK1MaxCtas];
+  int buf = 0;
+  namespace cgx = cooperative_groups;
+  cgx::cluster_group cl = cgx::this_cluster();
+  const int t = threadIdx.x;
+  auto z_of = [&](int64_t i, T r) { return PK == 0 ? r : a.dinv[i] * r; };
+  // mult = |b|
+  T q1[1] = {T(0)};
+  for (int64_t i = r0 + t; i < r1; i += blockDim.x) {
+    const T v = a.B[i * a.ldb];
+    q1[0] += v * v;
+  }
+  k1_cluster_sum<1, T>(q1, wsum, slots, buf);
+  const T mult = sqrt(q1[0]);
+  // r = b / mult - A x0 (x0 through P)
+  for (int64_t i = r0 + t; i < r1; i += blockDim.x) a.P[i] = a.X[i * a.ldx];
+  cl.sync();
+  own_matvec(a, a.P, a.AP, r0, r1);
+  for (int64_t i = r0 + t; i < r1; i += blockDim.x) a.R[i] = safe_div(a.B[i * a.ldb], mult) - a.AP[i];
+  cl.sync();  // every CTA is done reading x0 out of P
+  T q2[2] = {T(0), T(0)};
+  for (int64_t i = r0 + t; i < r1; i += blockDim.x) {
+    const T r = a.R[i];
+    const T z = z_of(i, r);
+    a.P[i] = z;
+    q2[0] += r * z;
+    q2[1] += r * r;
+  }
+  k1_cluster_sum<2, T>(q2, wsum, slots, buf);  // also publishes P
+  T gamma = q2[0];
+  T rn = sqrt(q2[1]);
+  const T tol_eff = (T)a.tol * rn + (T)a.tol;
+  bool conv = rn < SmallValue<T>::v;
+  if (blockIdx.x == 0 && t == 0 && a.hist) a.hist[0] = rn;
+  int it = 0;
+  bool running = rn > tol_eff && it < a.max_iters;
+  while (running) {
+    // A: Ap = A p, <p, Ap>
+    own_matvec(a, a.P, a.AP, r0, r1);
+    T qa[1] = {T(0)};
+    for (int64_t i = r0 + t; i < r1; i += blockDim.x) qa[0] += a.P[i] * a.AP[i];
+    k1_cluster_sum<1, T>(qa, wsum, slots, buf);
+    const T alpha = conv ? T(0) : safe_div(gamma, qa[0]);
+    // B: x, r updates, <r, z>, |r|^2
+    T qb[2] = {T(0), T(0)};
+    for (int64_t i = r0 + t; i < r1; i += blockDim.x) {
+      const T p = a.P[i];
+      a.X[i * a.ldx] += alpha * p;
+      const T r = a.R[i] - alpha * a.AP[i];
+      a.R[i] = r;
+      qb[0] += r * z_of(i, r);
+      qb[1] += r * r;
+    }
+    k1_cluster_sum<2, T>(qb, wsum, slots, buf);
+    const T beta = conv ? T(0) : safe_div(qb[0], gamma);
+    gamma = qb[0];
+    rn = sqrt(qb[1]);
+    conv = rn < SmallValue<T>::v;
+    ++it;
+    if (blockIdx.x == 0 && t == 0 && a.hist) a.hist[it] = rn;
+    running = rn > tol_eff && it < a.max_iters;
+    if (!running) break;
+    // C: p = z + beta p
+    for (int64_t i = r0 + t; i < r1; i += blockDim.x) a.P[i] = z_of(i, a.R[i]) + beta * a.P[i];
+    cl.sync();
+  }
+  for (int64_t i = r0 + t; i < r1; i += blockDim.x) a.X[i * a.ldx] *= mult;
+  if (blockIdx.x == 0 && t == 0) *a.s.iters = it;
+}
+
 template <class T, class S, int PK, bool CLUSTER>
 __global__ void __launch_bounds__(CLUSTER ? 512 : 256) k_cg_fused(FusedArgs<T, S> a) {
   extern __shared__ unsigned char smem_raw[];
@@ -557,6 +674,12 @@ __global__ void __launch_bounds__(CLUSTER ? 512 : 256) k_cg_fused(FusedArgs<T, S
   const int64_t r0 = (int64_t)blockIdx.x * rows_per_block;
   const int64_t r1 = (r0 + rows_per_block < n) ? r0 + rows_per_block : n;
   const int64_t kc = k < 256 ? k : 256;
+  if constexpr (CLUSTER) {
+    if (k == 1 && gridDim.x <= kK1MaxCtas) {
+      cg_fused_k1<T, S, PK>(a, r0, r1);
+      return;
+    }
+  }
   T* pA = a.s.pA + (int64_t)blockIdx.x * k;
   T* pB = a.s.pB + (int64_t)blockIdx.x * k;
   T* pC = a.s.pC + (int64_t)blockIdx.x * k;
