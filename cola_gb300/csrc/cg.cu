@@ -447,7 +447,23 @@ __device__ __forceinline__ void own_matvec(const FusedArgs<T, S>& a, const T* V,
       const int64_t i = r0 + u / k, c = u % k;
       T acc = a.shift * V[i * k + c];
       const int32_t b = a.indptr[i], e = a.indptr[i + 1];
-      for (int32_t j = b; j < e; ++j) acc += cvt<T>(a.vals[j]) * V[(int64_t)a.indices[j] * k + c];
+      // entries in groups of four: indices and values, then the gathers, in flight together
+      for (int32_t j0 = b; j0 < e; j0 += 4) {
+        int32_t col[4];
+        T v[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          const bool ok = j0 + t < e;
+          col[t] = ok ? a.indices[j0 + t] : 0;
+          v[t] = ok ? cvt<T>(a.vals[j0 + t]) : T(0);
+        }
+        T x[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) x[t] = j0 + t < e ? V[(int64_t)col[t] * k + c] : T(0);
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+          if (j0 + t < e) acc += v[t] * x[t];
+      }
       OUT[i * k + c] = acc;
     }
   } else {

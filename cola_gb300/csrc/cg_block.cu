@@ -264,10 +264,27 @@ __global__ void __launch_bounds__(kBT, 4) k_block_ir(const BlockArgs a) {
       const int64_t i = r0 + u / q;
       const int32_t b = __ldg(a.indptr + i), e = __ldg(a.indptr + i + 1);
       float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-      for (int32_t j = b; j < e; ++j) {
-        const float v = __ldg(a.vals + j);
-        const float4 x = P4[(int64_t)__ldg(a.indices + j) * q + cq];
-        acc.x += v * x.x; acc.y += v * x.y; acc.z += v * x.z; acc.w += v * x.w;
+      // entries in groups of four: the group's indices and values, then its four p-row gathers, are
+      // in flight together (one dependent index -> gather round trip per entry made this phase
+      // latency-bound); the products are added in entry order as before
+      for (int32_t j0 = b; j0 < e; j0 += 4) {
+        int32_t col[4];
+        float v[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          const bool ok = j0 + t < e;
+          col[t] = ok ? __ldg(a.indices + j0 + t) : 0;
+          v[t] = ok ? __ldg(a.vals + j0 + t) : 0.f;
+        }
+        float4 x[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) x[t] = j0 + t < e ? P4[(int64_t)col[t] * q + cq] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          if (j0 + t < e) {
+            acc.x += v[t] * x[t].x; acc.y += v[t] * x[t].y; acc.z += v[t] * x[t].z; acc.w += v[t] * x[t].w;
+          }
+        }
       }
       AP4[i * q + cq] = acc;
       const float4 p = P4[i * q + cq];

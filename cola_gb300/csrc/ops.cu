@@ -310,7 +310,24 @@ __global__ void __launch_bounds__(256) csr_spmm_kernel(const int32_t* __restrict
   const int32_t beg = indptr[row], end = indptr[row + 1];
   T acc = T(0);
   if (c < k)
-    for (int32_t j = beg; j < end; ++j) acc += cvt<T>(vals[j]) * X[(int64_t)indices[j] * ldx + c];
+    // entries in groups of four: indices and values, then the four gathers, in flight together;
+    // products added in entry order
+    for (int32_t j0 = beg; j0 < end; j0 += 4) {
+      int32_t col[4];
+      T v[4];
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const bool ok = j0 + t < end;
+        col[t] = ok ? indices[j0 + t] : 0;
+        v[t] = ok ? cvt<T>(vals[j0 + t]) : T(0);
+      }
+      T x[4];
+#pragma unroll
+      for (int t = 0; t < 4; ++t) x[t] = j0 + t < end ? X[(int64_t)col[t] * ldx + c] : T(0);
+#pragma unroll
+      for (int t = 0; t < 4; ++t)
+        if (j0 + t < end) acc += v[t] * x[t];
+    }
   if (c < k) Y[row * ldy + c] = combine(acc, alpha, beta, Y + row * ldy + c);
 }
 
