@@ -175,13 +175,15 @@ __global__ void __launch_bounds__(kBT, 4) k_block_ir(const BlockArgs a) {
     a.Bn[e] = bnorm[c] > 0.0 ? a.Bn[e] / bnorm[c] : 0.0;
   }
 
-  // FP64 residual replacement of every running column: X64 += D, D = 0, R = Bn - A X64 (FP64),
-  // then |r64|^2 and <r, z>; afterwards relres, gamma and rmax are set and converged columns frozen.
+  // FP64 residual replacement of every running column: X64 += D + alpha P (the step's correction,
+  // which phase C would otherwise add to D), D = 0, R = Bn - A X64 (FP64), then |r64|^2 and <r, z>;
+  // afterwards relres, gamma and rmax are set and converged columns frozen.
   auto replace = [&](bool first) -> bool {
     if (!first) {
       for (int64_t u = threadIdx.x; u < (r1 - r0) * kp; u += kBT) {
         const int64_t e = r0 * kp + u;
-        a.X64[e] += (double)a.D[e];
+        const int c = (int)(u % kp);
+        a.X64[e] += (double)(a.D[e] + alpha[c] * a.P[e]);
         a.D[e] = 0.f;
       }
       if (!grid_sync(a.gb)) return false;
@@ -304,17 +306,15 @@ __global__ void __launch_bounds__(kBT, 4) k_block_ir(const BlockArgs a) {
       }
     }
     __syncthreads();
-    // ---- B: d += alpha p, r -= alpha Ap, |r|^2, <r, z> ----
+    // ---- B: r -= alpha Ap, |r|^2, <r, z> (d += alpha p waits for phase C, which reads p anyway) ----
     float4 prr = make_float4(0.f, 0.f, 0.f, 0.f), prz = make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 al = make_float4(alpha[4 * cq], alpha[4 * cq + 1], alpha[4 * cq + 2], alpha[4 * cq + 3]);
     for (int64_t u = threadIdx.x; u < nu; u += kBT) {
       const int64_t i = r0 + u / q;
       const int64_t e = i * q + cq;
-      const float4 p = P4[e], ap = AP4[e];
-      float4 d = D4[e], r = R4[e];
-      d.x += al.x * p.x; d.y += al.y * p.y; d.z += al.z * p.z; d.w += al.w * p.w;
+      const float4 ap = AP4[e];
+      float4 r = R4[e];
       r.x -= al.x * ap.x; r.y -= al.y * ap.y; r.z -= al.z * ap.z; r.w -= al.w * ap.w;
-      D4[e] = d;
       R4[e] = r;
       const float di = a.jacobi ? a.dinv[i] : 1.f;
       prr.x += r.x * r.x; prr.y += r.y * r.y; prr.z += r.z * r.z; prr.w += r.w * r.w;
@@ -344,6 +344,7 @@ __global__ void __launch_bounds__(kBT, 4) k_block_ir(const BlockArgs a) {
       s_flag = trig;
     }
     __syncthreads();
+    const bool dpend = !s_flag;  // a replacement has already added this step's alpha p to x
     if (s_flag) {
       if (!replace(false)) return;
       ++nrep;
@@ -360,6 +361,11 @@ __global__ void __launch_bounds__(kBT, 4) k_block_ir(const BlockArgs a) {
       const int64_t i = r0 + u / q;
       const int64_t e = i * q + cq;
       const float4 r = R4[e], p = P4[e];
+      if (dpend) {
+        float4 d = D4[e];
+        d.x += al.x * p.x; d.y += al.y * p.y; d.z += al.z * p.z; d.w += al.w * p.w;
+        D4[e] = d;
+      }
       const float di = a.jacobi ? a.dinv[i] : 1.f;
       Pw4[e] = make_float4(di * r.x + be.x * p.x, di * r.y + be.y * p.y, di * r.z + be.z * p.z,
                            di * r.w + be.w * p.w);
