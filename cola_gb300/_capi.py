@@ -46,7 +46,7 @@ class OpNode(C.Structure):
         ("data", C.c_void_p), ("ld", C.c_int64), ("indptr", C.c_void_p), ("indices", C.c_void_p),
         ("nnz", C.c_int64), ("scalar", C.c_double), ("children", C.POINTER(C.c_int32)),
         ("num_children", C.c_int32), ("multiplicities", C.POINTER(C.c_int64)),
-        ("precision", C.c_int32), ("reserved", C.c_int32),
+        ("precision", C.c_int32), ("reserved", C.c_int32), ("perm", C.c_void_p),
     ]
 
 

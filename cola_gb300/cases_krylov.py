@@ -30,6 +30,7 @@ def main(argv=None):
     ap.add_argument("--precision", default="auto", choices=["auto", "fp32", "bf16", "bf16x3"])
     ap.add_argument("--probes", type=int, default=64)
     ap.add_argument("--steps", type=int, default=0, help="Lanczos / SLQ steps (0: the configuration's)")
+    ap.add_argument("--reorder", action="store_true", help="c5: store L in reverse Cuthill-McKee order")
     args = ap.parse_args(argv)
 
     import cola_gb300 as cola
@@ -44,6 +45,8 @@ def main(argv=None):
         n = m * m
         ip, ix, v = W.rgg_laplacian(n, 0.002 / args.scale, seed=7, device="cpu")
         L = cola.ops.Sparse.from_csr(ip.to(dev), ix.to(dev), v.to(dev), (n, n))
+        if args.reorder:
+            L = L.reordered()
         op = cola.SelfAdjoint(cola.ops.Kronecker(cola.ops.Dense(A1.to(dev)), cola.ops.Dense(A2.to(dev)),
                                                  precision=args.precision) + L)
         start = randn(n, dtype=torch.float32, key=PRNGKey(42)).to(dev)

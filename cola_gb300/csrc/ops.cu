@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(256) csr_spmv_kernel(const int32_t* __restrict
                                                        const S* __restrict__ vals, int64_t rows,
                                                        const T* __restrict__ X, int64_t ldx, int64_t bsx,
                                                        T* __restrict__ Y, int64_t ldy, int64_t bsy, T alpha,
-                                                       T beta, const int* skip) {
+                                                       T beta, const int32_t* __restrict__ operm, const int* skip) {
   if (skip && *skip) return;
   const int64_t b = blockIdx.y;
   X += b * bsx;
@@ -174,7 +174,10 @@ __global__ void __launch_bounds__(256) csr_spmv_kernel(const int32_t* __restrict
   }
 #pragma unroll
   for (int o = TPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  if (row < rows && sub == 0) Y[row * ldy] = combine(acc, alpha, beta, Y + row * ldy);
+  if (row < rows && sub == 0) {
+    const int64_t orow = operm ? (int64_t)operm[row] : row;  // a permuted node writes row perm[row]
+    Y[orow * ldy] = combine(acc, alpha, beta, Y + orow * ldy);
+  }
 }
 
 // CSR, one column, short rows ("CSR-stream"): one warp per group of 32 consecutive rows.  The group's
@@ -245,7 +248,7 @@ template <class T, class S, bool VEC>
 __global__ void __launch_bounds__(kStreamWarps * 32) csr_stream_kernel(
     const int32_t* __restrict__ indptr, const int32_t* __restrict__ indices, const S* __restrict__ vals,
     int64_t rows, int64_t nnz, const T* __restrict__ X, int64_t ldx, int64_t bsx, T* __restrict__ Y, int64_t ldy,
-    int64_t bsy, T alpha, T beta, const int* skip) {
+    int64_t bsy, T alpha, T beta, const int32_t* __restrict__ operm, const int* skip) {
   constexpr int CAP = StreamCap<T>::value;
   __shared__ T prod[kStreamWarps][CAP];
   if (skip && *skip) return;
@@ -287,7 +290,10 @@ __global__ void __launch_bounds__(kStreamWarps * 32) csr_stream_kernel(
       if (lane == rr) acc = sum;
     }
   }
-  if (lane < nr) Y[(r0 + lane) * ldy] = combine(acc, alpha, beta, Y + (r0 + lane) * ldy);
+  if (lane < nr) {
+    const int64_t orow = operm ? (int64_t)operm[r0 + lane] : r0 + lane;
+    Y[orow * ldy] = combine(acc, alpha, beta, Y + orow * ldy);
+  }
 }
 
 // CSR, k columns: one warp per row, lanes over 32-column chunks; each entry reads a contiguous
@@ -298,7 +304,8 @@ __global__ void __launch_bounds__(256) csr_spmm_kernel(const int32_t* __restrict
                                                        const S* __restrict__ vals, int64_t rows,
                                                        const T* __restrict__ X, int64_t ldx, int64_t bsx,
                                                        T* __restrict__ Y, int64_t ldy, int64_t bsy, int64_t k,
-                                                       T alpha, T beta, const int* skip) {
+                                                       T alpha, T beta, const int32_t* __restrict__ operm,
+                                                       const int* skip) {
   if (skip && *skip) return;
   const int64_t b = blockIdx.z;
   X += b * bsx;
@@ -328,7 +335,8 @@ __global__ void __launch_bounds__(256) csr_spmm_kernel(const int32_t* __restrict
       for (int t = 0; t < 4; ++t)
         if (j0 + t < end) acc += v[t] * x[t];
     }
-  if (c < k) Y[row * ldy + c] = combine(acc, alpha, beta, Y + row * ldy + c);
+  const int64_t orow = operm ? (int64_t)operm[row] : row;
+  if (c < k) Y[orow * ldy + c] = combine(acc, alpha, beta, Y + orow * ldy + c);
 }
 
 // Diagonal: Y = alpha * d * X + beta * Y
@@ -363,6 +371,21 @@ __global__ void axpby_kernel(const T* __restrict__ X, int64_t ldx, int64_t bsx, 
   }
 }
 
+// xp[b][i][c] = X[b][perm[i]][c]: the input of a permuted Sparse node in its stored order.
+template <class T>
+__global__ void k_perm_gather(const int32_t* __restrict__ perm, int64_t n, const T* __restrict__ X, int64_t ldx,
+                              int64_t bsx, T* __restrict__ xp, int64_t k, const int* skip) {
+  if (skip && *skip) return;
+  const int64_t b = blockIdx.y;
+  X += b * bsx;
+  xp += b * n * k;
+  const int64_t total = n * k;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < total; u += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = u / k, c = u - i * k;
+    xp[u] = X[(int64_t)perm[i] * ldx + c];
+  }
+}
+
 // --------------------------------------------------------------------------------------------
 // launch helpers
 
@@ -391,6 +414,16 @@ template int launch_axpby<float>(const float*, int64_t, float*, int64_t, int64_t
                                  const int*, cudaStream_t);
 template int launch_axpby<double>(const double*, int64_t, double*, int64_t, int64_t, int64_t, double, double,
                                   const int*, cudaStream_t);
+
+template <class T>
+int launch_perm_gather(const int32_t* perm, int64_t n, const T* X, int64_t ldx, int64_t bsx, T* xp, int64_t k,
+                       int64_t batch, const int* skip, cudaStream_t st) {
+  if (n * k == 0) return COLAGB_OK;
+  dim3 grid(elementwise_grid(n * k), (unsigned)batch);
+  k_perm_gather<T><<<grid, 256, 0, st>>>(perm, n, X, ldx, bsx, xp, k, skip);
+  COLAGB_CUDA(cudaGetLastError());
+  return COLAGB_OK;
+}
 
 template <class T, class S>
 static int launch_dense(const colagb_op_node& nd, const T* X, int64_t ldx, int64_t bsx, T* Y, int64_t ldy,
@@ -427,10 +460,12 @@ static int launch_csr(const colagb_op_node& nd, const T* X, int64_t ldx, int64_t
     dim3 grid((unsigned)ceil_div(nd.rows, (int64_t)kStreamWarps * 32), (unsigned)batch);
     if (vec)
       csr_stream_kernel<T, S, true><<<grid, kStreamWarps * 32, 0, st>>>(nd.indptr, nd.indices, v, nd.rows, nd.nnz, X,
-                                                                         ldx, bsx, Y, ldy, bsy, alpha, beta, skip);
+                                                                         ldx, bsx, Y, ldy, bsy, alpha, beta, nd.perm,
+                                                                         skip);
     else
       csr_stream_kernel<T, S, false><<<grid, kStreamWarps * 32, 0, st>>>(nd.indptr, nd.indices, v, nd.rows, nd.nnz,
-                                                                          X, ldx, bsx, Y, ldy, bsy, alpha, beta, skip);
+                                                                          X, ldx, bsx, Y, ldy, bsy, alpha, beta, nd.perm,
+                                                                          skip);
   } else if (k == 1) {
     int tpr = 1;
     while (tpr < 32 && tpr * 2 <= avg) tpr *= 2;
@@ -438,7 +473,7 @@ static int launch_csr(const colagb_op_node& nd, const T* X, int64_t ldx, int64_t
 #define COLAGB_CSR_CASE(N)                                                                                  \
   case N:                                                                                                   \
     csr_spmv_kernel<T, S, N><<<grid, 256, 0, st>>>(nd.indptr, nd.indices, v, nd.rows, X, ldx, bsx, Y, ldy, \
-                                                   bsy, alpha, beta, skip);                                 \
+                                                   bsy, alpha, beta, nd.perm, skip);                        \
     break;
     switch (tpr) {
       COLAGB_CSR_CASE(1)
@@ -452,7 +487,7 @@ static int launch_csr(const colagb_op_node& nd, const T* X, int64_t ldx, int64_t
   } else {
     dim3 grid((unsigned)ceil_div(nd.rows, 8), (unsigned)ceil_div(k, 32), (unsigned)batch);
     csr_spmm_kernel<T, S><<<grid, 256, 0, st>>>(nd.indptr, nd.indices, v, nd.rows, X, ldx, bsx, Y, ldy, bsy, k,
-                                                alpha, beta, skip);
+                                                alpha, beta, nd.perm, skip);
   }
   COLAGB_CUDA(cudaGetLastError());
   return COLAGB_OK;
@@ -520,8 +555,21 @@ int op_apply(const colagb_op* op, int node, const T* X, int64_t ldx, int64_t bsx
   const std::vector<int32_t>& ch = op->children[node];
   const bool measuring = ws.measure;
   switch (nd.kind) {
-    case COLAGB_OP_DENSE:
     case COLAGB_OP_CSR:
+      if (nd.perm) {  // stored P A P^T: gather x through perm, the product writes y through it
+        const size_t mark = ws.used;
+        T* xp = ws.take<T>((size_t)nd.cols * k * batch);
+        if (!measuring) {
+          COLAGB_TRY(launch_perm_gather<T>(nd.perm, nd.cols, X, ldx, bsx, xp, k, batch, skip, st));
+          COLAGB_TRY(LeafLaunch<T>::run(nd.kind, nd.dtype, nd, xp, k, nd.cols * k, Y, ldy, bsy, k, batch, alpha, beta,
+                                        skip, st));
+        }
+        ws.release(mark);
+        return COLAGB_OK;
+      }
+      if (measuring) return COLAGB_OK;
+      return LeafLaunch<T>::run(nd.kind, nd.dtype, nd, X, ldx, bsx, Y, ldy, bsy, k, batch, alpha, beta, skip, st);
+    case COLAGB_OP_DENSE:
     case COLAGB_OP_DIAG:
       if (measuring) return COLAGB_OK;
       return LeafLaunch<T>::run(nd.kind, nd.dtype, nd, X, ldx, bsx, Y, ldy, bsy, k, batch, alpha, beta, skip, st);
@@ -689,7 +737,7 @@ FusedForm fused_form(const colagb_op* op) {
   FusedForm f;
   const colagb_op_node& r = op->nodes[op->root];
   auto is_leaf = [](const colagb_op_node& n) {
-    return (n.kind == COLAGB_OP_CSR || n.kind == COLAGB_OP_DENSE) && n.rows == n.cols;
+    return (n.kind == COLAGB_OP_CSR || n.kind == COLAGB_OP_DENSE) && n.rows == n.cols && n.perm == nullptr;
   };
   if (is_leaf(r)) {
     f.ok = true;
@@ -731,6 +779,7 @@ static int validate_node(const colagb_op_node& n, int idx, int num_nodes) {
     return fail(COLAGB_ERR_INVALID, "operator node " + std::to_string(idx) + ": " + what);
   };
   if (n.rows < 0 || n.cols < 0) return bad("negative shape");
+  if (n.perm && n.kind != COLAGB_OP_CSR) return bad("a permutation on a node that is not Sparse");
   switch (n.kind) {
     case COLAGB_OP_DENSE:
       if (!n.data && n.rows * n.cols > 0) return bad("Dense without data");
@@ -739,6 +788,7 @@ static int validate_node(const colagb_op_node& n, int idx, int num_nodes) {
     case COLAGB_OP_CSR:
       if ((!n.indptr || !n.indices || !n.data) && n.nnz > 0) return bad("Sparse without indptr/indices/values");
       if (!n.indptr && n.rows > 0) return bad("Sparse without indptr");
+      if (n.perm && n.rows != n.cols) return bad("a permuted Sparse must be square");
       break;
     case COLAGB_OP_DIAG:
       if (n.rows != n.cols) return bad("Diagonal must be square");

@@ -59,6 +59,7 @@ static int vjp_supported(const colagb_op* op, int node) {
     case COLAGB_OP_CSR:
     case COLAGB_OP_DIAG:
       if (nd.dtype == COLAGB_BF16) return fail(COLAGB_ERR_UNSUPPORTED, "matmat VJP: BF16 leaves have no gradient here");
+      if (nd.perm) return fail(COLAGB_ERR_UNSUPPORTED, "matmat VJP: permuted Sparse leaves are not handled");
       return COLAGB_OK;
     case COLAGB_OP_SCALAR:
     case COLAGB_OP_IDENTITY:

@@ -54,9 +54,13 @@ def torch_matmat(A: O.LinearOperator, X: torch.Tensor, sub: dict | None = None) 
     if isinstance(A, O.Dense):
         return t(A.A).to(X.dtype) @ X
     if isinstance(A, O.Sparse):
-        rows = torch.repeat_interleave(torch.arange(A.shape[0], device=X.device),
-                                       (A.indptr[1:] - A.indptr[:-1]).to(torch.int64))
-        contrib = t(A.values).to(X.dtype)[:, None] * X[A.indices.to(torch.int64)]
+        if A.perm is not None:  # stored in a permuted order: the triplets in original coordinates
+            rows, cols = A.row_indices.to(torch.int64), A.col_indices.to(torch.int64)
+        else:
+            rows = torch.repeat_interleave(torch.arange(A.shape[0], device=X.device),
+                                           (A.indptr[1:] - A.indptr[:-1]).to(torch.int64))
+            cols = A.indices.to(torch.int64)
+        contrib = t(A.values).to(X.dtype)[:, None] * X[cols]
         return torch.zeros((A.shape[0], X.shape[1]), dtype=X.dtype, device=X.device).index_add(0, rows, contrib)
     if isinstance(A, O.Diagonal):
         return t(A.diag).to(X.dtype)[:, None] * X

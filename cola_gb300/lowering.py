@@ -91,9 +91,13 @@ class Lowered:
             self._keep += [op.indptr, op.indices, op.values]
             self._dev(op.values)
             self.leaf_tensors[len(self.nodes)] = op.values
+            extra = {}
+            if op.perm is not None:
+                self._keep.append(op.perm)
+                extra["perm"] = op.perm.data_ptr()
             return self._add(kind=_capi.OP_CSR, dtype=self._leaf_dtype(op.values), rows=rows, cols=cols,
                              data=op.values.data_ptr(), indptr=op.indptr.data_ptr(), indices=op.indices.data_ptr(),
-                             nnz=op.nnz)
+                             nnz=op.nnz, **extra)
         if isinstance(op, O.Diagonal):
             d = op.diag.contiguous()
             self._keep.append(d)

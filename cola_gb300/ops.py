@@ -192,8 +192,58 @@ class Sparse(LinearOperator):
         obj.data = obj.values
         return obj
 
+    perm = None  # stored order of a reordered matrix (see reordered)
+
+    def reordered(self, method: str = "rcm") -> "Sparse":
+        """The same matrix stored in a bandwidth-reducing order: P A P^T with P from reverse
+        Cuthill-McKee on the pattern (symmetrised), computed once on the host with scipy, like the
+        reference's own host-side CSR construction (operators.py:64-76).  Products gather x through
+        the permutation and write y through it (colagb_op_node.perm), so the operator still means A;
+        what changes is locality: on a graph numbered in random order every x gather of the original
+        storage is a scattered memory sector, on the reordered one neighbouring rows read neighbouring
+        entries.  Square matrices only."""
+        if method != "rcm":
+            raise ValueError("method must be 'rcm'")
+        n, m = self.shape
+        if n != m:
+            raise ValueError("reordered() needs a square matrix")
+        if self.perm is not None:
+            return self
+        import numpy as np
+        import scipy.sparse as sp
+        from scipy.sparse.csgraph import reverse_cuthill_mckee
+        ip, ix = self.indptr.cpu().numpy(), self.indices.cpu().numpy()
+        pattern = sp.csr_matrix((np.ones(ix.size, dtype=np.int8), ix, ip), shape=(n, n))
+        perm = torch.as_tensor(reverse_cuthill_mckee(pattern, symmetric_mode=False).astype(np.int64),
+                               device=self.device)
+        inv = torch.empty_like(perm)
+        inv[perm] = torch.arange(n, device=self.device)
+        counts = (self.indptr[1:] - self.indptr[:-1]).to(torch.int64)
+        old_row = torch.repeat_interleave(torch.arange(n, device=self.device), counts)
+        new_row, new_col = inv[old_row], inv[self.indices.to(torch.int64)]
+        order = torch.argsort(new_row * n + new_col)
+        obj = Sparse.__new__(Sparse)
+        obj.device = self.device
+        LinearOperator.__init__(obj, dtype=self.dtype, shape=self.shape)
+        indptr = torch.zeros(n + 1, dtype=torch.int64, device=self.device)
+        indptr[1:] = torch.cumsum(torch.bincount(new_row, minlength=n), 0)
+        obj.indptr = indptr.to(torch.int32).contiguous()
+        obj.indices = new_col[order].to(torch.int32).contiguous()
+        obj.values = self.values[order].contiguous()
+        obj.nnz = self.nnz
+        obj.perm = perm.to(torch.int32).contiguous()
+        # the triplets in the original coordinates, in the stored order (transpose, to_dense)
+        obj.row_indices = perm[new_row[order]]
+        obj.col_indices = perm[new_col[order]]
+        obj.data = obj.values
+        return obj
+
     def to_dense(self):
         D = torch.zeros(self.shape, dtype=self.dtype, device=self.device)
+        if self.perm is not None:
+            D.index_put_((self.row_indices.to(torch.int64), self.col_indices.to(torch.int64)), self.values,
+                         accumulate=True)
+            return D
         rows = torch.repeat_interleave(torch.arange(self.shape[0], device=self.device),
                                        (self.indptr[1:] - self.indptr[:-1]).to(torch.int64))
         D.index_put_((rows, self.indices.to(torch.int64)), self.values, accumulate=True)

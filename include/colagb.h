@@ -84,6 +84,10 @@ typedef struct colagb_op_node {
   const int64_t* multiplicities; /* host, BLOCKDIAG: one per child, NULL = all 1 */
   int32_t precision;       /* KRON: arithmetic of the factor contractions, COLAGB_KRON_* below */
   int32_t reserved;
+  const int32_t* perm;     /* CSR (square), or NULL: the matrix is stored symmetrically permuted,
+                              stored row / column r being original row / column perm[r] (a
+                              bandwidth-reducing order); products gather x through perm and write
+                              y through it, so the node still means the original matrix */
 } colagb_op_node;
 
 /* Kronecker contraction arithmetic (FP32 compute type; FP64 operators always use FP64 arithmetic).

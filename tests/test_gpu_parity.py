@@ -102,6 +102,49 @@ def test_csr_spmv_irregular_rows(dtype, misalign):
     assert rel(y2, 2 * ref) < tol
 
 
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64, torch.bfloat16])
+@pytest.mark.parametrize("k", [1, 3])
+def test_reordered_sparse_products(dtype, k):
+    """A Sparse stored in reverse Cuthill-McKee order (gather x through the permutation, write y
+    through it) gives the original matrix's products, alone, in a Sum (accumulating into y) and batched
+    through a Kronecker factor's column blocks."""
+    from cola_gb300.workloads import rgg_laplacian
+    n = 4096
+    ip, ix, v = rgg_laplacian(n, 0.03, seed=11, device="cpu")
+    A = cola.ops.Sparse.from_csr(ip.to(DEV), ix.to(DEV), v.to(DEV, dtype), (n, n))
+    R = A.reordered()
+    cdt = torch.float64 if dtype == torch.float64 else torch.float32
+    X = torch.randn(n, k, device=DEV, dtype=cdt)
+    ref = A @ X
+    tol = 1e-12 if dtype == torch.float64 else 1e-6
+    assert rel(R @ X, ref) < tol
+    D = cola.ops.Diagonal(torch.linspace(1, 2, n, device=DEV, dtype=cdt))
+    assert rel((R + D) @ X, ref + D @ X) < tol
+
+
+def test_reordered_sparse_in_lanczos_and_cg():
+    """Lanczos on Kronecker + reordered graph Laplacian gives the original operator's Ritz values, and
+    CG on a reordered SPD matrix the original's solution (the fused single-operator path does not take
+    permuted leaves: the generic loop runs)."""
+    from cola_gb300.workloads import dense_spd, rgg_laplacian
+    m = 64
+    n = m * m
+    ip, ix, v = rgg_laplacian(n, 0.05, seed=12, device="cpu")
+    L = cola.ops.Sparse.from_csr(ip.to(DEV), ix.to(DEV), v.to(DEV, torch.float64), (n, n))
+    A1, _, _ = dense_spd(m, seed=1, lo=1e-1, hi=1e1, dtype=torch.float64)
+    K = cola.ops.Kronecker(cola.ops.Dense(A1.to(DEV)), cola.ops.Dense(A1.to(DEV)))
+    start = torch.randn(n, dtype=torch.float64, generator=torch.Generator().manual_seed(3)).to(DEV)
+    alg = Lanczos(start_vector=start, max_iters=60, tol=1e-12)
+    v0, _ = cola.eig(cola.SelfAdjoint(K + L), 5, "LM", alg)
+    v1, _ = cola.eig(cola.SelfAdjoint(K + L.reordered()), 5, "LM", alg)
+    assert rel(v1, v0) < 1e-9  # each row's entries are summed in the new column order
+    S = cola.PSD(L.reordered() + cola.ops.ScalarMul(1.0, (n, n), torch.float64, DEV))
+    b = torch.randn(n, dtype=torch.float64, device=DEV)
+    x, info = cola.linalg.cg(S, b, tol=1e-10, max_iters=5000)
+    Ad = L.to_dense() + torch.eye(n, device=DEV, dtype=torch.float64)
+    assert float((b - Ad @ x).norm() / b.norm()) < 1e-9
+
+
 def test_sparse_known_answer(golden):
     g = golden("ops_sparse_known")
     S = cola.ops.Sparse(T(g["data"]), T(g["rows"]), T(g["cols"]), (3, 4))
