@@ -138,7 +138,8 @@ def test_reordered_sparse_in_lanczos_and_cg():
     v0, _ = cola.eig(cola.SelfAdjoint(K + L), 5, "LM", alg)
     v1, _ = cola.eig(cola.SelfAdjoint(K + L.reordered()), 5, "LM", alg)
     assert rel(v1, v0) < 1e-9  # each row's entries are summed in the new column order
-    S = cola.PSD(L.reordered() + cola.ops.ScalarMul(1.0, (n, n), torch.float64, DEV))
+    Lr = L.reordered()
+    S = cola.PSD(Lr + cola.ops.I_like(Lr))
     b = torch.randn(n, dtype=torch.float64, device=DEV)
     x, info = cola.linalg.cg(S, b, tol=1e-10, max_iters=5000)
     Ad = L.to_dense() + torch.eye(n, device=DEV, dtype=torch.float64)
