@@ -870,6 +870,11 @@ def main():
         _capi.load()
         if rank == 0:
             line = configs.RUNNERS[args.config]()
+            roof = line.get("roofline")
+            if isinstance(roof, dict) and roof.get("bound") == "hbm" and "achieved_gbs" in roof:
+                roof["peak"], roof["peak_kind"] = peaks()
+                roof["unit"] = "GB/s"
+                roof["frac"] = roof["achieved_gbs"] / roof["peak"]
             if args.cpu_baseline:
                 line["cpu_reference"] = config_reference_cpu(args.config)
             print(json.dumps(line))

@@ -4,12 +4,15 @@
     python -m cola_gb300.cases_krylov c3b [--probes 64]
     python -m cola_gb300.cases_krylov c1
     python -m cola_gb300.cases_krylov c2 [--scale 0.5] [--schedule block|cluster16] [--matvec fp32|bf16]
+    python -m cola_gb300.cases_krylov c3a [--systems 16] [--steps 20]
 
 c5: 256-step Lanczos top-64 of Kronecker(A1, A2) + L (random-geometric-graph Laplacian); --scale < 1
 shrinks the factors and the graph (n = (1024 s)^2 rows) so that a capture stays small.  c3b: the
 Kronecker SLQ log-determinant with 64 probes and 100 steps.  c1: the 2048 dense CG solve.  Prints one
 JSON line per run with its wall time (CUDA-synchronised).  c2: the 7-point diffusion solve of 32
-right-hand sides to a 1e-8 FP64 residual with Jacobi (grid side 128 s).
+right-hand sides to a 1e-8 FP64 residual with Jacobi (grid side 128 s).  c3a: the first --systems
+of the 256 uneven dense RBF systems, FP32 CG to 1e-6 in one persistent launch, at most --steps steps
+(0: 2000).
 """
 from __future__ import annotations
 
@@ -22,7 +25,7 @@ import torch
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("config", choices=["c1", "c2", "c3b", "c5"])
+    ap.add_argument("config", choices=["c1", "c2", "c3a", "c3b", "c5"])
     ap.add_argument("--schedule", default="auto")
     ap.add_argument("--matvec", default="fp32", choices=["fp32", "bf16"])
     ap.add_argument("--scale", type=float, default=1.0)
@@ -31,6 +34,7 @@ def main(argv=None):
     ap.add_argument("--probes", type=int, default=64)
     ap.add_argument("--steps", type=int, default=0, help="Lanczos / SLQ steps (0: the configuration's)")
     ap.add_argument("--reorder", action="store_true", help="c5: store L in reverse Cuthill-McKee order")
+    ap.add_argument("--systems", type=int, default=256, help="c3a: how many of the 256 systems")
     args = ap.parse_args(argv)
 
     import cola_gb300 as cola
@@ -63,6 +67,13 @@ def main(argv=None):
 
         def run():
             return cola.linalg.stochastic_lanczos_quad(op, torch.log, max_iters=steps, tol=0.0, probes=Z)
+    elif args.config == "c3a":
+        from cola_gb300.linalg.batched import solve_dense_batched
+        mats, rhs, _ = W.rbf_systems(num=args.systems, device=dev)
+        steps = args.steps or 2000
+
+        def run():
+            return solve_dense_batched(mats, rhs, tol=1e-6, max_iters=steps)
     elif args.config == "c2":
         from cola_gb300.linalg.batched import BatchedCSR, solve_batched
         m = max(8, int(128 * args.scale))

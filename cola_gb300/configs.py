@@ -111,10 +111,13 @@ def c3a_rbf_batch(num=256, steps=1, warmup=1, tol=1e-6, max_iters=2000):
         r = (b.double() - A.double() @ x.double()).norm() / b.double().norm()
         worst = max(worst, float(r))
     bytes_sweep = sum(n * n * 4 for n, _, _ in meta)
+    # every CG step of system s reads its n_s^2 FP32 matrix once (the vectors add O(n_s) per step)
+    streamed = sum(n * n * 4 * int(k) for (n, _, _), k in zip(meta, iters.tolist()))
     out = {"config": f"rbf-uneven-{num}", "systems_per_s": num / t, "s_per_call": t,
            "mean_iters": float(iters.double().mean()), "max_iters": int(iters.max()),
            "converged": int((status == 1).sum()), "true_relres_first8_max": worst,
-           "matrix_bytes_per_sweep": bytes_sweep}
+           "matrix_bytes_per_sweep": bytes_sweep,
+           "roofline": {"bound": "hbm", "matrix_bytes_streamed": streamed, "achieved_gbs": streamed / t / 1e9}}
     # with FP64 residual refinement (no counterpart in the reference): every system to 1e-8, checked
     # with an FP64 residual on all of them
     (res2, t2) = _timed(lambda: solve_dense_batched(mats, rhs, tol=1e-8, max_iters=max_iters, refine=True),

@@ -10,6 +10,13 @@
 // busy as small systems finish.
 //
 // Layout: A_s row-major at vals + a_off[s]; vectors of system s at v_off[s] in concatenated buffers.
+// The search direction p of system s is kept in four copies, copy h shifted right by h elements
+// (copy h holds p[i] at index i + h, each copy 16-byte aligned).  A row whose first element sits h
+// floats past a 16-byte boundary is read as aligned 128-bit quads from its first boundary on, and
+// copy h then lines the matching p quads up on 16-byte boundaries as well, so the matvec issues only
+// 128-bit loads whatever n_s and the offsets are (the up to 3 + 3 elements before the first and
+// after the last whole quad are scalar).  The shifted copies cost 3 extra n_s-float writes a step
+// against the n_s^2 floats of A the step reads.
 #include <algorithm>
 #include <string>
 
@@ -28,7 +35,7 @@ struct DenseBatchArgs {
   const float* vals;
   const float* B;
   float* X;
-  float *r, *p, *ap;
+  float *r, *p4, *ap;  // p4: the four shifted copies of p, system s at copy_base(s)
   double* acc;  // [3][S]: <p, Ap>, |r|^2, |b|^2
   int* out_iters;
   int* out_status;
@@ -48,6 +55,7 @@ struct DState {
   __device__ __forceinline__ long long* prefix() const {  // S + 1 cost prefix sums of the active list
     return reinterpret_cast<long long*>(base + (size_t)2 * 8 * S + (size_t)(6 + 4) * 4 * S + 16);
   }
+  __device__ __forceinline__ long long* pbase() const { return prefix() + S + 1; }  // S offsets into p4
   __device__ __forceinline__ double& gamma(int s) const { return f64(0)[s]; }
   __device__ __forceinline__ double& mult(int s) const { return f64(1)[s]; }
   __device__ __forceinline__ float& alpha(int s) const { return f32(0)[s]; }
@@ -60,7 +68,82 @@ struct DState {
   __device__ __forceinline__ int* act() const { return i32(2); }
 };
 
-static size_t dense_batch_smem(int S) { return (size_t)2 * 8 * S + (size_t)10 * 4 * S + 16 + (size_t)8 * (S + 1) + 64; }
+static size_t dense_batch_smem(int S) {
+  return (size_t)2 * 8 * S + (size_t)10 * 4 * S + 16 + (size_t)8 * (S + 1) + (size_t)8 * S + 64;
+}
+
+// Length of one shifted copy of an n-vector: room for index n - 1 + 3, rounded to whole quads.
+__host__ __device__ __forceinline__ int64_t pcopy_len(int64_t n) { return ((n + 3) & ~int64_t(3)) + 4; }
+
+// Write element i of p (value v) into all four shifted copies.
+__device__ __forceinline__ void put_p(float* P0, int64_t cs, int i, float v) {
+  P0[i] = v;
+  P0[cs + i + 1] = v;
+  P0[2 * cs + i + 2] = v;
+  P0[3 * cs + i + 3] = v;
+}
+
+__device__ __forceinline__ float4 ld_a4(const float* q) {  // read-only A: no L1 allocation
+  float4 v;
+  asm("ld.global.nc.L1::no_allocate.v4.f32 {%0, %1, %2, %3}, [%4];"
+      : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+      : "l"(q));
+  return v;
+}
+
+__device__ __forceinline__ float dot4(float4 a, float4 b, float s) {
+  s = fmaf(a.x, b.x, s);
+  s = fmaf(a.y, b.y, s);
+  s = fmaf(a.z, b.z, s);
+  return fmaf(a.w, b.w, s);
+}
+
+// <A row, p> over one warp; the result is in every lane.  Ar: the row (ns floats); P0: copy 0 of p,
+// cs: the copy length.  Each lane keeps eight independent 128-bit loads of A in flight (4 KB per
+// warp, four 256-thread blocks per SM): the matvec streams HBM and is bound by how many bytes are in
+// flight, not by instructions (four quads per lane and 3 blocks reached 0.46 of the copy bandwidth,
+// four quads and 4 blocks 0.64, eight quads and 4 blocks 0.78; an L2 prefetch ahead of the loads
+// lowered each).
+__device__ __forceinline__ float row_dot(const float* __restrict__ Ar, const float* P0, int64_t cs, int ns,
+                                         int lane) {
+  const int h = (int)((reinterpret_cast<uintptr_t>(Ar) >> 2) & 3);  // floats past the last 16-byte boundary
+  int j0 = (4 - h) & 3;                                              // first element of the first whole quad
+  if (j0 > ns) j0 = ns;
+  const int nq = (ns - j0) >> 2;
+  const int jt = j0 + 4 * nq;
+  const float* Aq = Ar + j0;              // 16-byte aligned
+  const float* Pq = P0 + h * cs + j0 + h;  // copy h: p[j] at index j + h; j0 + h is 0 or 4
+  float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+  int q = lane;
+  for (; q + 224 < nq; q += 256) {
+    const float4 a0 = ld_a4(Aq + 4 * q), a1 = ld_a4(Aq + 4 * (q + 32));
+    const float4 a2 = ld_a4(Aq + 4 * (q + 64)), a3 = ld_a4(Aq + 4 * (q + 96));
+    const float4 a4 = ld_a4(Aq + 4 * (q + 128)), a5 = ld_a4(Aq + 4 * (q + 160));
+    const float4 a6 = ld_a4(Aq + 4 * (q + 192)), a7 = ld_a4(Aq + 4 * (q + 224));
+    s0 = dot4(a4, *reinterpret_cast<const float4*>(Pq + 4 * (q + 128)), s0);
+    s1 = dot4(a5, *reinterpret_cast<const float4*>(Pq + 4 * (q + 160)), s1);
+    s2 = dot4(a6, *reinterpret_cast<const float4*>(Pq + 4 * (q + 192)), s2);
+    s3 = dot4(a7, *reinterpret_cast<const float4*>(Pq + 4 * (q + 224)), s3);
+    const float4 p0 = *reinterpret_cast<const float4*>(Pq + 4 * q);
+    const float4 p1 = *reinterpret_cast<const float4*>(Pq + 4 * (q + 32));
+    const float4 p2 = *reinterpret_cast<const float4*>(Pq + 4 * (q + 64));
+    const float4 p3 = *reinterpret_cast<const float4*>(Pq + 4 * (q + 96));
+    s0 = dot4(a0, p0, s0);
+    s1 = dot4(a1, p1, s1);
+    s2 = dot4(a2, p2, s2);
+    s3 = dot4(a3, p3, s3);
+  }
+  for (; q + 96 < nq; q += 128) {
+    s0 = dot4(ld_a4(Aq + 4 * q), *reinterpret_cast<const float4*>(Pq + 4 * q), s0);
+    s1 = dot4(ld_a4(Aq + 4 * (q + 32)), *reinterpret_cast<const float4*>(Pq + 4 * (q + 32)), s1);
+    s2 = dot4(ld_a4(Aq + 4 * (q + 64)), *reinterpret_cast<const float4*>(Pq + 4 * (q + 64)), s2);
+    s3 = dot4(ld_a4(Aq + 4 * (q + 96)), *reinterpret_cast<const float4*>(Pq + 4 * (q + 96)), s3);
+  }
+  for (; q < nq; q += 32) s0 = dot4(ld_a4(Aq + 4 * q), *reinterpret_cast<const float4*>(Pq + 4 * q), s0);
+  if (lane < j0) s1 = fmaf(Ar[lane], P0[lane], s1);
+  if (lane < ns - jt) s2 = fmaf(Ar[jt + lane], P0[jt + lane], s2);
+  return warp_sum((s0 + s1) + (s2 + s3));
+}
 
 // Build the active list and its cost prefix (rows * n per system for the matvec, rows for vectors).
 __device__ __forceinline__ int d_build(const DenseBatchArgs& a, const DState& m, bool by_cost) {
@@ -133,7 +216,7 @@ __device__ __forceinline__ void d_warp_rows(const DenseBatchArgs& a, const DStat
   }
 }
 
-__global__ void __launch_bounds__(kDBThreads) k_dense_batched_cg(const __grid_constant__ DenseBatchArgs a) {
+__global__ void __launch_bounds__(kDBThreads, 4) k_dense_batched_cg(const __grid_constant__ DenseBatchArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   DState m{smem_raw, a.S};
   const int lane = threadIdx.x & 31;
@@ -145,6 +228,13 @@ __global__ void __launch_bounds__(kDBThreads) k_dense_batched_cg(const __grid_co
   for (int s = threadIdx.x; s < S; s += blockDim.x) {
     m.active(s) = a.sizes[s] > 0;
     m.it(s) = 0;
+  }
+  if (threadIdx.x == 0) {
+    long long off = 0;
+    for (int s = 0; s < S; ++s) {
+      m.pbase()[s] = off;
+      off += 4 * pcopy_len(a.sizes[s]);
+    }
   }
   // |b|^2 (elementwise partition by rows)
   int nact = d_build(a, m, false);
@@ -171,10 +261,12 @@ __global__ void __launch_bounds__(kDBThreads) k_dense_batched_cg(const __grid_co
                 [&](int s, int r0, int r1) {
                   const int64_t o = a.v_off[s];
                   const double mu = m.mult(s);
+                  float* P0 = a.p4 + m.pbase()[s];
+                  const int64_t cs = pcopy_len(a.sizes[s]);
                   for (int i = r0 + lane; i < r1; i += 32) {
                     const float rv = (mu < 1e-40) ? a.B[o + i] / 1e-40f : (float)(a.B[o + i] / mu);
                     a.r[o + i] = rv;
-                    a.p[o + i] = rv;
+                    put_p(P0, cs, i, rv);
                     a.X[o + i] = 0.f;
                     part += (double)rv * rv;
                   }
@@ -210,22 +302,13 @@ __global__ void __launch_bounds__(kDBThreads) k_dense_batched_cg(const __grid_co
                   [&](int s, int r0, int r1) {
                     const int ns = a.sizes[s];
                     const float* A = a.vals + a.a_off[s];
-                    const float* p = a.p + a.v_off[s];
+                    const float* P0 = a.p4 + m.pbase()[s];
+                    const int64_t cs = pcopy_len(ns);
                     for (int row = r0; row < r1; ++row) {
-                      const float* Ar = A + (int64_t)row * ns;
-                      float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
-                      int j = lane;
-                      for (; j + 96 < ns; j += 128) {
-                        s0 += Ar[j] * p[j];
-                        s1 += Ar[j + 32] * p[j + 32];
-                        s2 += Ar[j + 64] * p[j + 64];
-                        s3 += Ar[j + 96] * p[j + 96];
-                      }
-                      for (; j < ns; j += 32) s0 += Ar[j] * p[j];
-                      const float v = warp_sum((s0 + s1) + (s2 + s3));
+                      const float v = row_dot(A + (int64_t)row * ns, P0, cs, ns, lane);
                       if (lane == 0) {
                         a.ap[a.v_off[s] + row] = v;
-                        part += (double)p[row] * v;
+                        part += (double)P0[row] * v;
                       }
                     }
                   },
@@ -252,8 +335,9 @@ __global__ void __launch_bounds__(kDBThreads) k_dense_batched_cg(const __grid_co
                   [&](int s, int r0, int r1) {
                     const int64_t o = a.v_off[s];
                     const float al = m.alpha(s);
+                    const float* P0 = a.p4 + m.pbase()[s];
                     for (int i = r0 + lane; i < r1; i += 32) {
-                      a.X[o + i] += al * a.p[o + i];
+                      a.X[o + i] += al * P0[i];
                       const float rv = a.r[o + i] - al * a.ap[o + i];
                       a.r[o + i] = rv;
                       part += (double)rv * rv;
@@ -289,7 +373,9 @@ __global__ void __launch_bounds__(kDBThreads) k_dense_batched_cg(const __grid_co
                 [&](int s, int r0, int r1) {
                   const int64_t o = a.v_off[s];
                   const float b = m.beta(s);
-                  for (int i = r0 + lane; i < r1; i += 32) a.p[o + i] = a.r[o + i] + b * a.p[o + i];
+                  float* P0 = a.p4 + m.pbase()[s];
+                  const int64_t cs = pcopy_len(a.sizes[s]);
+                  for (int i = r0 + lane; i < r1; i += 32) put_p(P0, cs, i, a.r[o + i] + b * P0[i]);
                 },
                 [&](int) {});
     if (!grid_sync(a.gb)) return;
@@ -320,7 +406,7 @@ extern "C" int colagb_cg_dense_batched_workspace_bytes(int64_t num_systems, int6
   if (!bytes || num_systems < 0 || total_rows < 0) return fail(COLAGB_ERR_INVALID, "dense batched CG: bad arguments");
   Bump ws = Bump::measuring();
   ws.take<float>(total_rows);
-  ws.take<float>(total_rows);
+  ws.take<float>(4 * (total_rows + 8 * num_systems));  // >= 4 * sum of pcopy_len(n_s)
   ws.take<float>(total_rows);
   ws.take<double>(3 * (num_systems > 0 ? num_systems : 1));
   ws.take<unsigned int>(8);
@@ -351,7 +437,7 @@ extern "C" int colagb_cg_dense_batched_solve(int64_t num_systems, const int32_t*
   a.B = B;
   a.X = X;
   a.r = ws.take<float>(total_rows);
-  a.p = ws.take<float>(total_rows);
+  a.p4 = ws.take<float>(4 * (total_rows + 8 * num_systems));
   a.ap = ws.take<float>(total_rows);
   a.acc = ws.take<double>(3 * num_systems);
   unsigned int* bar = ws.take<unsigned int>(8);

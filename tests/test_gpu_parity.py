@@ -675,6 +675,30 @@ def test_dense_batched_uneven_matches_per_system_reference_loop():
     assert torch.all(status == 1)
 
 
+def test_dense_batched_quad_loads_every_row_alignment():
+    """Sizes whose rows start at every offset within a 16-byte quad and are long enough for the
+    unrolled 128-bit loop (n >= 512), next to tiny ones; each system against the oracle's CG and an
+    FP64 solve."""
+    from cola_gb300.linalg.batched import solve_dense_batched
+    rng = np.random.default_rng(11)
+    mats, rhs, np_mats = [], [], []
+    for n in (515, 3, 1026, 2051, 7, 1, 2):
+        Q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+        lam = np.exp(rng.uniform(np.log(0.5), np.log(5.0), n))
+        A = ((Q * lam) @ Q.T).astype(np.float32)
+        b = rng.standard_normal(n).astype(np.float32)
+        np_mats.append((A, b))
+        mats.append(T(A))
+        rhs.append(T(b))
+    sols, iters, status = solve_dense_batched(mats, rhs, tol=1e-6, max_iters=400)
+    for (A, b), x, k in zip(np_mats, sols, iters.tolist()):
+        xo, ko, info = oracle.cg_solve(oracle.dense_op(A), b, tol=1e-6, max_iters=400)
+        assert abs(k - ko) <= 0.05 * ko + 2, (A.shape[0], k, ko)
+        xs = np.linalg.solve(A.astype(np.float64), b.astype(np.float64))
+        assert rel(x, xs) < 1e-4, A.shape[0]
+    assert torch.all(status == 1)
+
+
 def test_batched_ir_matches_oracle_iteration_structure():
     """The device restarted-refinement loop and the oracle's restatement need comparable inner iterations."""
     from cola_gb300.workloads import diffusion_family_2d
