@@ -26,6 +26,7 @@ namespace colagb {
 
 constexpr int kDBThreads = 256;
 constexpr int kDBMaxSystems = 1024;
+constexpr long long kDBChunk = 16384;  // matvec work claimed at a time: ~64 KB of A
 
 struct DenseBatchArgs {
   int S;
@@ -37,6 +38,7 @@ struct DenseBatchArgs {
   float* X;
   float *r, *p4, *ap;  // p4: the four shifted copies of p, system s at copy_base(s)
   double* acc;  // [3][S]: <p, Ap>, |r|^2, |b|^2
+  unsigned long long* claim;  // the matvec's chunk counter (zero at every phase start)
   int* out_iters;
   int* out_status;
   double tol;
@@ -216,6 +218,46 @@ __device__ __forceinline__ void d_warp_rows(const DenseBatchArgs& a, const DStat
   }
 }
 
+// The matvec's rows in chunks of about kDBChunk matrix elements, claimed from a counter in order, so
+// that warps whose loads return sooner (SMs nearer the data, less contended) take more chunks and all
+// finish together at the grid barrier.  A chunk holds the rows whose cost starts fall inside it.
+// Each warp claims its next chunk before working on the current one, hiding the atomic's latency.
+// f(s, r0, r1) per (system, row range); flush(s) when the warp moves on to another system and at the
+// end.
+template <class RowFn, class Flush>
+__device__ __forceinline__ void d_claim_rows(const DenseBatchArgs& a, const DState& m, int nact, RowFn f,
+                                             Flush flush) {
+  if (nact == 0) return;
+  const int lane = threadIdx.x & 31;
+  const long long T = m.prefix()[nact];
+  const long long nch = (T + kDBChunk - 1) / kDBChunk;
+  unsigned long long c = 0;
+  if (lane == 0) c = atomicAdd(a.claim, 1ull);
+  c = __shfl_sync(0xffffffffu, c, 0);
+  int last = -1;
+  while ((long long)c < nch) {
+    unsigned long long next = 0;
+    if (lane == 0) next = atomicAdd(a.claim, 1ull);
+    int k0, r0, k1, r1;
+    d_locate(a, m, nact, (long long)c * kDBChunk, true, k0, r0);
+    const long long e = ((long long)c + 1) * kDBChunk;
+    d_locate(a, m, nact, e < T ? e : T, true, k1, r1);
+    int k = k0, row = r0;
+    while (k < k1 || (k == k1 && row < r1)) {
+      if (k >= nact) break;
+      const int s = m.act()[k];
+      const int end = (k == k1) ? r1 : a.sizes[s];
+      if (s != last && last >= 0) flush(last);
+      last = s;
+      f(s, row, end);
+      k += 1;
+      row = 0;
+    }
+    c = __shfl_sync(0xffffffffu, next, 0);
+  }
+  if (last >= 0) flush(last);
+}
+
 __global__ void __launch_bounds__(kDBThreads, 4) k_dense_batched_cg(const __grid_constant__ DenseBatchArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   DState m{smem_raw, a.S};
@@ -298,7 +340,7 @@ __global__ void __launch_bounds__(kDBThreads, 4) k_dense_batched_cg(const __grid
     // A: Ap = A p (warp per row), <p, Ap>
     {
       double part = 0.0;
-      d_warp_rows(a, m, nact, true,
+      d_claim_rows(a, m, nact,
                   [&](int s, int r0, int r1) {
                     const int ns = a.sizes[s];
                     const float* A = a.vals + a.a_off[s];
@@ -318,6 +360,7 @@ __global__ void __launch_bounds__(kDBThreads, 4) k_dense_batched_cg(const __grid
                   });
     }
     if (!grid_sync(a.gb)) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *a.claim = 0ull;  // next used after two more grid barriers
     for (int j = threadIdx.x; j < nact; j += blockDim.x) {
       const int s = m.act()[j];
       const double pap = __ldcg(acc_pap + s);
@@ -410,6 +453,7 @@ extern "C" int colagb_cg_dense_batched_workspace_bytes(int64_t num_systems, int6
   ws.take<float>(total_rows);
   ws.take<double>(3 * (num_systems > 0 ? num_systems : 1));
   ws.take<unsigned int>(8);
+  ws.take<unsigned long long>(1);
   *bytes = ws.peak;
   return COLAGB_OK;
 }
@@ -441,6 +485,7 @@ extern "C" int colagb_cg_dense_batched_solve(int64_t num_systems, const int32_t*
   a.ap = ws.take<float>(total_rows);
   a.acc = ws.take<double>(3 * num_systems);
   unsigned int* bar = ws.take<unsigned int>(8);
+  a.claim = ws.take<unsigned long long>(1);
   a.out_iters = per_system_iters;
   a.out_status = per_system_status;
   a.tol = tol;
@@ -459,6 +504,7 @@ extern "C" int colagb_cg_dense_batched_solve(int64_t num_systems, const int32_t*
   const int nb = num_sms() * (occ < 4 ? occ : 4);
   a.gb.nblocks = (unsigned)nb;
   COLAGB_CUDA(cudaMemsetAsync(bar, 0, 8 * sizeof(unsigned int), st));
+  COLAGB_CUDA(cudaMemsetAsync(a.claim, 0, sizeof(unsigned long long), st));
   COLAGB_CUDA(cudaMemsetAsync(a.acc, 0, 3 * num_systems * sizeof(double), st));
   void* args[] = {&a};
   COLAGB_CUDA(cudaLaunchCooperativeKernel((const void*)k_dense_batched_cg, dim3(nb), dim3(kDBThreads), args, smem, st));
