@@ -6,8 +6,9 @@
 //   steps while |r| > tol_eff and k < max_iters, alpha/beta zeroed once |r| < 1e-40,
 //   solution scaled back by |b|.
 // Systems converge independently (per-system masks); the rows of the still-active systems are
-// re-partitioned over all warps at every phase, balanced by matvec cost (n_s per row), so warps stay
-// busy as small systems finish.
+// re-partitioned over all warps at every phase, so warps stay busy as small systems finish: the
+// matvec's rows in chunks of about equal cost (n_s per row) claimed from a counter, the vector
+// phases' rows split evenly.
 //
 // Layout: A_s row-major at vals + a_off[s]; vectors of system s at v_off[s] in concatenated buffers.
 // The search direction p of system s is kept in four copies, copy h shifted right by h elements
