@@ -4,6 +4,7 @@ from .arnoldi import arnoldi, gmres
 from .batched import BatchedCSR, solve_batched
 from .inverse import IterativeOperatorWInfo, cg, inv, solve
 from .lanczos import eig, eigmax, eigmin, lanczos, lanczos_eigs, run_lanczos, tridiag_eigh
+from .preconditioning import NystromPrecond, NystromPrecondLazy, get_nys_approx
 from .prng import PRNGKey, next_key, randn, sha_hash
 from .batched import solve_dense_batched
 from .unary import (LanczosUnary, apply_unary, diag, exact_diag, exp, hutchinson_diag_estimate, log, logdet, pow,
@@ -15,4 +16,5 @@ __all__ = [
     "run_lanczos", "tridiag_eigh", "PRNGKey", "next_key", "randn", "sha_hash", "LanczosUnary", "apply_unary",
     "diag", "exact_diag", "hutchinson_diag_estimate", "log", "logdet", "slogdet", "stochastic_lanczos_quad",
     "trace", "BatchedCSR", "solve_batched", "solve_dense_batched", "exp", "sqrt", "pow",
+    "NystromPrecond", "NystromPrecondLazy", "get_nys_approx",
 ]

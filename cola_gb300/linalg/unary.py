@@ -106,7 +106,11 @@ def exp(A: O.LinearOperator, alg: Algorithm = Auto()):
 
 
 def sqrt(A: O.LinearOperator, alg: Algorithm = Auto()):
-    """Matrix square root of a PSD operator (unary.py:265-280); Diagonal / ScalarMul / Identity exactly."""
+    """Matrix square root of a PSD operator (unary.py:265-280); Diagonal / ScalarMul / Identity exactly,
+    a Nystrom preconditioner in its own form (preconditioners.py:163-170)."""
+    from .preconditioning import NystromPrecondLazy, sqrt as nystrom_sqrt
+    if isinstance(A, NystromPrecondLazy):
+        return nystrom_sqrt(A)
     if isinstance(A, O.Diagonal):
         return O.Diagonal(torch.sqrt(A.diag))
     if isinstance(A, O.ScalarMul):

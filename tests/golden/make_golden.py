@@ -245,10 +245,33 @@ def case_arnoldi_gmres():
     save("gmres_dense_multi_f32", A=A.astype(np.float32), B=B, max_iters=25, tol=1e-6, x=X, iterations=info["iterations"])
 
 
+def case_nystrom():
+    """The reference's Nystrom preconditioner (preconditioners.py:88-190) on its own test matrices
+    (tests/algorithms/test_cg.py: spectrum 1 - x^0.75 on 25 points, rank 5, mu 0), its sqrt and
+    inverse, and run_batched_cg with it as P."""
+    from cola.linalg.preconditioning.preconditioners import NystromPrecond, inverse as nys_inverse, sqrt as nys_sqrt
+    from cola.utils.utils_for_tests import generate_pd_from_diag, generate_spectrum
+    diag = generate_spectrum(coeff=0.75, scale=1.0, size=25, dtype=np.float32)
+    A32 = np.array(generate_pd_from_diag(diag, dtype=diag.dtype, seed=21), dtype=np.float32)
+    for dt in (np.float32, np.float64):
+        A = A32.astype(dt)
+        At = torch.from_numpy(A)
+        P = NystromPrecond(cola.ops.Dense(At), rank=5, mu=0, eps=1e-8)
+        Pdef = NystromPrecond(cola.ops.Dense(At), rank=5)  # mu = 1e-7, adjust_mu = True
+        rhs = np.ones((25, 5), dtype=dt)
+        x, _, k, _ = run_batched_cg(cola.ops.Dense(At), torch.from_numpy(rhs), torch.zeros(25, 5, dtype=At.dtype), 100,
+                                    1e-8, P, pbar=False)
+        tag = "f32" if dt == np.float32 else "f64"
+        save(f"nystrom_{tag}", A=A, rank=5, eps=1e-8, Lambda=P.Lambda, P=P.to_dense(), P_default=Pdef.to_dense(),
+             P_sqrt=nys_sqrt(P).to_dense(), P_inv=nys_inverse(P).to_dense(), rhs=rhs, x=x, k=int(k),
+             eigmax=P.preconditioned_eigmax, eigmin=P.preconditioned_eigmin)
+
+
 if __name__ == "__main__":
     import os
     cases = [case_cg_dense, case_cg_multi_jacobi_x0, case_cg_sparse, case_cg_repeated_eig, case_lanczos, case_eig,
-             case_lanczos_unary, case_logdet_slq, case_kron_slq, case_slq_tbd, case_ops, case_arnoldi_gmres]
+             case_lanczos_unary, case_logdet_slq, case_kron_slq, case_slq_tbd, case_ops, case_arnoldi_gmres,
+             case_nystrom]
     only = [x for x in os.environ.get("GOLDEN_ONLY", "").split(",") if x]
     for fn in cases:
         if not only or fn.__name__ in only:

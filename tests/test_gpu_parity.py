@@ -295,6 +295,30 @@ def test_cg_general_preconditioner_and_shift():
     assert info2["fused"] and rel(x2, xo) < 1e-8
 
 
+@pytest.mark.parametrize("tag", ["f32", "f64"])
+def test_nystrom_preconditioner_matches_reference(golden, tag):
+    """NystromPrecond on the device operator path against the reference's own NystromPrecond (its
+    test matrices, rank 5): Lambda, the dense P (mu = 0 and the defaults), sqrt and inverse, and CG
+    with P (run_batched_cg, tol 1e-8)."""
+    from cola_gb300.linalg import NystromPrecond, sqrt
+    from cola_gb300.linalg.preconditioning import inverse
+    g = golden(f"nystrom_{tag}")
+    f64 = tag == "f64"
+    tol = 1e-9 if f64 else 2e-5
+    A = cola.ops.Dense(T(g["A"]))
+    P = NystromPrecond(A, rank=int(g["rank"]), mu=0, eps=float(g["eps"]))
+    assert rel(P.Lambda, g["Lambda"]) < tol
+    assert rel(P.to_dense(), g["P"]) < tol
+    assert rel(NystromPrecond(A, rank=int(g["rank"])).to_dense(), g["P_default"]) < tol
+    assert rel(sqrt(P).to_dense(), g["P_sqrt"]) < tol
+    assert rel(inverse(P).to_dense(), g["P_inv"]) < tol
+    assert abs(float(P.preconditioned_eigmax) - float(g["eigmax"])) < tol
+    x, info = cola.linalg.inverse.cg(A, T(g["rhs"]), P=P, tol=1e-8, max_iters=100)
+    assert not info["fused"]
+    assert rel(x, g["x"]) < (1e-9 if f64 else 1e-5)
+    assert abs(int(info["iterations"]) - int(g["k"])) <= (1 if f64 else 3)
+
+
 def test_cg_edge_cases():
     A = cola.PSD(cola.ops.Dense(torch.tensor([[2.0]], device=DEV)))
     x, info = cola.linalg.inverse.cg(A, torch.tensor([4.0], device=DEV), tol=1e-8)
